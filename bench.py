@@ -1,0 +1,319 @@
+"""Benchmark of the GB300 DPD engine: bead-steps/s on the 128^3 polymer-solvent box.
+
+Workload (default): 128x128x128 periodic box at density 3 = 6,291,456 beads, types W/H/T,
+5% of the beads in H-T-T-T-T-T chains (Hookean k=128 r0=0.5, angle k=20 theta0=0),
+a_WW=a_HH=a_TT=25, a_WH=35, a_WT=a_HT=75, gamma=4.5, dt=0.01, FP32 engine.  Synthetic data:
+seeded uniform positions, Gaussian kT=1 velocities.  A "step" is one DPD timestep of the
+whole box.  The state (~300 MB of bead payload) is larger than L2, so no flush is needed.
+
+  value     bead-steps/s with the state resident on the GPU: K steps timed with CUDA events
+            on the engine's stream (graph replays), barrier + synchronize on both sides.
+  e2e       the same metric through the C ABI with host buffers: Attach (upload) + Run(K) +
+            read back x, v, f, timed on the host.
+  roofline  the force kernel (dominant): algorithmic bytes per launch (1,180 B per
+            bead-step x beads) / its average CUDA-event duration, against the measured HBM
+            copy bandwidth.
+  cpu_baseline  the oracle (C restatement of the reference's FP64 half-step engine) on all
+            host cores, on a bounded sample of the same recipe.
+
+--impl reference times the reference's CPU implementation of the path (the oracle port;
+the reference sources are not present where this runs) on the same recipe and metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "poets-dpd_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+import pdpd_world as W  # noqa: E402
+
+ALGO_BYTES = {"fp32": 1180.0, "fp64": 2188.0}  # per bead-step, half-shell cell-list stream model
+COMPULSORY_BYTES = 88.0
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    # name: (box side, chain fraction, seed, dt)
+    "polymer128": (128, 0.05, 3, 0.01),
+    "polymer32": (32, 0.10, 2, 0.01),
+    "water8": (8, 0.0, 1, 0.02),
+}
+
+
+def make_world(name, side=None):
+    L, frac, seed, dt = WORKLOADS[name]
+    L = side or L
+    if frac == 0.0:
+        return W.make_water(L, seed=seed, dt=dt)
+    return W.make_polymer_box(L, chain_fraction=frac, seed=seed, dt=dt)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def oracle_rate(world, max_seconds=12.0, max_steps=200, threads=None):
+    """Oracle (C port of the reference's FP64 half-step engine) bead-steps/s on all host
+    cores: runs steps until max_seconds or max_steps."""
+    import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    ow = O.OracleWorld(world)
+    ow.run(1, nthreads=threads)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < max_seconds:
+        ow.run(1, nthreads=threads)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return world.n_beads * steps / dt, threads, steps, dt
+
+
+def dist_setup(n_gpus):
+    rank, world_size = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if world_size > 1:
+        import torch
+        import torch.distributed as dist
+
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world_size, local
+    return 0, 1, 0
+
+
+def run_reference_arm(args):
+    rank, world_size, _ = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    side = args.ref_side
+    world = make_world(args.workload, side=side)
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    ow = O.OracleWorld(world)
+    for _ in range(args.warmup):
+        ow.run(1, nthreads=threads)
+    t0 = time.perf_counter()
+    ow.run(args.steps, nthreads=threads)
+    dt = time.perf_counter() - t0
+    rate = world.n_beads * args.steps / dt
+    L = WORKLOADS[args.workload][0]
+    line = {
+        "impl": "reference", "metric": "bead-steps/s", "value": rate, "unit": "bead-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {L}^3 polymer-solvent box recipe",
+                   "sample": f"{side}^3 box of the same recipe ({world.n_beads} beads)",
+                   "parallelism": "replicas only"},
+        "cpu_baseline": {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{side}^3 box, {world.n_beads} beads, {args.steps} steps"},
+        "e2e": {"value": rate, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_engine_arm(args):
+    import torch
+
+    import pdpd_engine as E
+
+    rank, world_size, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    world = make_world(args.workload)
+    n = world.n_beads
+    eng = E.GB300DPDEngine(args.precision, device=local)
+
+    # --- e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
+    w_e2e = world.copy()
+    eng.Attach(w_e2e)
+    eng.Run(args.warmup)
+    torch.cuda.synchronize()
+    w_e2e = world.copy()
+    t0 = time.perf_counter()
+    eng.Attach(w_e2e)
+    eng.Run(args.steps)  # Run() reads x, v, f back into the host world
+    e2e_dt = time.perf_counter() - t0
+    h2d = n * (9 * 8 + 4)
+    bb, _, _, ab, _, _ = w_e2e.flat_bonds()
+    h2d += (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
+    d2h = n * 9 * 8
+    e2e_rate = n * args.steps / e2e_dt
+
+    # --- value: resident state, graph replays, CUDA events on the engine's stream
+    w = world.copy()
+    eng.Attach(w)
+    eng.run_async(args.warmup)
+    eng.sync()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = eng.kernel_launches()
+    with ClockSampler(local) as clocks:
+        time.sleep(0.3)
+        ev0.record(stream)
+        eng.run_async(args.steps)
+        ev1.record(stream)
+        eng.sync()
+        torch.cuda.synchronize()
+        time.sleep(0.2)
+    launches = eng.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world_size > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    value = world_size * n * args.steps / (ms / 1e3)
+
+    # --- dominant kernel: per-phase CUDA-event times over the same number of steps
+    phases = eng.profile_run(args.steps)
+    force_ms = phases["force_ms"] / max(1, phases["force_launches"])
+    peak, peak_kind = measured_peaks()
+    algo = ALGO_BYTES[args.precision] * n
+    achieved = algo / (force_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "force_kernel_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tj = json.load(fh)
+        key = f"{args.precision}_bytes_per_bead_step"
+        if key in tj:
+            traffic = tj[key] * n
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        sample_side = args.ref_side
+        rate, threads, steps, dt = oracle_rate(make_world(args.workload, side=sample_side))
+        cpu = {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{sample_side}^3 box of the same recipe, {steps} steps in {dt:.1f} s"}
+    L = WORKLOADS[args.workload][0]
+    line = {
+        "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {L}^3 box, density 3, {n} beads, "
+                               f"{WORKLOADS[args.workload][1]:.0%} H-T5 chains, {args.precision}",
+                   "beads": n, "precision": args.precision, "l2": "state > L2 (no flush)",
+                   "parallelism": "replicas only" if world_size > 1 else "single GPU"},
+        "e2e": {"value": e2e_rate, "unit": "bead-steps/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps,
+                "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "force", "kernel_ms": force_ms,
+                     "algo_bytes_per_bead_step": ALGO_BYTES[args.precision],
+                     "peak_source": peak_kind,
+                     "compulsory_frac": COMPULSORY_BYTES * n / (force_ms / 1e3) / 1e9 / peak},
+        "phases_ms_per_step": {"force": force_ms,
+                               "sort": phases["sort_ms"] / max(1, phases["sort_launches"])},
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="polymer128", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--ref-side", type=int, default=32,
+                    help="box side of the bounded CPU sample (same recipe)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_engine_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/* pdpd_gpu.h -- C ABI of the GB300 DPD engine.
+ *
+ * This is the boundary between the reference's engine plug-in API and the GPU runtime.
+ * The reference's plug-in interface is the C++ class DPDEngine
+ * (include/dpd/core/dpd_engine.hpp:10-216 in the reference); the adapter
+ * poets-dpd_gb300/host/gb300_dpd_engine.hpp subclasses it and forwards every call here.
+ * Each entry point below names the DPDEngine member it serves.
+ *
+ * Conventions: every call returns PDPD_OK (0) or a positive PDPD_E_* status; no exception
+ * or C++ type crosses this boundary.  After a failure, pdpd_last_error() returns a
+ * human-readable message.  All pointers are host pointers; arrays are indexed by bead id
+ * (the bead's index in WorldState::beads).  Functions are not thread-safe per engine: one
+ * caller thread per engine, as in the reference (the interval callback runs on that thread).
+ */
+#ifndef PDPD_GPU_H
+#define PDPD_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDPD_ABI_VERSION 1
+
+enum pdpd_status {
+    PDPD_OK = 0,
+    PDPD_E_INVALID = 1,      /* bad argument, or a world that fails validation */
+    PDPD_E_UNSUPPORTED = 2,  /* the world uses a feature this engine does not support */
+    PDPD_E_CUDA = 3,         /* CUDA runtime error (message has the CUDA error string) */
+    PDPD_E_STATE = 4,        /* call out of order, e.g. Run before Attach */
+    PDPD_E_BOND_SNAPPED = 5, /* a Hookean bond grew beyond the maximum bond length */
+    PDPD_E_BEAD_LOST = 6,    /* a bead position or velocity became non-finite */
+    PDPD_E_NOMEM = 7         /* device memory exhausted, or a fixed budget exceeded */
+};
+
+enum pdpd_precision {
+    PDPD_FP32 = 0, /* FP32 forces; positions as integer cell + FP32 offset */
+    PDPD_FP64 = 1  /* FP64 everywhere, same operation order as the reference's FP64 engines */
+};
+
+/* A world in flat form: the fields of the reference's WorldState
+ * (include/dpd/core/dpd_state.hpp:245-264) that the integrator reads, with the polymer
+ * templates expanded into per-bond lists.  x/v/f point at the first bead's vector; bead i's
+ * vector starts bead_stride_bytes * i bytes later (0 means packed, 24 bytes), so the adapter
+ * can pass &state.beads[0].x[0] with stride sizeof(Bead) and no copy. */
+typedef struct pdpd_world {
+    int32_t box[3];                /* integer box sides (WorldState::box) */
+    double dt;                     /* WorldState::dt */
+    double lambda;                 /* WorldState::lambda (the half-step integrator uses 0.5) */
+    uint64_t seed;                 /* WorldState::seed */
+    int64_t t;                     /* WorldState::t */
+    uint32_t n_bead_types;
+    const double *conservative;    /* n_bead_types^2 row-major, a_ij */
+    const double *dissipative;     /* n_bead_types^2 row-major, gamma_ij */
+    const uint8_t *stationary;     /* n_bead_types flags, may be NULL */
+    uint32_t n_beads;
+    const uint32_t *hash;          /* BeadHash::hash of each bead (dpd_state.hpp:52-60) */
+    const double *x, *v, *f;       /* bead vectors, see bead_stride_bytes */
+    size_t bead_stride_bytes;
+    uint32_t n_bonds;              /* Hookean bonds, polymer-major, polymer-type order */
+    const uint32_t *bond_beads;    /* 2*n_bonds: head, tail bead ids */
+    const double *bond_kappa, *bond_r0;
+    uint32_t n_angles;             /* angle bonds (BondPair), polymer-major */
+    const uint32_t *angle_beads;   /* 3*n_angles: head, middle, tail bead ids */
+    const double *angle_kappa, *angle_theta0;
+} pdpd_world;
+
+/* Phase timings, same meaning as DPDEngine::timings_t (dpd_engine.hpp:38-46); -1 = unset. */
+typedef struct pdpd_timings {
+    double compile, aquire, configure, execute_to_first_bead, execute_to_last_bead,
+        perf_counters;
+} pdpd_timings;
+
+typedef struct pdpd_engine pdpd_engine;
+
+/* Interval callback for pdpd_run_intervals: called on the caller's thread after the
+ * interval's state has been written to the host arrays.  Return nonzero to continue. */
+typedef int (*pdpd_interval_fn)(void *user, int64_t t);
+
+/* Create/destroy an engine (DPDEngineFactory::create, dpd_engine.hpp:244-252).
+ * device < 0 uses the current CUDA device. */
+int pdpd_create(int precision, int device, pdpd_engine **out);
+void pdpd_destroy(pdpd_engine *e);
+
+/* Message for the last failed call on e (or on a NULL engine: the last failed create or
+ * can_support on this thread).  Never NULL. */
+const char *pdpd_last_error(const pdpd_engine *e);
+
+/* DPDEngine::CanSupport (dpd_engine.hpp:57-128): PDPD_OK, or PDPD_E_UNSUPPORTED /
+ * PDPD_E_INVALID with the reason in reason[0..reason_len).  Host-only, touches no GPU. */
+int pdpd_can_support(const pdpd_world *w, char *reason, size_t reason_len);
+
+/* DPDEngine::GetMaxBondLength (dpd_engine.hpp:130): the length beyond which a Hookean bond
+ * counts as snapped (2.0, as naive_dpd_engine_half_step.hpp:96). */
+double pdpd_max_bond_length(void);
+
+/* DPDEngine::Attach (dpd_engine.hpp:177): copy the world to the device and build its cell
+ * list.  w == NULL detaches.  The host arrays are not retained. */
+int pdpd_attach(pdpd_engine *e, const pdpd_world *w);
+
+/* Batched attach: n independent worlds share one device arena and are stepped together;
+ * each keeps its own box, parameters, seed and t.  Bead ids are per world. */
+int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *worlds, uint32_t n_worlds);
+
+/* DPDEngine::Run(nSteps) (dpd_engine.hpp:185): advance every attached world by n_steps.
+ * Blocks until the device has finished and reports device-side errors. */
+int pdpd_run(pdpd_engine *e, uint32_t n_steps);
+
+/* Enqueue n_steps on the engine's stream and return at once (no error check). */
+int pdpd_run_async(pdpd_engine *e, uint32_t n_steps);
+
+/* Wait for queued work and report device-side errors. */
+int pdpd_sync(pdpd_engine *e);
+
+/* The engine's CUDA stream (a cudaStream_t), for timing with events. */
+void *pdpd_stream(pdpd_engine *e);
+
+/* Copy world `world`'s state x(t), v(t), f(t) and t to host arrays (bead-id order, vector
+ * layout as in pdpd_world; any pointer may be NULL). */
+int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
+                    size_t bead_stride_bytes, int64_t *t);
+
+/* DPDEngine::Run(interval_count, interval_size, callback) (dpd_engine.hpp:195-215) for a
+ * single attached world: after each interval the state is written to x/v/f (layout as in
+ * pdpd_world) and cb is called; the next interval already runs on the device meanwhile.
+ * interval_count < 0 runs until cb returns 0.  *steps_done receives the steps completed;
+ * on an early stop the device state is rolled back to the last reported interval. */
+int pdpd_run_intervals(pdpd_engine *e, int32_t interval_count, uint32_t interval_size,
+                       double *x, double *v, double *f, size_t bead_stride_bytes,
+                       pdpd_interval_fn cb, void *user, uint32_t *steps_done);
+
+/* DPDEngine::GetTimings (dpd_engine.hpp:145-148). */
+int pdpd_get_timings(pdpd_engine *e, pdpd_timings *out);
+
+/* DPDEngine::GetConfigEntries / SetConfigEntry (dpd_engine.hpp:150-169).  Entry i's name,
+ * description and value are copied into the buffers; returns PDPD_E_INVALID past the end. */
+int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len, char *desc,
+                    size_t desc_len, char *value, size_t value_len);
+int pdpd_set_config(pdpd_engine *e, const char *key, const char *value);
+
+/* Per-phase device time of a run, in milliseconds, measured with CUDA events on the
+ * engine's stream around each kernel group.  `force` covers the force kernels (pair + bond
+ * forces, velocity update, next position update and cell count), `sort` the counting sort
+ * (scan, place, canon), `other` the first position update and the final copy. */
+typedef struct pdpd_phase_times {
+    double force_ms;
+    double sort_ms;
+    double other_ms;
+    uint32_t force_launches;
+    uint32_t sort_launches;
+} pdpd_phase_times;
+
+/* Run n_steps like pdpd_run, but launch kernels one by one (no graph) with CUDA events
+ * between phases, and report the per-phase device times.  The trajectory is identical to
+ * pdpd_run's. */
+int pdpd_profile_run(pdpd_engine *e, uint32_t n_steps, pdpd_phase_times *out);
+
+/* Evaluate the engine's device RNG on n host-supplied records: for each i,
+ * h_out[i] = hash_rng_sym(get_t_hash(t[i], seed[i]), a[i], b[i]) and
+ * u_out[i] = default_hash(...) (reference include/dpd/core/hash.hpp:61-65,81-88 and
+ * include/dpd/maths/dpd_maths_core.hpp:55-79), computed by the same device functions the
+ * force kernels use.  For known-answer tests of the RNG; either output may be NULL. */
+int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
+                  const uint32_t *b, uint32_t *h_out, float *u_out);
+
+/* Number of kernel launches the engine has issued since creation (graph replays count
+ * each kernel node).  For accounting in benchmarks. */
+uint64_t pdpd_kernel_launches(pdpd_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

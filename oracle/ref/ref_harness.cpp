@@ -1,0 +1,237 @@
+// Test infrastructure: drives the reference's own engines, compiled unchanged from the
+// reference headers, on worlds stored in the PDW1 file format (see oracle/pdw1.md).
+// Only the fixture generator (tests/golden/make_golden.py) runs this program, and only
+// in a container where the reference sources are present.
+//
+//   ref_harness step  <engine> <in.pdw1> <out.bin> <n_checkpoints> <steps_1> ... <steps_n>
+//       Attach + Run(steps_k - steps_{k-1}) and dump (t, x, v, f of every bead) at each
+//       checkpoint.  Engines: naive_dpd_engine_half_step (include/dpd/engines/naive/
+//       naive_dpd_engine_half_step.hpp:42), naive_dpd_engine_half_merge
+//       (naive_dpd_engine_half_merge.hpp) and naive_dpd_engine (NaiveDPDEngine<false>,
+//       naive_dpd_engine.hpp).
+//   ref_harness hash  <in.bin> <out.bin>
+//       For each record (uint32 t, uint64 seed, uint32 a, uint32 b) write get_t_hash
+//       (hash.hpp:61-65), hash_rng_sym (hash.hpp:81-88) and dpd_maths_core::default_hash
+//       (dpd_maths_core.hpp:55-79).
+//   ref_harness cansupport <engine> <in.pdw1>
+//       Print the engine's CanSupport() string.
+//   ref_harness time <engine> <in.pdw1> <steps>
+//       Attach + Run(steps), print bead-steps/s of the Run call.
+
+#include "dpd/core/dpd_engine.hpp"
+#include "dpd/core/dpd_state_validator.hpp"
+#include "dpd/core/logging.hpp"
+#include "dpd/core/logging_impl.hpp"
+#include "dpd/engines/naive/naive_dpd_engine.hpp"
+#include "dpd/engines/naive/naive_dpd_engine_half_step.hpp"
+#include "dpd/engines/naive/naive_dpd_engine_half_merge.hpp"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <chrono>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct Reader {
+    FILE *f;
+    explicit Reader(const char *path) : f(fopen(path, "rb")) {
+        if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    }
+    ~Reader() { if (f) fclose(f); }
+    template <class T> T get() {
+        T v;
+        if (fread(&v, sizeof(T), 1, f) != 1) throw std::runtime_error("short read");
+        return v;
+    }
+};
+
+WorldState read_pdw1(const char *path)
+{
+    Reader r(path);
+    char magic[4];
+    if (fread(magic, 1, 4, r.f) != 4 || memcmp(magic, "PDW1", 4) != 0)
+        throw std::runtime_error("not a PDW1 file");
+    WorldState s;
+    for (int i = 0; i < 3; i++) s.box[i] = r.get<int32_t>();
+    s.dt = r.get<double>();
+    s.lambda = r.get<double>();
+    s.seed = r.get<uint64_t>();
+    s.t = r.get<int64_t>();
+    unsigned nt = r.get<uint32_t>();
+    for (unsigned i = 0; i < nt; i++) {
+        BeadType bt;
+        bt.name = "T" + std::to_string(i);
+        bt.r = 0.5;
+        bt.id = i;
+        bt.stationary = r.get<uint32_t>() != 0;
+        s.bead_types.push_back(bt);
+    }
+    s.interactions.resize(nt * nt);
+    for (unsigned i = 0; i < nt * nt; i++) s.interactions[i].conservative = r.get<double>();
+    for (unsigned i = 0; i < nt * nt; i++) s.interactions[i].dissipative = r.get<double>();
+    unsigned npt = r.get<uint32_t>();
+    for (unsigned i = 0; i < npt; i++) {
+        PolymerType pt;
+        pt.name = "P" + std::to_string(i);
+        pt.polymer_id = i;
+        unsigned nb = r.get<uint32_t>();
+        for (unsigned k = 0; k < nb; k++) pt.bead_types.push_back(r.get<uint32_t>());
+        unsigned nbond = r.get<uint32_t>();
+        for (unsigned k = 0; k < nbond; k++) {
+            Bond b;
+            b.bead_offset_head = r.get<uint32_t>();
+            b.bead_offset_tail = r.get<uint32_t>();
+            b.kappa = r.get<double>();
+            b.r0 = r.get<double>();
+            pt.bonds.push_back(b);
+        }
+        unsigned npair = r.get<uint32_t>();
+        for (unsigned k = 0; k < npair; k++) {
+            BondPair bp;
+            bp.bond_offset_head = r.get<uint32_t>();
+            bp.bond_offset_tail = r.get<uint32_t>();
+            bp.kappa = r.get<double>();
+            bp.theta0 = r.get<double>();
+            pt.bond_pairs.push_back(bp);
+        }
+        s.polymer_types.push_back(pt);
+    }
+    unsigned np = r.get<uint32_t>();
+    s.polymers.resize(np);
+    for (unsigned i = 0; i < np; i++) {
+        Polymer &p = s.polymers[i];
+        p.polymer_id = i;
+        p.polymer_type = r.get<uint32_t>();
+        unsigned n = r.get<uint32_t>();
+        for (unsigned k = 0; k < n; k++) p.bead_ids.push_back(r.get<uint32_t>());
+    }
+    unsigned nb = r.get<uint32_t>();
+    s.beads.resize(nb);
+    for (unsigned i = 0; i < nb; i++) {
+        Bead &b = s.beads[i];
+        b.bead_id = r.get<uint32_t>();
+        b.polymer_id = r.get<uint32_t>();
+        b.polymer_offset = r.get<uint8_t>();
+        b.bead_type = r.get<uint8_t>();
+        b.polymer_type = r.get<uint8_t>();
+        b.is_monomer = r.get<uint8_t>() != 0;
+        for (int d = 0; d < 3; d++) b.x[d] = r.get<double>();
+        for (int d = 0; d < 3; d++) b.v[d] = r.get<double>();
+        for (int d = 0; d < 3; d++) b.f[d] = r.get<double>();
+    }
+    return s;
+}
+
+std::shared_ptr<DPDEngine> make_engine(const std::string &name)
+{
+    if (name == "naive_dpd_engine_half_step") return std::make_shared<NaiveDPDEngineHalfStep>();
+    if (name == "naive_dpd_engine_half_merge") return std::make_shared<NaiveDPDEngineHalfMerge>();
+    if (name == "naive_dpd_engine") return std::make_shared<NaiveDPDEngine<false>>();
+    throw std::runtime_error("unknown engine " + name);
+}
+
+void dump(FILE *out, const WorldState &s)
+{
+    int64_t t = s.t;
+    fwrite(&t, sizeof(t), 1, out);
+    uint32_t n = s.beads.size();
+    fwrite(&n, sizeof(n), 1, out);
+    for (const Bead &b : s.beads) {
+        double rec[9];
+        for (int d = 0; d < 3; d++) { rec[d] = b.x[d]; rec[3 + d] = b.v[d]; rec[6 + d] = b.f[d]; }
+        fwrite(rec, sizeof(double), 9, out);
+    }
+}
+
+int cmd_step(int argc, char **argv)
+{
+    if (argc < 6) throw std::runtime_error("usage: step engine in out n steps...");
+    std::string engine_name = argv[2];
+    WorldState s = read_pdw1(argv[3]);
+    FILE *out = fopen(argv[4], "wb");
+    if (!out) throw std::runtime_error("cannot open output");
+    unsigned n = atoi(argv[5]);
+    auto e = make_engine(engine_name);
+    std::string why = e->CanSupport(&s);
+    if (!why.empty()) throw std::runtime_error("CanSupport: " + why);
+    e->Attach(&s);
+    unsigned done = 0;
+    for (unsigned k = 0; k < n; k++) {
+        unsigned target = atoi(argv[6 + k]);
+        if (target > done) e->Run(target - done);
+        done = target;
+        dump(out, s);
+    }
+    fclose(out);
+    return 0;
+}
+
+int cmd_hash(int argc, char **argv)
+{
+    Reader r(argv[2]);
+    FILE *out = fopen(argv[3], "wb");
+    if (!out) throw std::runtime_error("cannot open output");
+    while (true) {
+        uint32_t t;
+        if (fread(&t, 4, 1, r.f) != 1) break;
+        uint64_t seed = r.get<uint64_t>();
+        uint32_t a = r.get<uint32_t>();
+        uint32_t b = r.get<uint32_t>();
+        uint64_t th = get_t_hash(t, seed);
+        uint32_t h = hash_rng_sym(th, a, b);
+        float u = dpd_maths_core::default_hash(th, a, b);
+        fwrite(&th, 8, 1, out);
+        fwrite(&h, 4, 1, out);
+        fwrite(&u, 4, 1, out);
+    }
+    fclose(out);
+    return 0;
+}
+
+int cmd_cansupport(int argc, char **argv)
+{
+    WorldState s = read_pdw1(argv[3]);
+    auto e = make_engine(argv[2]);
+    printf("%s\n", e->CanSupport(&s).c_str());
+    return 0;
+}
+
+int cmd_time(int argc, char **argv)
+{
+    WorldState s = read_pdw1(argv[3]);
+    unsigned steps = atoi(argv[4]);
+    auto e = make_engine(argv[2]);
+    e->Attach(&s);
+    auto t0 = std::chrono::steady_clock::now();
+    e->Run(steps);
+    auto t1 = std::chrono::steady_clock::now();
+    double sec = std::chrono::duration<double>(t1 - t0).count();
+    printf("%.6e\n", double(s.beads.size()) * steps / sec);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    try {
+        if (argc < 2) throw std::runtime_error("usage: ref_harness step|hash|cansupport|time ...");
+        std::string cmd = argv[1];
+        if (cmd == "step") return cmd_step(argc, argv);
+        if (cmd == "hash") return cmd_hash(argc, argv);
+        if (cmd == "cansupport") return cmd_cansupport(argc, argv);
+        if (cmd == "time") return cmd_time(argc, argv);
+        throw std::runtime_error("unknown command " + cmd);
+    } catch (std::exception &e) {
+        fprintf(stderr, "ref_harness: %s\n", e.what());
+        return 1;
+    } catch (std::string &e) {
+        fprintf(stderr, "ref_harness: %s\n", e.c_str());
+        return 1;
+    }
+}

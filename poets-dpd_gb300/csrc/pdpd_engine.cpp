@@ -1,0 +1,981 @@
+// Host runtime of the GB300 DPD engine: implements the C ABI declared in include/pdpd_gpu.h.
+//
+// The engine owns one device arena holding every attached world (a batch of one for the
+// plain DPDEngine path).  A timestep is a fixed sequence of kernels on the engine's stream:
+//   force (finish step t, start step t+1) -> scan x2 -> place -> canon
+// which is captured once per attach into a CUDA graph of G consecutive steps and replayed.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pdpd_gpu.h"
+#include "pdpd_internal.h"
+
+using namespace pdpd;
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t alloc(size_t n)
+    {
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T *as() const { return (T *)p; }
+};
+
+struct HostPinned {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t alloc(size_t n)
+    {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMallocHost(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct WorldHost {
+    WorldDev dev;
+};
+
+struct ConfigEntry {
+    const char *name;
+    const char *desc;
+};
+
+const ConfigEntry kConfig[] = {
+    {"tile_cells", "Cells per work tile of the step kernels (0 = automatic)."},
+    {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
+    {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
+    {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
+};
+
+}  // namespace
+
+struct pdpd_engine {
+    int precision = PDPD_FP32;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;
+    std::string err;
+    pdpd_timings timings{-1, -1, -1, -1, -1, -1};
+    uint64_t launches = 0;
+
+    // configuration
+    int cfg_tile_cells = 0;
+    int cfg_grid_blocks = 0;
+    int cfg_graph_steps = 0;
+    int cfg_use_graphs = 1;
+
+    // attached worlds
+    bool attached = false;
+    std::vector<WorldHost> worlds;
+    uint32_t n_beads = 0, n_cells = 0, n_tiles = 0;
+
+    // device arena
+    DevBuf d_worlds, d_tiles, d_start, d_cnt, d_blocksums;
+    DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
+    DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash;
+    DevBuf d_staging[2];
+    HostPinned h_staging[2];
+    HostPinned h_err;
+    cudaEvent_t ev_snap[2] = {nullptr, nullptr};
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr};
+
+    // graphs
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    int graph_kernels = 0;
+
+    KArgs args{};
+
+    int fail(int code, const char *fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what)
+    {
+        return fail(PDPD_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+
+    void drop_graph()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_steps = 0;
+    }
+
+    void release()
+    {
+        drop_graph();
+        DevBuf *bufs[] = {&d_worlds, &d_tiles, &d_start, &d_cnt, &d_blocksums, &d_posA, &d_velA,
+                          &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
+                          &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
+                          &d_pair, &d_hash, &d_staging[0], &d_staging[1]};
+        for (DevBuf *b : bufs) b->release();
+        worlds.clear();
+        attached = false;
+        n_beads = n_cells = n_tiles = 0;
+    }
+
+    bool fp64() const { return precision == PDPD_FP64; }
+
+    // ---- step sequences ------------------------------------------------------------------
+    int enqueue_begin(cudaStream_t s)
+    {
+        int n = fp64() ? launch_begin64(args, s) : launch_begin32(args, s);
+        n += launch_sort(args, fp64(), 0, 0, s);
+        return n;
+    }
+    int enqueue_step(cudaStream_t s)  // finish step t and start t+1
+    {
+        int n = fp64() ? launch_force64(args, 0, s) : launch_force32(args, 0, s);
+        n += launch_sort(args, fp64(), 1, 0, s);
+        return n;
+    }
+    int enqueue_final(cudaStream_t s)
+    {
+        int n = fp64() ? launch_force64(args, 1, s) : launch_force32(args, 1, s);
+        n += fp64() ? launch_finish64(args, s) : launch_finish32(args, s);
+        return n;
+    }
+
+    int auto_graph_steps() const
+    {
+        if (cfg_graph_steps > 0) return std::min(cfg_graph_steps, 256);
+        uint64_t target = 4u << 20;  // about 4M bead-steps per replay
+        uint64_t g = n_beads ? target / n_beads : 64;
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>(64, g));
+    }
+
+    int build_graph()
+    {
+        drop_graph();
+        int G = auto_graph_steps();
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+        int k = 0;
+        for (int i = 0; i < G; i++) k += enqueue_step(stream);
+        e = cudaStreamEndCapture(stream, &g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            graph = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+        graph_steps = G;
+        graph_kernels = k;
+        return PDPD_OK;
+    }
+
+    // Enqueue n steps (n >= 1) on stream s.
+    int enqueue_run(uint32_t n, cudaStream_t s)
+    {
+        if (n == 0) return PDPD_OK;
+        launches += enqueue_begin(s);
+        uint32_t mid = n - 1;
+        if (cfg_use_graphs && mid > 0 && s == stream) {
+            if (!graph) {
+                int rc = build_graph();
+                if (rc) return rc;
+            }
+            while (mid >= (uint32_t)graph_steps) {
+                cudaError_t e = cudaGraphLaunch(graph, s);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+                launches += graph_kernels;
+                mid -= graph_steps;
+            }
+        }
+        for (uint32_t i = 0; i < mid; i++) launches += enqueue_step(s);
+        launches += enqueue_final(s);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        return PDPD_OK;
+    }
+
+    int check_device_errors()
+    {
+        size_t nb = sizeof(WorldDev) * worlds.size();
+        if (h_err.alloc(nb) != cudaSuccess) return fail(PDPD_E_NOMEM, "pinned allocation failed");
+        cudaError_t e = cudaMemcpyAsync(h_err.p, d_worlds.p, nb, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "device error check");
+        const WorldDev *wd = (const WorldDev *)h_err.p;
+        for (size_t i = 0; i < worlds.size(); i++) {
+            worlds[i].dev.t = wd[i].t;
+            uint32_t f = wd[i].err;
+            if (!f) continue;
+            if (f & ERR_BOND_SNAPPED)
+                return fail(PDPD_E_BOND_SNAPPED,
+                            "world %zu: an angle bond has snapped (Hookean bond longer than %.1f)", i,
+                            pdpd_max_bond_length());
+            if (f & ERR_NONFINITE)
+                return fail(PDPD_E_BEAD_LOST, "world %zu: a bead position or velocity became non-finite", i);
+            if (f & ERR_OUT_OF_BOX)
+                return fail(PDPD_E_BEAD_LOST, "world %zu: a bead is outside the box or moved more than a box in one step", i);
+        }
+        return PDPD_OK;
+    }
+};
+
+// ------------------------------------------------------------------------------------------
+// validation
+
+static int check_world(const pdpd_world *w, char *reason, size_t n)
+{
+    auto say = [&](int code, const char *msg) {
+        if (reason && n) snprintf(reason, n, "%s", msg);
+        return code;
+    };
+    if (!w) return say(PDPD_E_INVALID, "No state");
+    uint64_t cells = 1;
+    for (int i = 0; i < 3; i++) {
+        if (w->box[i] < 2) return say(PDPD_E_INVALID, "Distance in each direction must be at least 2");
+        if (w->box[i] > 4096) return say(PDPD_E_UNSUPPORTED, "Box side larger than 4096 cells.");
+        cells *= (uint64_t)w->box[i];
+    }
+    if (cells >= (1ull << 31)) return say(PDPD_E_UNSUPPORTED, "Box has more than 2^31 cells.");
+    if (!(w->dt > 0 && w->dt < 1)) return say(PDPD_E_INVALID, "dt must be in (0, 1).");
+    if (w->n_bead_types == 0 || w->n_bead_types > 16)
+        return say(PDPD_E_UNSUPPORTED, "Engine supports 1..16 bead types (4-bit BeadHash type field).");
+    if (!w->conservative || !w->dissipative)
+        return say(PDPD_E_INVALID, "Missing interaction matrices.");
+    if (w->stationary)
+        for (uint32_t i = 0; i < w->n_bead_types; i++)
+            if (w->stationary[i]) return say(PDPD_E_UNSUPPORTED, "Engine does not support stationary bead types.");
+    for (uint32_t i = 0; i < w->n_bead_types * w->n_bead_types; i++)
+        if (!(w->dissipative[i] >= 0) || !std::isfinite(w->conservative[i]))
+            return say(PDPD_E_INVALID, "Interaction strengths must be finite and gamma >= 0.");
+    if (w->n_beads && (!w->hash || !w->x || !w->v || !w->f))
+        return say(PDPD_E_INVALID, "Missing bead arrays.");
+    for (uint32_t i = 0; i < w->n_beads; i++)
+        if ((w->hash[i] >> 28) >= w->n_bead_types) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
+    if (w->n_bonds && (!w->bond_beads || !w->bond_kappa || !w->bond_r0))
+        return say(PDPD_E_INVALID, "Missing bond arrays.");
+    for (uint32_t k = 0; k < 2 * w->n_bonds; k++)
+        if (w->bond_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Bond refers to a bead that does not exist.");
+    if (w->n_angles && (!w->angle_beads || !w->angle_kappa || !w->angle_theta0))
+        return say(PDPD_E_INVALID, "Missing angle-bond arrays.");
+    for (uint32_t k = 0; k < 3 * w->n_angles; k++)
+        if (w->angle_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Angle bond refers to a bead that does not exist.");
+    return PDPD_OK;
+}
+
+static const double *vec_at(const double *base, size_t stride_bytes, uint32_t i)
+{
+    size_t s = stride_bytes ? stride_bytes : 3 * sizeof(double);
+    return (const double *)((const char *)base + s * (size_t)i);
+}
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int pdpd_create(int precision, int device, pdpd_engine **out)
+{
+    if (!out) return PDPD_E_INVALID;
+    *out = nullptr;
+    if (precision != PDPD_FP32 && precision != PDPD_FP64) {
+        g_last_error = "precision must be PDPD_FP32 or PDPD_FP64";
+        return PDPD_E_INVALID;
+    }
+    int dev = device;
+    cudaError_t e = cudaSuccess;
+    if (dev < 0) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaSetDevice(dev);
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+        g_last_error = std::string("no usable CUDA device: ") + cudaGetErrorString(e);
+        return PDPD_E_CUDA;
+    }
+    pdpd_engine *eng = new pdpd_engine();
+    eng->precision = precision;
+    eng->device = dev;
+    eng->sm_count = sms;
+    e = cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->side, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaEventCreateWithFlags(&eng->ev_snap[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&eng->ev_copied[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        g_last_error = std::string("stream creation failed: ") + cudaGetErrorString(e);
+        pdpd_destroy(eng);
+        return PDPD_E_CUDA;
+    }
+    *out = eng;
+    return PDPD_OK;
+}
+
+void pdpd_destroy(pdpd_engine *e)
+{
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->side) cudaStreamSynchronize(e->side);
+    e->release();
+    e->h_staging[0].release();
+    e->h_staging[1].release();
+    e->h_err.release();
+    for (int i = 0; i < 2; i++) {
+        if (e->ev_snap[i]) cudaEventDestroy(e->ev_snap[i]);
+        if (e->ev_copied[i]) cudaEventDestroy(e->ev_copied[i]);
+    }
+    if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->side) cudaStreamDestroy(e->side);
+    delete e;
+}
+
+const char *pdpd_last_error(const pdpd_engine *e)
+{
+    return e ? e->err.c_str() : g_last_error.c_str();
+}
+
+int pdpd_can_support(const pdpd_world *w, char *reason, size_t reason_len)
+{
+    if (reason && reason_len) reason[0] = 0;
+    int rc = check_world(w, reason, reason_len);
+    if (rc && reason) g_last_error = reason;
+    return rc;
+}
+
+double pdpd_max_bond_length(void)
+{
+    return 2.0;
+}
+
+int pdpd_attach(pdpd_engine *e, const pdpd_world *w)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!w) {
+        cudaSetDevice(e->device);
+        cudaStreamSynchronize(e->stream);
+        e->release();
+        return PDPD_OK;
+    }
+    return pdpd_attach_batch(e, w, 1);
+}
+
+int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!ws || n_worlds == 0) return e->fail(PDPD_E_INVALID, "no worlds given");
+    double t0 = now_s();
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    e->release();
+    char reason[256];
+    uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        int rc = check_world(&ws[i], reason, sizeof reason);
+        if (rc) return e->fail(rc, "world %u: %s", i, reason);
+        nb += ws[i].n_beads;
+        nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
+        n_pair += (uint64_t)ws[i].n_bead_types * ws[i].n_bead_types;
+        n_terms += 2ull * ws[i].n_bonds + 3ull * ws[i].n_angles;
+        n_bparams += ws[i].n_bonds + ws[i].n_angles;
+    }
+    if (nb >= (1ull << 31) || nc >= (1ull << 31))
+        return e->fail(PDPD_E_UNSUPPORTED, "batch too large (%llu beads, %llu cells)",
+                       (unsigned long long)nb, (unsigned long long)nc);
+    e->n_beads = (uint32_t)nb;
+    e->n_cells = (uint32_t)nc;
+
+    // --- world table, tiles, pair table
+    int tile_cells = e->cfg_tile_cells > 0 ? e->cfg_tile_cells : 64;
+    std::vector<Tile> tiles;
+    std::vector<WorldDev> wdev(n_worlds);
+    const bool f64 = e->fp64();
+    std::vector<double> pair64;
+    std::vector<float> pair32;
+    uint32_t cell_base = 0, bead_base = 0, param_base = 0;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        WorldDev &d = wdev[i];
+        memset(&d, 0, sizeof d);
+        for (int k = 0; k < 3; k++) d.L[k] = w.box[k];
+        d.n_cells = (uint32_t)w.box[0] * w.box[1] * w.box[2];
+        d.cell_base = cell_base;
+        d.bead_base = bead_base;
+        d.n_beads = w.n_beads;
+        d.n_types = w.n_bead_types;
+        d.param_base = param_base;
+        d.dt = w.dt;
+        d.scale_inv_sqrt_dt = std::sqrt(24 * 1.0 / w.dt);  // pow_half(24 kT / dt)
+        d.seed = w.seed;
+        d.t = w.t;
+        for (uint32_t c = 0; c < d.n_cells; c += tile_cells)
+            tiles.push_back({i, cell_base + c, cell_base + std::min<uint32_t>(d.n_cells, c + tile_cells), 0});
+        for (uint32_t k = 0; k < w.n_bead_types * w.n_bead_types; k++) {
+            double a = w.conservative[k], sg = std::sqrt(w.dissipative[k]);
+            pair64.push_back(a);
+            pair64.push_back(sg);
+            pair32.push_back((float)a);
+            pair32.push_back((float)sg);
+        }
+        cell_base += d.n_cells;
+        bead_base += w.n_beads;
+        param_base += w.n_bead_types * w.n_bead_types;
+        WorldHost wh;
+        wh.dev = d;
+        e->worlds.push_back(wh);
+    }
+    e->n_tiles = (uint32_t)tiles.size();
+
+    // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
+    // the flat list order.
+    std::vector<uint32_t> row(nb + 1, 0);
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        uint32_t bb = wdev[i].bead_base;
+        for (uint32_t k = 0; k < 2 * w.n_bonds; k++) row[bb + w.bond_beads[k] + 1]++;
+        for (uint32_t k = 0; k < 3 * w.n_angles; k++) row[bb + w.angle_beads[k] + 1]++;
+    }
+    for (uint64_t i = 0; i < nb; i++) row[i + 1] += row[i];
+    std::vector<BondTerm> terms(n_terms);
+    std::vector<uint32_t> fill(row.begin(), row.end() - 1);
+    std::vector<double> bp64;
+    std::vector<float> bp32;
+    uint32_t pidx = 0;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        uint32_t bb = wdev[i].bead_base;
+        for (uint32_t k = 0; k < w.n_bonds; k++, pidx++) {
+            uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
+            terms[fill[h]++] = {0u | (0u << 8), t, t, pidx};
+            terms[fill[t]++] = {0u | (1u << 8), h, h, pidx};
+            double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
+            for (double v : p) {
+                bp64.push_back(v);
+                bp32.push_back((float)v);
+            }
+        }
+    }
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        uint32_t bb = wdev[i].bead_base;
+        for (uint32_t k = 0; k < w.n_angles; k++, pidx++) {
+            uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
+                     t = bb + w.angle_beads[3 * k + 2];
+            terms[fill[h]++] = {1u | (0u << 8), m, t, pidx};
+            terms[fill[m]++] = {1u | (1u << 8), h, t, pidx};
+            terms[fill[t]++] = {1u | (2u << 8), h, m, pidx};
+            double th = w.angle_theta0[k];
+            double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
+            for (double v : p) {
+                bp64.push_back(v);
+                bp32.push_back((float)v);
+            }
+        }
+    }
+    // The per-bead order must be: this bead's Hookean terms in flat order, then its angle
+    // terms in flat order.  Filling all Hookean bonds of all worlds before any angle bond
+    // gives exactly that.
+
+    // --- allocate
+    const size_t P = payload_bytes(f64);
+    cudaError_t ce = cudaSuccess;
+    auto A = [&](DevBuf &b, size_t n) {
+        if (ce == cudaSuccess) ce = b.alloc(n);
+    };
+    A(e->d_worlds, sizeof(WorldDev) * n_worlds);
+    A(e->d_tiles, sizeof(Tile) * std::max<size_t>(1, tiles.size()));
+    A(e->d_start, sizeof(uint32_t) * ((size_t)nc + 1));
+    A(e->d_cnt, sizeof(uint32_t) * (size_t)nc);
+    A(e->d_blocksums, sizeof(uint32_t) * (scan_blocks((uint32_t)nc) + 1));
+    A(e->d_posA, P * nb);
+    A(e->d_velA, P * nb);
+    A(e->d_frc, P * nb);
+    A(e->d_posB, P * nb);
+    A(e->d_velB, P * nb);
+    A(e->d_frcB, P * nb);
+    A(e->d_ids, sizeof(uint32_t) * nb);
+    A(e->d_cellg, sizeof(uint32_t) * nb);
+    A(e->d_slot_of_id, sizeof(uint32_t) * nb);
+    A(e->d_keyrank, sizeof(uint2) * nb);
+    A(e->d_tmp, sizeof(uint4) * nb);
+    A(e->d_bond_row, sizeof(uint32_t) * (nb + 1));
+    A(e->d_bond_terms, sizeof(BondTerm) * std::max<uint64_t>(1, n_terms));
+    A(e->d_bond_params, (f64 ? sizeof(double) : sizeof(float)) * 4 * std::max<uint64_t>(1, n_bparams));
+    A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
+    A(e->d_hash, sizeof(uint32_t) * nb);
+    A(e->d_staging[0], sizeof(double) * 9 * nb);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        e->release();
+        return e->fail(PDPD_E_NOMEM, "device allocation failed: %s", cudaGetErrorString(ce));
+    }
+    if (e->h_staging[0].alloc(sizeof(double) * 9 * nb + sizeof(uint32_t) * nb) != cudaSuccess) {
+        e->release();
+        return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
+    }
+
+    // --- stage and upload
+    double *hs = (double *)e->h_staging[0].p;
+    uint32_t *hh = (uint32_t *)(hs + 9 * nb);
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        uint32_t bb = wdev[i].bead_base;
+        for (uint32_t k = 0; k < w.n_beads; k++) {
+            const double *x = vec_at(w.x, w.bead_stride_bytes, k);
+            const double *v = vec_at(w.v, w.bead_stride_bytes, k);
+            const double *f = vec_at(w.f, w.bead_stride_bytes, k);
+            double *o = hs + 9 * (size_t)(bb + k);
+            for (int d = 0; d < 3; d++) {
+                o[d] = x[d];
+                o[3 + d] = v[d];
+                o[6 + d] = f[d];
+            }
+            hh[bb + k] = w.hash[k];
+        }
+    }
+    cudaStream_t s = e->stream;
+    auto H2D = [&](DevBuf &b, const void *src, size_t n) {
+        if (ce == cudaSuccess && n) ce = cudaMemcpyAsync(b.p, src, n, cudaMemcpyHostToDevice, s);
+    };
+    H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
+    H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
+    H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
+    H2D(e->d_bond_terms, terms.data(), sizeof(BondTerm) * n_terms);
+    if (f64) {
+        H2D(e->d_bond_params, bp64.data(), sizeof(double) * bp64.size());
+        H2D(e->d_pair, pair64.data(), sizeof(double) * pair64.size());
+    } else {
+        H2D(e->d_bond_params, bp32.data(), sizeof(float) * bp32.size());
+        H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
+    }
+    H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
+    H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_cnt.p, 0, sizeof(uint32_t) * nc, s);
+    uint32_t total = (uint32_t)nb;  // start[n_cells] = total beads, fixed for the attach
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(e->d_start.as<uint32_t>() + nc, &total, sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) {
+        e->release();
+        return e->cuda_fail(ce, "upload");
+    }
+
+    // --- kernel arguments
+    KArgs &a = e->args;
+    memset(&a, 0, sizeof a);
+    a.worlds = e->d_worlds.as<WorldDev>();
+    a.n_worlds = n_worlds;
+    a.tiles = e->d_tiles.as<Tile>();
+    a.n_tiles = e->n_tiles;
+    a.n_beads = e->n_beads;
+    a.n_cells = e->n_cells;
+    a.start = e->d_start.as<uint32_t>();
+    a.cnt = e->d_cnt.as<uint32_t>();
+    a.blocksums = e->d_blocksums.as<uint32_t>();
+    a.posA = e->d_posA.p;
+    a.velA = e->d_velA.p;
+    a.frc = e->d_frc.p;
+    a.posB = e->d_posB.p;
+    a.velB = e->d_velB.p;
+    a.frcB = e->d_frcB.p;
+    a.ids = e->d_ids.as<uint32_t>();
+    a.cellg = e->d_cellg.as<uint32_t>();
+    a.slot_of_id = e->d_slot_of_id.as<uint32_t>();
+    a.keyrank = e->d_keyrank.as<uint2>();
+    a.tmp = e->d_tmp.as<uint4>();
+    a.bond_row = e->d_bond_row.as<uint32_t>();
+    a.bond_terms = e->d_bond_terms.as<BondTerm>();
+    a.bond_params = e->d_bond_params.p;
+    a.pair = e->d_pair.p;
+    a.staging = e->d_staging[0].as<double>();
+    a.block_threads = 128;
+    int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
+    a.grid_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)gb, e->n_tiles));
+
+    // --- bin + sort into the rest state
+    const uint32_t *hash_in = e->d_hash.as<uint32_t>();
+    e->launches += f64 ? launch_bin64(a, hash_in, s) : launch_bin32(a, hash_in, s);
+    e->launches += launch_sort(a, f64, 0, 1, s);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+        e->release();
+        return e->cuda_fail(ce, "attach kernels");
+    }
+    e->attached = true;
+    int rc = e->check_device_errors();
+    if (rc) {
+        std::string m = e->err;
+        e->release();
+        e->err = m;
+        return rc;
+    }
+    e->timings = pdpd_timings{-1, -1, now_s() - t0, -1, -1, -1};
+    return PDPD_OK;
+}
+
+int pdpd_run_async(pdpd_engine *e, uint32_t n_steps)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "Run called with no world attached");
+    cudaSetDevice(e->device);
+    return e->enqueue_run(n_steps, e->stream);
+}
+
+int pdpd_sync(pdpd_engine *e)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    cudaSetDevice(e->device);
+    cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "cudaStreamSynchronize");
+    return e->check_device_errors();
+}
+
+int pdpd_run(pdpd_engine *e, uint32_t n_steps)
+{
+    if (!e) return PDPD_E_INVALID;
+    double t0 = now_s();
+    int rc = pdpd_run_async(e, n_steps);
+    if (rc) return rc;
+    rc = pdpd_sync(e);
+    double dt = now_s() - t0;
+    auto acc = [](double &slot, double v) { slot = slot < 0 ? v : slot + v; };
+    acc(e->timings.execute_to_first_bead, dt);
+    acc(e->timings.execute_to_last_bead, dt);
+    return rc;
+}
+
+void *pdpd_stream(pdpd_engine *e)
+{
+    return e ? (void *)e->stream : nullptr;
+}
+
+static int download(pdpd_engine *e, int buf, cudaStream_t s)
+{
+    KArgs a = e->args;
+    if (!e->d_staging[buf].p) {
+        cudaError_t ce = e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads);
+        if (ce != cudaSuccess) return e->fail(PDPD_E_NOMEM, "staging allocation failed");
+    }
+    a.staging = e->d_staging[buf].as<double>();
+    e->launches += e->fp64() ? launch_unsort64(a, s) : launch_unsort32(a, s);
+    return PDPD_OK;
+}
+
+static void scatter(const double *src, uint32_t n, double *x, double *v, double *f, size_t stride)
+{
+    size_t sb = stride ? stride : 3 * sizeof(double);
+    for (uint32_t i = 0; i < n; i++) {
+        const double *r = src + 9 * (size_t)i;
+        if (x) memcpy((char *)x + sb * i, r, 3 * sizeof(double));
+        if (v) memcpy((char *)v + sb * i, r + 3, 3 * sizeof(double));
+        if (f) memcpy((char *)f + sb * i, r + 6, 3 * sizeof(double));
+    }
+}
+
+int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
+                    size_t stride, int64_t *t)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    cudaSetDevice(e->device);
+    int rc = download(e, 0, e->stream);
+    if (rc) return rc;
+    const WorldDev &wd = e->worlds[world].dev;
+    size_t nbytes = sizeof(double) * 9 * (size_t)wd.n_beads;
+    if (e->h_staging[0].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    if (nbytes) {
+        cudaError_t ce = cudaMemcpyAsync(e->h_staging[0].p, e->d_staging[0].as<double>() + 9 * (size_t)wd.bead_base,
+                                         nbytes, cudaMemcpyDeviceToHost, e->stream);
+        if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
+    }
+    rc = e->check_device_errors();  // synchronises
+    if (rc) return rc;
+    scatter((const double *)e->h_staging[0].p, wd.n_beads, x, v, f, stride);
+    if (t) *t = e->worlds[world].dev.t;
+    return PDPD_OK;
+}
+
+int pdpd_run_intervals(pdpd_engine *e, int32_t interval_count, uint32_t interval_size, double *x,
+                       double *v, double *f, size_t stride, pdpd_interval_fn cb, void *user,
+                       uint32_t *steps_done)
+{
+    if (steps_done) *steps_done = 0;
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "Run called with no world attached");
+    if (e->worlds.size() != 1) return e->fail(PDPD_E_STATE, "interval runs need exactly one attached world");
+    if (!cb) return e->fail(PDPD_E_INVALID, "no callback");
+    cudaSetDevice(e->device);
+    double t0 = now_s();
+    const WorldDev wd0 = e->worlds[0].dev;
+    const uint32_t n = wd0.n_beads;
+    const size_t nbytes = sizeof(double) * 9 * (size_t)n;
+    for (int b = 0; b < 2; b++) {
+        if (!e->d_staging[b].p && e->d_staging[b].alloc(nbytes) != cudaSuccess)
+            return e->fail(PDPD_E_NOMEM, "staging allocation failed");
+        if (e->h_staging[b].alloc(nbytes + sizeof(WorldDev)) != cudaSuccess)
+            return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    }
+    uint32_t done = 0;
+    int64_t t_cur = wd0.t;
+    int rc = PDPD_OK;
+    if (interval_count == 0) return PDPD_OK;
+    rc = e->enqueue_run(interval_size, e->stream);
+    for (int64_t k = 1; rc == PDPD_OK; k++) {
+        const int b = (int)(k & 1);
+        // Snapshot interval k into device staging b and start copying it to the host on the
+        // side stream; the main stream goes straight on with interval k+1.
+        rc = download(e, b, e->stream);
+        if (rc) break;
+        WorldDev *herr = (WorldDev *)((char *)e->h_staging[b].p + nbytes);
+        cudaMemcpyAsync(herr, e->d_worlds.p, sizeof(WorldDev), cudaMemcpyDeviceToHost, e->stream);
+        cudaEventRecord(e->ev_snap[b], e->stream);
+        cudaStreamWaitEvent(e->side, e->ev_snap[b], 0);
+        cudaMemcpyAsync(e->h_staging[b].p, e->d_staging[b].p, nbytes, cudaMemcpyDeviceToHost, e->side);
+        cudaEventRecord(e->ev_copied[b], e->side);
+        const bool more = interval_count < 0 || k < interval_count;
+        if (more) {
+            rc = e->enqueue_run(interval_size, e->stream);
+            if (rc) break;
+        }
+        cudaError_t ce = cudaEventSynchronize(e->ev_copied[b]);
+        if (ce != cudaSuccess) {
+            rc = e->cuda_fail(ce, "snapshot copy");
+            break;
+        }
+        if (herr->err) {
+            cudaStreamSynchronize(e->stream);
+            rc = e->check_device_errors();
+            if (!rc) rc = e->fail(PDPD_E_BEAD_LOST, "device error during interval");
+            break;
+        }
+        t_cur = herr->t;
+        scatter((const double *)e->h_staging[b].p, n, x, v, f, stride);
+        done += interval_size;
+        int go = cb(user, t_cur);
+        if (!go || !more) {
+            if (more) {
+                // Roll the device back to the state the caller has just seen: re-bin the
+                // snapshot (lossless in both precisions) and reset t.
+                cudaStreamSynchronize(e->stream);
+                KArgs a = e->args;
+                a.staging = e->d_staging[b].as<double>();
+                std::vector<WorldDev> wv(1);
+                memcpy(wv.data(), herr, sizeof(WorldDev));
+                wv[0].err = 0;
+                cudaMemcpyAsync(e->d_worlds.p, wv.data(), sizeof(WorldDev), cudaMemcpyHostToDevice, e->stream);
+                e->launches += e->fp64() ? launch_bin64(a, e->d_hash.as<uint32_t>(), e->stream)
+                                         : launch_bin32(a, e->d_hash.as<uint32_t>(), e->stream);
+                e->launches += launch_sort(a, e->fp64(), 0, 1, e->stream);
+                rc = pdpd_sync(e);
+            }
+            break;
+        }
+    }
+    if (rc == PDPD_OK) rc = pdpd_sync(e);
+    if (steps_done) *steps_done = done;
+    double dt = now_s() - t0;
+    auto acc = [](double &slot, double v) { slot = slot < 0 ? v : slot + v; };
+    acc(e->timings.execute_to_first_bead, dt);
+    acc(e->timings.execute_to_last_bead, dt);
+    return rc;
+}
+
+int pdpd_get_timings(pdpd_engine *e, pdpd_timings *out)
+{
+    if (!e || !out) return PDPD_E_INVALID;
+    *out = e->timings;
+    return PDPD_OK;
+}
+
+int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len, char *desc,
+                    size_t desc_len, char *value, size_t value_len)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
+    int vals[] = {e->cfg_tile_cells, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs};
+    if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
+    if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
+    if (value && value_len) snprintf(value, value_len, "%d", vals[index]);
+    return PDPD_OK;
+}
+
+int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
+{
+    if (!e || !key || !value) return PDPD_E_INVALID;
+    char *end = nullptr;
+    long v = strtol(value, &end, 10);
+    if (!end || *end || v < 0 || v > (1 << 24)) return e->fail(PDPD_E_INVALID, "bad value '%s' for '%s'", value, key);
+    std::string k = key;
+    if (k == "tile_cells") e->cfg_tile_cells = (int)v;
+    else if (k == "grid_blocks") e->cfg_grid_blocks = (int)v;
+    else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
+    else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
+    else return e->fail(PDPD_E_INVALID, "Unknown engine config name '%s'", key);
+    e->drop_graph();  // layout-dependent settings take effect at the next attach / capture
+    return PDPD_OK;
+}
+
+int pdpd_profile_run(pdpd_engine *e, uint32_t n_steps, pdpd_phase_times *out)
+{
+    if (!e || !out) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "Run called with no world attached");
+    cudaSetDevice(e->device);
+    memset(out, 0, sizeof *out);
+    if (n_steps == 0) return PDPD_OK;
+    const bool f64 = e->fp64();
+    cudaStream_t s = e->stream;
+    // events: one before and after every phase
+    std::vector<cudaEvent_t> ev;
+    auto mark = [&]() {
+        cudaEvent_t x;
+        cudaEventCreate(&x);
+        cudaEventRecord(x, s);
+        ev.push_back(x);
+        return ev.size() - 1;
+    };
+    struct Span {
+        size_t a, b;
+        int kind;  // 0 force, 1 sort, 2 other
+    };
+    std::vector<Span> spans;
+    size_t m0 = mark();
+    e->launches += f64 ? launch_begin64(e->args, s) : launch_begin32(e->args, s);
+    size_t m1 = mark();
+    spans.push_back({m0, m1, 2});
+    e->launches += launch_sort(e->args, f64, 0, 0, s);
+    size_t m2 = mark();
+    spans.push_back({m1, m2, 1});
+    for (uint32_t i = 0; i + 1 < n_steps; i++) {
+        size_t a = mark();
+        e->launches += f64 ? launch_force64(e->args, 0, s) : launch_force32(e->args, 0, s);
+        size_t b = mark();
+        e->launches += launch_sort(e->args, f64, 1, 0, s);
+        size_t c = mark();
+        spans.push_back({a, b, 0});
+        spans.push_back({b, c, 1});
+    }
+    size_t a = mark();
+    e->launches += f64 ? launch_force64(e->args, 1, s) : launch_force32(e->args, 1, s);
+    size_t b = mark();
+    e->launches += f64 ? launch_finish64(e->args, s) : launch_finish32(e->args, s);
+    size_t c = mark();
+    spans.push_back({a, b, 0});
+    spans.push_back({b, c, 2});
+    cudaError_t ce = cudaGetLastError();
+    int rc = ce == cudaSuccess ? pdpd_sync(e) : e->cuda_fail(ce, "kernel launch");
+    if (rc == PDPD_OK) {
+        for (const Span &sp : spans) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[sp.a], ev[sp.b]);
+            if (sp.kind == 0) {
+                out->force_ms += ms;
+                out->force_launches++;
+            } else if (sp.kind == 1) {
+                out->sort_ms += ms;
+                out->sort_launches++;
+            } else {
+                out->other_ms += ms;
+            }
+        }
+    }
+    for (cudaEvent_t x : ev) cudaEventDestroy(x);
+    return rc;
+}
+
+int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
+                  const uint32_t *b, uint32_t *h_out, float *u_out)
+{
+    if (n == 0) return PDPD_OK;
+    if (!t || !seed || !a || !b) {
+        g_last_error = "pdpd_rng_eval: missing input array";
+        return PDPD_E_INVALID;
+    }
+    DevBuf dt, ds, da, db, dh, du;
+    cudaError_t ce = cudaSuccess;
+    auto A = [&](DevBuf &bf, size_t bytes) {
+        if (ce == cudaSuccess) ce = bf.alloc(bytes);
+    };
+    A(dt, 4 * n);
+    A(ds, 8 * n);
+    A(da, 4 * n);
+    A(db, 4 * n);
+    A(dh, 4 * n);
+    A(du, 4 * n);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dt.p, t, 4 * n, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(ds.p, seed, 8 * n, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(da.p, a, 4 * n, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(db.p, b, 4 * n, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) {
+        launch_rng_eval(n, dt.as<uint32_t>(), ds.as<uint64_t>(), da.as<uint32_t>(), db.as<uint32_t>(),
+                        dh.as<uint32_t>(), du.as<float>(), 0);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess && h_out) ce = cudaMemcpy(h_out, dh.p, 4 * n, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && u_out) ce = cudaMemcpy(u_out, du.p, 4 * n, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) {
+        g_last_error = std::string("pdpd_rng_eval: ") + cudaGetErrorString(ce);
+        return PDPD_E_CUDA;
+    }
+    return PDPD_OK;
+}
+
+uint64_t pdpd_kernel_launches(pdpd_engine *e)
+{
+    return e ? e->launches : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,427 @@
+// FP32 engine kernels.
+//
+// State per bead (sorted by cell, ascending bead id inside a cell):
+//   pos = (ox, oy, oz, hash)  -- FP32 offset inside the bead's integer cell, in [0, 1)
+//   vel = (vx, vy, vz, 0), frc = (fx, fy, fz, 0), cellg = global cell index, ids = bead id.
+// Positions are integer cell + FP32 offset, so the resolution of a position does not depend
+// on the box size: a pair separation is (o_i - o_j) - (cell_j - cell_i), an O(1) quantity.
+//
+// One timestep (the reference's step_impl, naive_dpd_engine_half_step.hpp:239-356):
+//   update_pos -> re-bin -> pair forces -> bond forces -> update_mom.
+// Here the force kernel finishes step t (pair + bond forces of x(t+1), v(t+1) = vh + f dt/2)
+// and, unless it is the last step of a run, goes straight on with update_pos of step t+1 and
+// counts the bead into its new cell; the counting sort (pdpd_sort.cu) then re-bins.
+#include <cmath>
+
+#include "pdpd_device.cuh"
+
+namespace pdpd {
+namespace {
+
+constexpr int MAX_PAIR = 256;  // n_types <= 16
+
+struct WorldCache {
+    WorldDev w;
+    uint32_t world;
+};
+
+__device__ __forceinline__ void load_world(const KArgs &a, uint32_t world, WorldCache &wc,
+                                           float2 *s_pair)
+{
+    // Block-uniform: every thread sees the same tile.
+    if (wc.world != world) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            wc.w = a.worlds[world];
+            wc.world = world;
+        }
+        __syncthreads();
+        const uint32_t np = wc.w.n_types * wc.w.n_types;
+        const float2 *pair = (const float2 *)a.pair;
+        for (uint32_t i = threadIdx.x; i < np && i < MAX_PAIR; i += blockDim.x)
+            s_pair[i] = pair[wc.w.param_base + i];
+        __syncthreads();
+    }
+}
+
+// update_pos (dpd_maths_core_half_step.hpp:22-49) in cell + offset form:
+//   x' = x + v dt + f dt^2/2, wrapped into the box; returns the new global cell.
+__device__ __forceinline__ uint32_t advance_position(const WorldDev &w, float dt, float hdt2,
+                                                     const int c[3], float o[3], const float v[3],
+                                                     const float f[3], uint32_t &err)
+{
+    int nc[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        float on = o[d] + (v[d] * dt + f[d] * hdt2);
+        if (!(fabsf(on) < 1.0e6f)) {  // also catches NaN / inf
+            err |= ERR_NONFINITE;
+            on = 0.5f;
+        }
+        float fl = floorf(on);
+        on -= fl;
+        if (on >= 1.0f) on = 0x1.fffffep-1f;  // offset rounded up to 1: stay below it
+        if (on < 0.0f) on = 0.0f;
+        o[d] = on;
+        nc[d] = wrap_index(c[d] + (int)fl, w.L[d]);
+    }
+    return w.cell_base + ((uint32_t)nc[0] * (uint32_t)w.L[1] + (uint32_t)nc[1]) * (uint32_t)w.L[2] +
+           (uint32_t)nc[2];
+}
+
+// Position of bead `slot` relative to a bead at (cell c, offset o), using the
+// minimum-image integer cell difference.
+__device__ __forceinline__ void rel_pos(const WorldDev &w, const float4 *__restrict__ pos,
+                                        const uint32_t *__restrict__ cellg, uint32_t slot,
+                                        const int c[3], const float o[3], float r[3])
+{
+    float4 p = pos[slot];
+    int pc[3];
+    decode_cell(cellg[slot] - w.cell_base, w.L, pc[0], pc[1], pc[2]);
+    const float po[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        int dc = pc[d] - c[d];
+        if (2 * dc > w.L[d]) dc -= w.L[d];
+        if (2 * dc < -w.L[d]) dc += w.L[d];
+        r[d] = (float)dc + (po[d] - o[d]);
+    }
+}
+
+// calc_distance_from_to's periodic rule (naive_dpd_engine_half_step.hpp:198-209).
+__device__ __forceinline__ void min_image(const WorldDev &w, float d[3])
+{
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float L = (float)w.L[k];
+        if (d[k] > L * 0.5f)
+            d[k] -= L;
+        else if (d[k] < -L * 0.5f)
+            d[k] += L;
+    }
+}
+
+// Bond forces on one bead from its CSR row (update_hookean_bond / update_angle_bond,
+// naive_dpd_engine_half_step.hpp:426-483; calc_angle_force dpd_maths_core_half_step.hpp:177-229).
+__device__ void bond_forces32(const KArgs &a, const WorldDev &w, uint32_t id, const int c[3],
+                              const float o[3], float F[3], uint32_t &err)
+{
+    const float4 *pos = (const float4 *)a.posA;
+    const float4 *prm_tab = (const float4 *)a.bond_params;
+    const uint32_t r0 = a.bond_row[id], r1 = a.bond_row[id + 1];
+    for (uint32_t r = r0; r < r1; r++) {
+        const BondTerm bt = a.bond_terms[r];
+        const float4 prm = prm_tab[bt.param];
+        const uint32_t kind = bt.meta & 0xffu, role = bt.meta >> 8;
+        float ra[3], rb[3] = {0.f, 0.f, 0.f};
+        rel_pos(w, pos, a.cellg, a.slot_of_id[bt.a], c, o, ra);
+        if (kind == 0) {
+            // Hookean: dx = tail - head; head gets -f, tail +f, f = dx * kappa (r0 - r) / r.
+            float dx[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) dx[d] = role == 0 ? ra[d] : -ra[d];
+            min_image(w, dx);
+            float dr = sqrtf(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+            if (dr > 2.0f) err |= ERR_BOND_SNAPPED;
+            float s = (prm.x * (prm.y - dr)) / dr;
+            float sign = role == 0 ? -1.0f : 1.0f;
+#pragma unroll
+            for (int d = 0; d < 3; d++) F[d] += sign * (dx[d] * s);
+        } else {
+            rel_pos(w, pos, a.cellg, a.slot_of_id[bt.b], c, o, rb);
+            float xh[3], xm[3], xt[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                xh[d] = role == 0 ? 0.f : ra[d];
+                xm[d] = role == 0 ? ra[d] : (role == 1 ? 0.f : rb[d]);
+                xt[d] = role == 2 ? 0.f : rb[d];
+            }
+            float b1[3], b2[3];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                b1[d] = xm[d] - xh[d];
+                b2[d] = xt[d] - xm[d];
+            }
+            min_image(w, b1);
+            min_image(w, b2);
+            float r01 = sqrtf(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
+            float r12 = sqrtf(b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2]);
+            float mag = r01 * r12;
+            if (mag > 0.0001f) {
+                float dot = b1[0] * b2[0] + b1[1] * b2[1] + b1[2] * b2[2];
+                float p1 = dot / (r01 * r01);
+                float p2 = dot / (r12 * r12);
+                float fm = prm.x / mag;
+                if (fabsf(dot) > 0.000001f && prm.z > 0.0f) {
+                    // 1/sqrt(1/cos^2 phi - 1) loses all precision in FP32 as the bonds turn
+                    // collinear: evaluate the normalisation in FP64.
+                    double b1d[3] = {b1[0], b1[1], b1[2]}, b2d[3] = {b2[0], b2[1], b2[2]};
+                    double dd = b1d[0] * b2d[0] + b1d[1] * b2d[1] + b1d[2] * b2d[2];
+                    double n1 = b1d[0] * b1d[0] + b1d[1] * b1d[1] + b1d[2] * b1d[2];
+                    double n2 = b2d[0] * b2d[0] + b2d[1] * b2d[1] + b2d[2] * b2d[2];
+                    double cos_phi_sq = (dd * dd) / (n1 * n2);
+                    double ip = 1.0 / sqrt(1.0 / cos_phi_sq - 1.0);
+                    fm = (float)((double)fm * ((double)prm.y - (double)prm.z * ip));
+                }
+                float hf[3], tf[3];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    hf[d] = (b1[d] * p1 - b2[d]) * fm;
+                    tf[d] = (b1[d] - b2[d] * p2) * fm;
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    float add = role == 0 ? hf[d] : (role == 2 ? tf[d] : -(hf[d] + tf[d]));
+                    F[d] += add;
+                }
+            }
+        }
+    }
+}
+
+// Pair forces on one bead: full-shell gather over the 27 neighbour cells in the reference's
+// direction order, beads of a cell in id order (naive_dpd_engine_half_step.hpp:300-315,
+// 358-424; calc_force dpd_maths_core_half_step.hpp:69-157).
+__device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
+                                              const float2 *s_pair, uint32_t th_lo,
+                                              uint32_t th_hi, float scale, const int c[3],
+                                              const float4 ph, const float4 vh, float F[3])
+{
+    const float4 *__restrict__ pos = (const float4 *)a.posA;
+    const float4 *__restrict__ vel = (const float4 *)a.velA;
+    const uint32_t *__restrict__ start = a.start;
+    const uint32_t hh = __float_as_uint(ph.w);
+    const uint32_t nt = w.n_types;
+    const uint32_t ti = min(hh >> 28, nt - 1u);
+    const float min2 = min_dist_sqr_f();
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    for (int ddx = -1; ddx <= 1; ddx++) {
+        const int nx = wrap_index(c[0] + ddx, w.L[0]);
+        const float ax = ph.x - (float)ddx;
+        for (int ddy = -1; ddy <= 1; ddy++) {
+            const int ny = wrap_index(c[1] + ddy, w.L[1]);
+            const float ay = ph.y - (float)ddy;
+            const uint32_t row = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2];
+            for (int ddz = -1; ddz <= 1; ddz++) {
+                const int nz = wrap_index(c[2] + ddz, w.L[2]);
+                const float az = ph.z - (float)ddz;
+                const uint32_t nc = row + (uint32_t)nz;
+                const uint32_t j1 = start[nc + 1];
+                for (uint32_t j = start[nc]; j < j1; j++) {
+                    const float4 pj = pos[j];
+                    const float dx = ax - pj.x, dy = ay - pj.y, dz = az - pj.z;
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 < 1.0f && r2 >= min2) {
+                        const float4 vj = vel[j];
+                        const uint32_t hj = __float_as_uint(pj.w);
+                        const float2 pp = s_pair[ti * nt + min(hj >> 28, nt - 1u)];
+                        const float inv_r = rsqrtf(r2);
+                        const float r = r2 * inv_r;
+                        const float wr = 1.0f - r;
+                        const float ex = dx * inv_r, ey = dy * inv_r, ez = dz * inv_r;
+                        const float rdotv = ex * (vh.x - vj.x) + ey * (vh.y - vj.y) + ez * (vh.z - vj.z);
+                        const float sg = pp.y * wr;
+                        const float u = hash_u(th_lo, th_hi, hh, hj);
+                        const float scaled = pp.x * wr - sg * sg * rdotv + (sg * scale) * u;
+                        fx += ex * scaled;
+                        fy += ey * scaled;
+                        fz += ez * scaled;
+                    }
+                }
+            }
+        }
+    }
+    F[0] = fx;
+    F[1] = fy;
+    F[2] = fz;
+}
+
+template <int FINAL>
+__global__ void __launch_bounds__(128) k_force32(KArgs a)
+{
+    __shared__ float2 s_pair[MAX_PAIR];
+    __shared__ WorldCache wc;
+    if (threadIdx.x == 0) wc.world = 0xffffffffu;
+    __syncthreads();
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        load_world(a, tl.world, wc, s_pair);
+        const WorldDev &w = wc.w;
+        const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
+        const float scale = (float)w.scale_inv_sqrt_dt;
+        const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+        const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
+        uint32_t err = 0;
+        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const float4 ph = ((const float4 *)a.posA)[s];
+            const float4 vh = ((const float4 *)a.velA)[s];
+            int c[3];
+            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+            float F[3];
+            pair_forces32(a, w, s_pair, th_lo, th_hi, scale, c, ph, vh, F);
+            float o[3] = {ph.x, ph.y, ph.z};
+            if (!(__float_as_uint(ph.w) & (1u << 27)))  // polymer bead: bonds
+                bond_forces32(a, w, a.ids[s], c, o, F, err);
+            // update_mom (dpd_maths_core_half_step.hpp:51-61)
+            float v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+            if (FINAL) {
+                ((float4 *)a.velB)[s] = make_float4(v[0], v[1], v[2], 0.f);
+                ((float4 *)a.frc)[s] = make_float4(F[0], F[1], F[2], 0.f);
+                if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
+            } else {
+                const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
+                const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+                ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
+                ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
+                a.keyrank[s] = make_uint2(key, rank);
+            }
+        }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+// First update_pos of a run, from the rest state x(t), v(t), f(t).
+__global__ void __launch_bounds__(128) k_begin32(KArgs a)
+{
+    __shared__ float2 s_pair[MAX_PAIR];
+    __shared__ WorldCache wc;
+    if (threadIdx.x == 0) wc.world = 0xffffffffu;
+    __syncthreads();
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        load_world(a, tl.world, wc, s_pair);
+        const WorldDev &w = wc.w;
+        const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
+        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
+        uint32_t err = 0;
+        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const float4 ph = ((const float4 *)a.posA)[s];
+            const float4 vh = ((const float4 *)a.velA)[s];
+            const float4 fh = ((const float4 *)a.frc)[s];
+            int c[3];
+            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+            float o[3] = {ph.x, ph.y, ph.z};
+            const float v[3] = {vh.x, vh.y, vh.z};
+            const float F[3] = {fh.x, fh.y, fh.z};
+            const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
+            const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+            ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
+            ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
+            a.keyrank[s] = make_uint2(key, rank);
+        }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+// Attach: id-ordered FP64 staging (x, v, f) -> B in slot = id order, with cell counts.
+__global__ void k_bin32(KArgs a, const uint32_t *__restrict__ hash_in)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.n_beads) return;
+    // world of bead g: worlds are in bead_base order
+    uint32_t lo = 0, hi = a.n_worlds;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) / 2;
+        if (a.worlds[mid].bead_base <= g) lo = mid; else hi = mid;
+    }
+    const WorldDev &w = a.worlds[lo];
+    const double *st = a.staging + 9 * (size_t)g;
+    int c[3];
+    float o[3];
+    uint32_t err = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double x = st[d];
+        if (!(x >= 0.0 && x < (double)w.L[d])) {
+            err |= ERR_OUT_OF_BOX;
+            x = 0.0;
+        }
+        double fl = floor(x);
+        c[d] = (int)fl;
+        float off = (float)(x - fl);
+        if (off >= 1.0f) off = 0x1.fffffep-1f;
+        o[d] = off;
+    }
+    if (err) atomicOr(&a.worlds[lo].err, err);
+    const uint32_t key = w.cell_base + ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
+    const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+    ((float4 *)a.posB)[g] = make_float4(o[0], o[1], o[2], __uint_as_float(hash_in[g]));
+    ((float4 *)a.velB)[g] = make_float4((float)st[3], (float)st[4], (float)st[5], 0.f);
+    ((float4 *)a.frcB)[g] = make_float4((float)st[6], (float)st[7], (float)st[8], 0.f);
+    a.ids[g] = g;
+    a.keyrank[g] = make_uint2(key, rank);
+}
+
+__global__ void k_finish32(KArgs a)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.n_beads) ((float4 *)a.velA)[s] = ((const float4 *)a.velB)[s];
+    if (blockIdx.x == 0)
+        for (uint32_t w = threadIdx.x; w < a.n_worlds; w += blockDim.x) a.worlds[w].t += 1;
+}
+
+// Rest state -> id-ordered FP64 staging (x, v, f): x = cell + offset exactly.
+__global__ void __launch_bounds__(128) k_unsort32(KArgs a)
+{
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const WorldDev &w = a.worlds[tl.world];
+        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
+        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const float4 p = ((const float4 *)a.posA)[s];
+            const float4 v = ((const float4 *)a.velA)[s];
+            const float4 f = ((const float4 *)a.frc)[s];
+            int c[3];
+            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+            double *st = a.staging + 9 * (size_t)a.ids[s];
+            st[0] = (double)c[0] + (double)p.x;
+            st[1] = (double)c[1] + (double)p.y;
+            st[2] = (double)c[2] + (double)p.z;
+            st[3] = v.x;
+            st[4] = v.y;
+            st[5] = v.z;
+            st[6] = f.x;
+            st[7] = f.y;
+            st[8] = f.z;
+        }
+    }
+}
+
+}  // namespace
+
+int launch_bin32(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
+{
+    if (a.n_beads == 0) return 0;
+    k_bin32<<<(a.n_beads + 255) / 256, 256, 0, s>>>(a, hash_in);
+    return 1;
+}
+
+int launch_begin32(const KArgs &a, cudaStream_t s)
+{
+    k_begin32<<<a.grid_blocks, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_force32(const KArgs &a, int final_step, cudaStream_t s)
+{
+    if (final_step)
+        k_force32<1><<<a.grid_blocks, 128, 0, s>>>(a);
+    else
+        k_force32<0><<<a.grid_blocks, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_finish32(const KArgs &a, cudaStream_t s)
+{
+    k_finish32<<<(a.n_beads + 255) / 256 + 1, 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_unsort32(const KArgs &a, cudaStream_t s)
+{
+    k_unsort32<<<a.grid_blocks, 128, 0, s>>>(a);
+    return 1;
+}
+
+}  // namespace pdpd

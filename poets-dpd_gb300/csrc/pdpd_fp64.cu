@@ -1,0 +1,408 @@
+// FP64 engine kernels.
+//
+// Same pipeline as the FP32 engine, but with absolute FP64 positions in [0, L) and every
+// floating-point operation in the order the reference's FP64 half-step engine performs it
+// (naive_dpd_engine_half_step.hpp, dpd_maths_core_half_step.hpp).  This translation unit is
+// compiled with -fmad=false, so no multiply-add is fused; with the canonical cell order
+// (ascending bead id inside a cell) each bead's force is summed in the reference's order and
+// the trajectory is bit-identical to the reference's.
+//
+// State per bead (sorted): pos = (x, y, z, hash as the low bits of w), vel = (v, 0),
+// frc = (f, 0).
+#include <cmath>
+
+#include "pdpd_device.cuh"
+
+namespace pdpd {
+namespace {
+
+constexpr int MAX_PAIR = 256;
+
+struct WorldCache {
+    WorldDev w;
+    uint32_t world;
+};
+
+__device__ __forceinline__ uint32_t hash_of(const Vec4d &p)
+{
+    return (uint32_t)__double_as_longlong(p.w);
+}
+
+__device__ __forceinline__ void load_world(const KArgs &a, uint32_t world, WorldCache &wc,
+                                           Vec2d *s_pair)
+{
+    if (wc.world != world) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            wc.w = a.worlds[world];
+            wc.world = world;
+        }
+        __syncthreads();
+        const uint32_t np = wc.w.n_types * wc.w.n_types;
+        const Vec2d *pair = (const Vec2d *)a.pair;
+        for (uint32_t i = threadIdx.x; i < np && i < MAX_PAIR; i += blockDim.x)
+            s_pair[i] = pair[wc.w.param_base + i];
+        __syncthreads();
+    }
+}
+
+// update_pos (dpd_maths_core_half_step.hpp:22-49): x' = (x + v dt) + f (dt dt / 2), with the
+// reference's single periodic wrap.  Returns the global cell of x'.
+__device__ __forceinline__ uint32_t advance_position64(const WorldDev &w, double dt, double hdt2,
+                                                       double x[3], const double v[3],
+                                                       const double f[3], uint32_t &err)
+{
+    int c[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const double L = (double)w.L[d];
+        double xn = x[d] + v[d] * dt + f[d] * hdt2;
+        if (xn < 0) {
+            xn += L;
+            if (xn == L) xn = 0;
+        } else if (xn >= L) {
+            xn -= L;
+        }
+        if (!(xn >= 0.0 && xn < L)) {  // moved more than a box, or non-finite
+            err |= ERR_OUT_OF_BOX;
+            xn = 0.0;
+        }
+        x[d] = xn;
+        c[d] = (int)floor(xn);
+    }
+    return w.cell_base + ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] +
+           (uint32_t)c[2];
+}
+
+// calc_distance_from_to (naive_dpd_engine_half_step.hpp:198-209).
+__device__ __forceinline__ void distance_from_to(const WorldDev &w, const double base[3],
+                                                 const double other[3], double res[3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const double len = (double)w.L[i];
+        const double dx = other[i] - base[i];
+        const int wrap_neg = dx > len * 0.5;
+        const int wrap_pos = dx < -len * 0.5;
+        res[i] = dx + (double)(wrap_pos - wrap_neg) * len;
+    }
+}
+
+__device__ __forceinline__ void load_x(const Vec4d *__restrict__ pos, uint32_t slot, double x[3])
+{
+    const Vec4d p = pos[slot];
+    x[0] = p.x;
+    x[1] = p.y;
+    x[2] = p.z;
+}
+
+// Bond forces on one bead, in the order of its CSR row (Hookean bonds, then angle bonds),
+// each term evaluated exactly as update_hookean_bond / update_angle_bond
+// (naive_dpd_engine_half_step.hpp:426-483) and calc_angle_force
+// (dpd_maths_core_half_step.hpp:177-229).
+__device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, const double xs[3],
+                              double F[3], uint32_t &err)
+{
+    const Vec4d *pos = (const Vec4d *)a.posA;
+    const Vec4d *prm_tab = (const Vec4d *)a.bond_params;
+    const uint32_t r0 = a.bond_row[id], r1 = a.bond_row[id + 1];
+    for (uint32_t r = r0; r < r1; r++) {
+        const BondTerm bt = a.bond_terms[r];
+        const Vec4d prm = prm_tab[bt.param];
+        const uint32_t kind = bt.meta & 0xffu, role = bt.meta >> 8;
+        double xa[3], xb[3];
+        load_x(pos, a.slot_of_id[bt.a], xa);
+        if (kind == 0) {
+            const double *xh = role == 0 ? xs : xa;
+            const double *xt = role == 0 ? xa : xs;
+            double dx[3];
+            distance_from_to(w, xh, xt, dx);
+            const double dr = sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+            if (dr > 2.0) err |= ERR_BOND_SNAPPED;
+            const double dr0 = prm.y - dr;
+            const double hookean_force = prm.x * dr0;
+            const double s = hookean_force / dr;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const double fd = dx[d] * s;
+                F[d] = role == 0 ? F[d] - fd : F[d] + fd;
+            }
+        } else {
+            load_x(pos, a.slot_of_id[bt.b], xb);
+            const double *xh = role == 0 ? xs : xa;
+            const double *xm = role == 0 ? xa : (role == 1 ? xs : xb);
+            const double *xt = role == 2 ? xs : xb;
+            double first[3], second[3];
+            distance_from_to(w, xh, xm, first);
+            distance_from_to(w, xm, xt, second);
+            const double r01 = sqrt(first[0] * first[0] + first[1] * first[1] + first[2] * first[2]);
+            const double r12 = sqrt(second[0] * second[0] + second[1] * second[1] + second[2] * second[2]);
+            const double kappa = prm.x, cos_theta0 = prm.y, sin_theta0 = prm.z;
+            double hf[3] = {0, 0, 0}, tf[3] = {0, 0, 0}, mf[3] = {0, 0, 0};
+            const double mag_product = r01 * r12;
+            if (mag_product > 0.0001) {
+                const double b1_mag_sq = r01 * r01;
+                const double b2_mag_sq = r12 * r12;
+                const double b1_dot_b2 = first[0] * second[0] + first[1] * second[1] + first[2] * second[2];
+                const double p1 = b1_dot_b2 / b1_mag_sq;
+                const double p2 = b1_dot_b2 / b2_mag_sq;
+                const double cos_phi_sq = p1 * p2;
+                double force_mag = kappa / mag_product;
+                if (fabs(b1_dot_b2) > 0.000001 && sin_theta0 > 0) {
+                    const double inv_prefactor = 1.0 / sqrt(1.0 / cos_phi_sq - 1.0);
+                    force_mag = force_mag * (cos_theta0 - sin_theta0 * inv_prefactor);
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    hf[d] = (first[d] * p1 - second[d]) * force_mag;
+                    tf[d] = (first[d] - second[d] * p2) * force_mag;
+                    mf[d] = -(hf[d] + tf[d]);
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < 3; d++) F[d] = F[d] + (role == 0 ? hf[d] : (role == 1 ? mf[d] : tf[d]));
+        }
+    }
+}
+
+// Pair forces on one bead: for each of the 27 directions in (-1..1)^3 order, for each bead
+// of that cell in id order: the reference's update_cell_forces + calc_force, with
+// kappa = 0, r0 = 0.5 (naive_dpd_engine_half_step.hpp:358-424).
+__device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
+                                              const Vec2d *s_pair, uint32_t th_lo, uint32_t th_hi,
+                                              double scale_inv_sqrt_dt, const int c[3],
+                                              const double xh[3], const Vec4d &vh, uint32_t hh,
+                                              double F[3])
+{
+    const Vec4d *__restrict__ pos = (const Vec4d *)a.posA;
+    const Vec4d *__restrict__ vel = (const Vec4d *)a.velA;
+    const uint32_t *__restrict__ start = a.start;
+    const uint32_t nt = w.n_types;
+    const uint32_t ti = min(hh >> 28, nt - 1u);
+    const double min2 = (double)min_dist_sqr_f();
+    F[0] = F[1] = F[2] = 0.0;
+    int dir[3];
+    for (dir[0] = -1; dir[0] <= 1; dir[0]++)
+        for (dir[1] = -1; dir[1] <= 1; dir[1]++)
+            for (dir[2] = -1; dir[2] <= 1; dir[2]++) {
+                int op[3];
+                double delta[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) {  // make_relative_cell_pos (:181-196)
+                    const int raw = c[i] + dir[i];
+                    const int is_left = raw < 0;
+                    const int is_right = raw == w.L[i];
+                    op[i] = raw + (is_left - is_right) * w.L[i];
+                    delta[i] = (double)(is_right - is_left) * (double)w.L[i];
+                }
+                const uint32_t nc = w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] + (uint32_t)op[2];
+                const uint32_t j1 = start[nc + 1];
+                for (uint32_t j = start[nc]; j < j1; j++) {
+                    const Vec4d pj = pos[j];
+                    const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
+                    const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
+                    const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+                    if (dr2 >= 1 || dr2 < min2) continue;
+                    const double dr = sqrt(dr2);
+                    const Vec4d vj = vel[j];
+                    const uint32_t hj = hash_of(pj);
+                    const Vec2d pp = s_pair[ti * nt + min(hj >> 28, nt - 1u)];
+                    const double kappa = 0.0, r0 = 0.5;
+                    const double inv_dr = 1.0 / dr;
+                    const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
+                    const double wr = 1.0 - dr;
+                    const double con_force = pp.x * wr;
+                    const double e0 = dx0 * inv_dr, e1 = dx1 * inv_dr, e2 = dx2 * inv_dr;
+                    const double rdotv = e0 * dv0 + e1 * dv1 + e2 * dv2;
+                    const double sqrt_gammap = pp.y * wr;
+                    const double diss_force = -sqrt_gammap * sqrt_gammap * rdotv;
+                    const double u = (double)hash_u(th_lo, th_hi, hh, hj);
+                    const double rand_scale = sqrt_gammap * scale_inv_sqrt_dt;
+                    const double rand_force = rand_scale * u;
+                    const double dr0 = r0 - dr;
+                    const double hookean_force = kappa * dr0;
+                    const double scaled = con_force + diss_force + rand_force + hookean_force;
+                    F[0] = F[0] + e0 * scaled;
+                    F[1] = F[1] + e1 * scaled;
+                    F[2] = F[2] + e2 * scaled;
+                }
+            }
+}
+
+template <int FINAL>
+__global__ void __launch_bounds__(128) k_force64(KArgs a)
+{
+    __shared__ Vec2d s_pair[MAX_PAIR];
+    __shared__ WorldCache wc;
+    if (threadIdx.x == 0) wc.world = 0xffffffffu;
+    __syncthreads();
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        load_world(a, tl.world, wc, s_pair);
+        const WorldDev &w = wc.w;
+        const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+        const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+        const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
+        uint32_t err = 0;
+        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const Vec4d ph = ((const Vec4d *)a.posA)[s];
+            const Vec4d vh = ((const Vec4d *)a.velA)[s];
+            const uint32_t hh = hash_of(ph);
+            int c[3];
+            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+            double x[3] = {ph.x, ph.y, ph.z};
+            double F[3];
+            pair_forces64(a, w, s_pair, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, vh, hh, F);
+            if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
+            // update_mom: v += f * half(dt)
+            double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+            if (FINAL) {
+                Vec4d vo = {v[0], v[1], v[2], 0.0};
+                Vec4d fo = {F[0], F[1], F[2], 0.0};
+                ((Vec4d *)a.velB)[s] = vo;
+                ((Vec4d *)a.frc)[s] = fo;
+                if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
+            } else {
+                const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
+                const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+                Vec4d po = {x[0], x[1], x[2], ph.w};
+                Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
+                ((Vec4d *)a.posB)[s] = po;
+                ((Vec4d *)a.velB)[s] = vo;
+                a.keyrank[s] = make_uint2(key, rank);
+            }
+        }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_begin64(KArgs a)
+{
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const WorldDev w = a.worlds[tl.world];
+        const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
+        uint32_t err = 0;
+        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+            const Vec4d ph = ((const Vec4d *)a.posA)[s];
+            const Vec4d vh = ((const Vec4d *)a.velA)[s];
+            const Vec4d fh = ((const Vec4d *)a.frc)[s];
+            double x[3] = {ph.x, ph.y, ph.z};
+            const double v[3] = {vh.x, vh.y, vh.z};
+            const double F[3] = {fh.x, fh.y, fh.z};
+            const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
+            const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+            Vec4d po = {x[0], x[1], x[2], ph.w};
+            Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
+            ((Vec4d *)a.posB)[s] = po;
+            ((Vec4d *)a.velB)[s] = vo;
+            a.keyrank[s] = make_uint2(key, rank);
+        }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+__global__ void k_bin64(KArgs a, const uint32_t *__restrict__ hash_in)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.n_beads) return;
+    uint32_t lo = 0, hi = a.n_worlds;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) / 2;
+        if (a.worlds[mid].bead_base <= g) lo = mid; else hi = mid;
+    }
+    const WorldDev &w = a.worlds[lo];
+    const double *st = a.staging + 9 * (size_t)g;
+    int c[3];
+    double x[3];
+    uint32_t err = 0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double xd = st[d];
+        if (!(xd >= 0.0 && xd < (double)w.L[d])) {
+            err |= ERR_OUT_OF_BOX;
+            xd = 0.0;
+        }
+        x[d] = xd;
+        c[d] = (int)floor(xd);
+    }
+    if (err) atomicOr(&a.worlds[lo].err, err);
+    const uint32_t key = w.cell_base + ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
+    const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+    Vec4d po = {x[0], x[1], x[2], __longlong_as_double((long long)hash_in[g])};
+    Vec4d vo = {st[3], st[4], st[5], 0.0};
+    Vec4d fo = {st[6], st[7], st[8], 0.0};
+    ((Vec4d *)a.posB)[g] = po;
+    ((Vec4d *)a.velB)[g] = vo;
+    ((Vec4d *)a.frcB)[g] = fo;
+    a.ids[g] = g;
+    a.keyrank[g] = make_uint2(key, rank);
+}
+
+__global__ void k_finish64(KArgs a)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < a.n_beads) ((Vec4d *)a.velA)[s] = ((const Vec4d *)a.velB)[s];
+    if (blockIdx.x == 0)
+        for (uint32_t w = threadIdx.x; w < a.n_worlds; w += blockDim.x) a.worlds[w].t += 1;
+}
+
+__global__ void k_unsort64(KArgs a)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_beads) return;
+    const Vec4d p = ((const Vec4d *)a.posA)[s];
+    const Vec4d v = ((const Vec4d *)a.velA)[s];
+    const Vec4d f = ((const Vec4d *)a.frc)[s];
+    double *st = a.staging + 9 * (size_t)a.ids[s];
+    st[0] = p.x;
+    st[1] = p.y;
+    st[2] = p.z;
+    st[3] = v.x;
+    st[4] = v.y;
+    st[5] = v.z;
+    st[6] = f.x;
+    st[7] = f.y;
+    st[8] = f.z;
+}
+
+}  // namespace
+
+int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
+{
+    if (a.n_beads == 0) return 0;
+    k_bin64<<<(a.n_beads + 255) / 256, 256, 0, s>>>(a, hash_in);
+    return 1;
+}
+
+int launch_begin64(const KArgs &a, cudaStream_t s)
+{
+    k_begin64<<<a.grid_blocks, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_force64(const KArgs &a, int final_step, cudaStream_t s)
+{
+    if (final_step)
+        k_force64<1><<<a.grid_blocks, 128, 0, s>>>(a);
+    else
+        k_force64<0><<<a.grid_blocks, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_finish64(const KArgs &a, cudaStream_t s)
+{
+    k_finish64<<<(a.n_beads + 255) / 256 + 1, 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_unsort64(const KArgs &a, cudaStream_t s)
+{
+    if (a.n_beads == 0) return 0;
+    k_unsort64<<<(a.n_beads + 255) / 256, 256, 0, s>>>(a);
+    return 1;
+}
+
+}  // namespace pdpd

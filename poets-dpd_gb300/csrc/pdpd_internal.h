@@ -1,0 +1,114 @@
+// Internal interface between the host runtime (pdpd_engine.cpp) and the kernel
+// translation units (pdpd_fp32.cu, pdpd_fp64.cu, pdpd_sort.cu).  Not part of the C ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace pdpd {
+
+// Per-world parameters and state, resident on the device.  Worlds of a batch share one
+// arena: world w owns global cells [cell_base, cell_base+n_cells) and global bead slots /
+// ids [bead_base, bead_base+n_beads).
+struct WorldDev {
+    int32_t L[3];
+    uint32_t cell_base;
+    uint32_t n_cells;
+    uint32_t bead_base;
+    uint32_t n_beads;
+    uint32_t n_types;
+    uint32_t param_base;  // first entry of this world's n_types^2 pair parameters
+    uint32_t err;         // device-side error flags (ERR_*)
+    double dt;
+    double scale_inv_sqrt_dt;  // sqrt(24 kT / dt), kT = 1 (dpd_maths_core.hpp:24)
+    uint64_t seed;
+    int64_t t;
+};
+
+// A run of consecutive cells of one world: the unit of work of the tile kernels.
+struct Tile {
+    uint32_t world;
+    uint32_t cell_begin;  // global cell index
+    uint32_t cell_end;
+    uint32_t pad;
+};
+
+enum ErrFlags : uint32_t {
+    ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
+    ERR_NONFINITE = 2u,     // non-finite position / velocity / force
+    ERR_OUT_OF_BOX = 4u,    // a bead outside [0, L) on attach, or moved more than a box
+};
+
+// Bond term of the per-bead CSR: what one bead contributes to itself from one Hookean bond
+// or one angle bond.  kind: 0 Hookean, 1 angle.  role: Hookean 0 head / 1 tail; angle
+// 0 head / 1 middle / 2 tail.  a, b: the other bead ids of the term in (head, middle,
+// tail) order.  param: index into the bond parameter table.
+struct BondTerm {
+    uint32_t meta;  // kind | role << 8
+    uint32_t a;
+    uint32_t b;
+    uint32_t param;
+};
+
+// Everything a step kernel needs.  Pointers are device pointers; the payload arrays are
+// float4 (FP32 engine) or Vec4d (FP64 engine).
+struct KArgs {
+    WorldDev *worlds;
+    uint32_t n_worlds;
+    const Tile *tiles;
+    uint32_t n_tiles;
+    uint32_t n_beads;  // total over all worlds
+    uint32_t n_cells;  // total over all worlds
+    uint32_t *start;   // n_cells+1: first slot of each cell (sorted order); start[n_cells] = n_beads
+    uint32_t *cnt;     // n_cells: bead counts of the next cell list (zero between steps)
+    uint32_t *blocksums;
+    // sorted state (A)
+    void *posA, *velA, *frc;
+    uint32_t *ids;       // bead id of each sorted slot
+    uint32_t *cellg;     // global cell of each sorted slot
+    uint32_t *slot_of_id;
+    // advanced, not yet sorted state (B), indexed by the A slot it came from
+    void *posB, *velB, *frcB;
+    uint2 *keyrank;      // (new global cell, arrival rank in that cell)
+    uint4 *tmp;          // (old slot, id, cell, 0) placed by provisional rank
+    // bonds
+    const uint32_t *bond_row;  // n_beads+1 CSR rows by global id
+    const BondTerm *bond_terms;
+    const void *bond_params;   // float4 / Vec4d: (kappa, r0 | cos theta0, sin theta0, 0)
+    const void *pair;          // float2 / Vec2d: (a_ij, sqrt(gamma_ij))
+    // id-ordered staging for upload / download: 9 doubles per bead (x, v, f)
+    double *staging;
+    int block_threads;
+    int grid_blocks;     // persistent grid size for the tile kernels
+};
+
+// Kernel launchers.  Each returns the number of kernels it launched.
+//   bin:    id-ordered staging (x, v, f) -> B with counts      (attach)
+//   begin:  A rest state x(t), v(t), f(t) -> B with counts      (first update_pos of a run)
+//   force:  A -> B: forces, update_mom and (unless final) the next update_pos with counts;
+//           final: v(t+1) -> B.vel, f(t+1) -> frc
+//   finish: B.vel -> A.vel and t += 1                           (after a final force pass)
+//   unsort: A rest state -> id-ordered staging                  (download)
+//   sort:   B -> A counting sort (pdpd_sort.cu)
+int launch_bin32(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
+int launch_begin32(const KArgs &a, cudaStream_t s);
+int launch_force32(const KArgs &a, int final_step, cudaStream_t s);
+int launch_finish32(const KArgs &a, cudaStream_t s);
+int launch_unsort32(const KArgs &a, cudaStream_t s);
+int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
+int launch_begin64(const KArgs &a, cudaStream_t s);
+int launch_force64(const KArgs &a, int final_step, cudaStream_t s);
+int launch_finish64(const KArgs &a, cudaStream_t s);
+int launch_unsort64(const KArgs &a, cudaStream_t s);
+int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s);
+
+// Device RNG on arrays (device pointers), for known-answer tests.
+int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
+                    const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
+
+size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
+uint32_t scan_blocks(uint32_t n_cells);
+
+}  // namespace pdpd

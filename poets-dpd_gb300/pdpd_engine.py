@@ -1,0 +1,309 @@
+"""Python mirror of the reference's ``DPDEngine`` plug-in interface over the engine's C ABI.
+
+``GB300DPDEngine`` has the members of ``class DPDEngine`` (reference
+include/dpd/core/dpd_engine.hpp:10-216) with the same meaning:
+
+=========================  ==============================================================
+``CanSupport(world)``      "" if the world can be attached, else the reason (:57-128)
+``Attach(world)``          copy the world to the GPU; ``Attach(None)`` detaches (:177)
+``Run(n)``                 advance n steps; the world's x/v/f/t are updated on return (:185)
+``Run(count, size, cb)``   interval runs with a callback; returns steps done (:195-215)
+``GetMaxBondLength()``     2.0 (:130)
+``GetTimings()``           dict of ``timings_t`` fields (:38-46, :145-148)
+``GetConfigEntries()``     list of (name, description, value) (:160-164)
+``SetConfigEntry(k, v)``   raises on an unknown key (:166-169)
+=========================  ==============================================================
+
+Errors are raised as ``RuntimeError`` (the reference throws ``std::runtime_error``).  The
+shared library must exist (built by ``build.py``); there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpdpd_gb300.so")
+
+PDPD_FP32, PDPD_FP64 = 0, 1
+STATUS = {0: "PDPD_OK", 1: "PDPD_E_INVALID", 2: "PDPD_E_UNSUPPORTED", 3: "PDPD_E_CUDA",
+          4: "PDPD_E_STATE", 5: "PDPD_E_BOND_SNAPPED", 6: "PDPD_E_BEAD_LOST", 7: "PDPD_E_NOMEM"}
+
+# Every symbol include/pdpd_gpu.h declares.
+EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support",
+            "pdpd_max_bond_length", "pdpd_attach", "pdpd_attach_batch", "pdpd_run",
+            "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
+            "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
+            "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run"]
+
+
+class PdpdWorld(C.Structure):
+    _fields_ = [
+        ("box", C.c_int32 * 3), ("dt", C.c_double), ("lam", C.c_double), ("seed", C.c_uint64),
+        ("t", C.c_int64), ("n_bead_types", C.c_uint32), ("conservative", C.c_void_p),
+        ("dissipative", C.c_void_p), ("stationary", C.c_void_p), ("n_beads", C.c_uint32),
+        ("hash", C.c_void_p), ("x", C.c_void_p), ("v", C.c_void_p), ("f", C.c_void_p),
+        ("bead_stride_bytes", C.c_size_t), ("n_bonds", C.c_uint32), ("bond_beads", C.c_void_p),
+        ("bond_kappa", C.c_void_p), ("bond_r0", C.c_void_p), ("n_angles", C.c_uint32),
+        ("angle_beads", C.c_void_p), ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p),
+    ]
+
+
+class PdpdTimings(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("compile", "aquire", "configure",
+                                          "execute_to_first_bead", "execute_to_last_bead",
+                                          "perf_counters")]
+
+
+class PdpdPhaseTimes(C.Structure):
+    _fields_ = [("force_ms", C.c_double), ("sort_ms", C.c_double), ("other_ms", C.c_double),
+                ("force_launches", C.c_uint32), ("sort_launches", C.c_uint32)]
+
+
+INTERVAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)
+
+_LIB = None
+
+
+def lib():
+    """Load libpdpd_gb300.so.  Raises if it has not been built: the engine has no fallback."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run build.py (or __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+    sig = {
+        "pdpd_create": (i32, [i32, i32, C.POINTER(vp)]),
+        "pdpd_destroy": (None, [vp]),
+        "pdpd_last_error": (C.c_char_p, [vp]),
+        "pdpd_can_support": (i32, [C.POINTER(PdpdWorld), C.c_char_p, C.c_size_t]),
+        "pdpd_max_bond_length": (C.c_double, []),
+        "pdpd_attach": (i32, [vp, C.POINTER(PdpdWorld)]),
+        "pdpd_attach_batch": (i32, [vp, C.POINTER(PdpdWorld), u32]),
+        "pdpd_run": (i32, [vp, u32]),
+        "pdpd_run_async": (i32, [vp, u32]),
+        "pdpd_sync": (i32, [vp]),
+        "pdpd_stream": (vp, [vp]),
+        "pdpd_read_state": (i32, [vp, u32, vp, vp, vp, C.c_size_t, C.POINTER(C.c_int64)]),
+        "pdpd_run_intervals": (i32, [vp, C.c_int32, u32, vp, vp, vp, C.c_size_t, INTERVAL_FN, vp,
+                                     C.POINTER(u32)]),
+        "pdpd_get_timings": (i32, [vp, C.POINTER(PdpdTimings)]),
+        "pdpd_get_config": (i32, [vp, u32, C.c_char_p, C.c_size_t, C.c_char_p, C.c_size_t,
+                                  C.c_char_p, C.c_size_t]),
+        "pdpd_set_config": (i32, [vp, C.c_char_p, C.c_char_p]),
+        "pdpd_kernel_launches": (C.c_uint64, [vp]),
+        "pdpd_rng_eval": (i32, [C.c_size_t, vp, vp, vp, vp, vp, vp]),
+        "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+class _Flat:
+    """Contiguous arrays of one World in the C ABI's layout, kept alive with the struct."""
+
+    def __init__(self, world):
+        self.cons = np.ascontiguousarray(world.conservative, np.float64)
+        self.diss = np.ascontiguousarray(world.dissipative, np.float64)
+        self.stat = np.ascontiguousarray(world.stationary, np.uint8)
+        self.hash = np.ascontiguousarray(world.hashes(), np.uint32)
+        self.x = np.ascontiguousarray(world.x, np.float64)
+        self.v = np.ascontiguousarray(world.v, np.float64)
+        self.f = np.ascontiguousarray(world.f, np.float64)
+        bb, bk, br, ab, ak, at = world.flat_bonds()
+        self.bb = np.ascontiguousarray(bb, np.uint32)
+        self.bk, self.br = np.ascontiguousarray(bk), np.ascontiguousarray(br)
+        self.ab = np.ascontiguousarray(ab, np.uint32)
+        self.ak, self.at = np.ascontiguousarray(ak), np.ascontiguousarray(at)
+        s = PdpdWorld()
+        for i in range(3):
+            s.box[i] = int(world.box[i])
+        s.dt, s.lam = float(world.dt), float(world.lam)
+        s.seed, s.t = int(world.seed) & 0xFFFFFFFFFFFFFFFF, int(world.t)
+        s.n_bead_types = self.cons.shape[0]
+        s.conservative, s.dissipative, s.stationary = _p(self.cons), _p(self.diss), _p(self.stat)
+        s.n_beads = self.x.shape[0]
+        s.hash, s.x, s.v, s.f = _p(self.hash), _p(self.x), _p(self.v), _p(self.f)
+        s.bead_stride_bytes = 24
+        s.n_bonds, s.bond_beads, s.bond_kappa, s.bond_r0 = (self.bb.shape[0], _p(self.bb),
+                                                            _p(self.bk), _p(self.br))
+        s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (self.ab.shape[0], _p(self.ab),
+                                                                    _p(self.ak), _p(self.at))
+        self.struct = s
+
+
+def can_support(world) -> str:
+    """``DPDEngine::CanSupport``: empty string when the world can run on this engine."""
+    fl = _Flat(world)
+    buf = C.create_string_buffer(512)
+    rc = lib().pdpd_can_support(C.byref(fl.struct), buf, 512)
+    return "" if rc == 0 else buf.value.decode()
+
+
+def rng_eval(t, seed, a, b):
+    """The device RNG (hash_rng_sym and default_hash) on arrays; returns (h, u)."""
+    t = np.ascontiguousarray(t, np.uint32)
+    seed = np.ascontiguousarray(seed, np.uint64)
+    a = np.ascontiguousarray(a, np.uint32)
+    b = np.ascontiguousarray(b, np.uint32)
+    h = np.zeros(t.size, np.uint32)
+    u = np.zeros(t.size, np.float32)
+    rc = lib().pdpd_rng_eval(t.size, _p(t), _p(seed), _p(a), _p(b), _p(h), _p(u))
+    if rc != 0:
+        raise RuntimeError(f"pdpd_rng_eval: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
+    return h, u
+
+
+class GB300DPDEngine:
+    """A GPU DPD engine.  ``precision`` is ``"fp32"`` or ``"fp64"``."""
+
+    def __init__(self, precision="fp32", device=-1):
+        self.precision = precision
+        code = {"fp32": PDPD_FP32, "fp64": PDPD_FP64}[precision]
+        h = C.c_void_p()
+        rc = lib().pdpd_create(code, device, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"pdpd_create: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
+        self._h = h
+        self._worlds = []
+
+    # -- life-cycle ---------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pdpd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().pdpd_last_error(self._h).decode()
+            raise RuntimeError(f"{what}: {STATUS.get(rc, rc)}: {msg}")
+
+    # -- DPDEngine interface -----------------------------------------------------------
+    def CanSupport(self, world) -> str:
+        return can_support(world)
+
+    def GetMaxBondLength(self) -> float:
+        return lib().pdpd_max_bond_length()
+
+    def Attach(self, world):
+        if world is None:
+            self._check(lib().pdpd_attach(self._h, None), "Attach")
+            self._worlds = []
+            return
+        fl = _Flat(world)
+        self._check(lib().pdpd_attach(self._h, C.byref(fl.struct)), "Attach")
+        self._worlds = [world]
+
+    def AttachBatch(self, worlds):
+        flats = [_Flat(w) for w in worlds]
+        arr = (PdpdWorld * len(flats))(*[f.struct for f in flats])
+        self._check(lib().pdpd_attach_batch(self._h, arr, len(flats)), "AttachBatch")
+        self._worlds = list(worlds)
+
+    def Run(self, *args):
+        if len(args) == 1:
+            self._check(lib().pdpd_run(self._h, int(args[0])), "Run")
+            for i, w in enumerate(self._worlds):
+                self.read_state(i, into=w)
+            return None
+        count, size, cb = args
+        return self._run_intervals(int(count), int(size), cb)
+
+    def _run_intervals(self, count, size, cb):
+        if len(self._worlds) != 1:
+            raise RuntimeError("interval runs need exactly one attached world")
+        w = self._worlds[0]
+        x = np.ascontiguousarray(w.x)
+        v = np.ascontiguousarray(w.v)
+        f = np.ascontiguousarray(w.f)
+        w.x, w.v, w.f = x, v, f
+        err = []
+
+        def tramp(_user, t):
+            try:
+                w.t = int(t)
+                return 1 if cb() else 0
+            except BaseException as e:  # stop the run, re-raise below
+                err.append(e)
+                return 0
+
+        fn = INTERVAL_FN(tramp)
+        done = C.c_uint32(0)
+        rc = lib().pdpd_run_intervals(self._h, count, size, _p(x), _p(v), _p(f), 24, fn, None,
+                                      C.byref(done))
+        if err:
+            raise err[0]
+        self._check(rc, "Run(intervals)")
+        return int(done.value)
+
+    def GetTimings(self):
+        t = PdpdTimings()
+        self._check(lib().pdpd_get_timings(self._h, C.byref(t)), "GetTimings")
+        return {n: getattr(t, n) for n, _ in PdpdTimings._fields_}
+
+    def GetConfigEntries(self):
+        out = []
+        i = 0
+        while True:
+            n, d, v = (C.create_string_buffer(128) for _ in range(3))
+            if lib().pdpd_get_config(self._h, i, n, 128, d, 128, v, 128) != 0:
+                break
+            out.append((n.value.decode(), d.value.decode(), v.value.decode()))
+            i += 1
+        return out
+
+    def SetConfigEntry(self, key, value):
+        self._check(lib().pdpd_set_config(self._h, key.encode(), str(value).encode()),
+                    "SetConfigEntry")
+
+    # -- extras -----------------------------------------------------------------------
+    def run_async(self, n):
+        self._check(lib().pdpd_run_async(self._h, int(n)), "run_async")
+
+    def sync(self):
+        self._check(lib().pdpd_sync(self._h), "sync")
+
+    def stream(self):
+        return lib().pdpd_stream(self._h)
+
+    def profile_run(self, n):
+        """Run n steps launching kernels one by one with CUDA events between phases; returns
+        per-phase device milliseconds (the trajectory equals Run(n)'s)."""
+        pt = PdpdPhaseTimes()
+        self._check(lib().pdpd_profile_run(self._h, int(n), C.byref(pt)), "profile_run")
+        return {n_: getattr(pt, n_) for n_, _ in PdpdPhaseTimes._fields_}
+
+    def kernel_launches(self):
+        return int(lib().pdpd_kernel_launches(self._h))
+
+    def read_state(self, world_index=0, into=None):
+        """Copy world ``world_index``'s x, v, f, t to numpy (into a World when given)."""
+        n = (self._worlds[world_index].n_beads if self._worlds else 0)
+        x = np.empty((n, 3))
+        v = np.empty((n, 3))
+        f = np.empty((n, 3))
+        t = C.c_int64(0)
+        self._check(lib().pdpd_read_state(self._h, world_index, _p(x), _p(v), _p(f), 24,
+                                          C.byref(t)), "read_state")
+        if into is not None:
+            into.x, into.v, into.f, into.t = x, v, f, int(t.value)
+        return x, v, f, int(t.value)

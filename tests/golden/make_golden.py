@@ -1,0 +1,177 @@
+"""Generate the golden fixtures in this directory from the reference's own code.
+
+Run in a container that has the reference sources (default /root/reference):
+
+    make -C oracle/ref REF_ROOT=/root/reference     # builds oracle/_ref/ref_harness
+    python tests/golden/make_golden.py
+
+The harness (oracle/ref/ref_harness.cpp) compiles the reference's FP64 engines unchanged from
+the reference headers.  Each world fixture stores the input world (PDW1 bytes) and the
+reference engine's x, v, f after each checkpoint step count, so the tests can run anywhere
+without the reference present.  The hash fixture stores get_t_hash / hash_rng_sym /
+default_hash outputs of the reference's own functions for seeded and edge-case inputs.
+"""
+
+from __future__ import annotations
+
+import io
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "poets-dpd_gb300"))
+
+import pdpd_world as W  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+ENGINE = "naive_dpd_engine_half_step"
+
+
+def run_reference(world, checkpoints, engine=ENGINE):
+    tmp_in = os.path.join(HERE, "_in.pdw1")
+    tmp_out = os.path.join(HERE, "_out.bin")
+    W.write_pdw1(world, tmp_in)
+    subprocess.run([HARNESS, "step", engine, tmp_in, tmp_out, str(len(checkpoints))]
+                   + [str(c) for c in checkpoints], check=True)
+    data = open(tmp_out, "rb").read()
+    os.remove(tmp_in)
+    os.remove(tmp_out)
+    p = 0
+    ts, xs, vs, fs = [], [], [], []
+    for _ in checkpoints:
+        t = int(np.frombuffer(data, np.int64, 1, p)[0])
+        n = int(np.frombuffer(data, np.uint32, 1, p + 8)[0])
+        p += 12
+        rec = np.frombuffer(data, np.float64, 9 * n, p).reshape(n, 9)
+        p += 72 * n
+        ts.append(t)
+        xs.append(rec[:, 0:3])
+        vs.append(rec[:, 3:6])
+        fs.append(rec[:, 6:9])
+    return np.array(ts), np.stack(xs), np.stack(vs), np.stack(fs)
+
+
+def save_world_fixture(name, world, checkpoints, note):
+    ts, xs, vs, fs = run_reference(world, checkpoints)
+    buf = io.BytesIO()
+    W.write_pdw1(world, buf)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        world=np.frombuffer(buf.getvalue(), np.uint8),
+                        checkpoints=np.array(checkpoints), t=ts, x=xs, v=vs, f=fs,
+                        engine=np.array(ENGINE), note=np.array(note))
+    print(f"{name}: {world.n_beads} beads, checkpoints {checkpoints}")
+
+
+def pair_world(dx, v0, gamma, box=(4, 4, 4), seed=7):
+    """Two monomers at x0 +- dx moving towards each other (a head-on collision)."""
+    b = W.WorldBuilder(box, 1, [[25.0]], [[gamma]], dt=0.02, seed=seed)
+    b.add_polymer_type([0])
+    x0 = np.array([2.0, 2.0, 2.0])
+    dx = np.asarray(dx, float)
+    b.add_polymer(0, [x0 + dx], [(-np.asarray(v0)).tolist()])
+    b.add_polymer(0, [x0 - dx], [np.asarray(v0).tolist()])
+    return b.build()
+
+
+def triple_world(theta0, seed=11):
+    """A bent 3-bead chain with Hookean bonds and one angle bond, in a little water."""
+    rng = np.random.default_rng(123)
+    a, g = W.polymer_interactions(75.0, 4.5)
+    b = W.WorldBuilder((5, 5, 5), 3, a, g, dt=0.01, seed=seed)
+    b.add_polymer_type([1, 2, 2], [(0, 1, 128.0, 0.5), (1, 2, 128.0, 0.5)],
+                       [(0, 1, 20.0, theta0)])
+    b.add_polymer_type([0])
+    b.add_polymer(0, [(2.0, 2.0, 2.0), (2.45, 2.1, 2.05), (2.7, 2.5, 2.2)],
+                  [(0.1, 0.0, 0.0), (0.0, 0.2, 0.0), (0.0, 0.0, -0.1)])
+    for _ in range(40):
+        b.add_polymer(1, [tuple(rng.random(3) * 5.0)], [tuple(rng.standard_normal(3))])
+    return b.build()
+
+
+def boundary_world(seed=5):
+    """Beads placed on cell faces and the box faces, moving across the periodic boundary."""
+    b = W.WorldBuilder((4, 4, 4), 1, [[25.0]], [[4.5]], dt=0.02, seed=seed)
+    b.add_polymer_type([0])
+    pts = [(0.0, 0.0, 0.0), (3.999999999, 2.0, 1.0), (1.0, 3.0, 0.0), (2.0, 2.0, 3.9),
+           (0.05, 3.95, 2.0), (3.95, 0.05, 2.0), (1.0, 1.0, 1.0), (2.5, 0.0, 3.5)]
+    vel = [(-1.0, -1.0, -1.0), (1.5, 0.0, 0.0), (0.0, 1.0, -2.0), (0.0, 0.0, 3.0),
+           (-2.0, 2.0, 0.0), (2.0, -2.0, 0.0), (0.0, 0.0, 0.0), (0.5, -0.5, 0.5)]
+    for p, v in zip(pts, vel):
+        b.add_polymer(0, [p], [v])
+    return b.build()
+
+
+def hash_fixture():
+    rng = np.random.default_rng(2024)
+    n = 4096
+    t = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    seed = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
+    a = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    b = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    edge_t = [0, 1, 0xFFFFFFFF, 0x80000000, 12345]
+    edge_s = [0, 1, 0xFFFFFFFFFFFFFFFF, 0x8000000000000000, 42]
+    edge_ab = [(0, 0), (1, 0), (0, 1), (0xFFFFFFFF, 0), (0, 0xFFFFFFFF), (0xFFFFFFFF, 0xFFFFFFFF),
+               (0x80000000, 0x7FFFFFFF), (7, 7)]
+    et, es, ea, eb = [], [], [], []
+    for tt in edge_t:
+        for ss in edge_s:
+            for aa, bb in edge_ab:
+                et.append(tt)
+                es.append(ss)
+                ea.append(aa)
+                eb.append(bb)
+    t = np.concatenate([t, np.array(et, np.uint32)])
+    seed = np.concatenate([seed, np.array(es, np.uint64)])
+    a = np.concatenate([a, np.array(ea, np.uint32)])
+    b = np.concatenate([b, np.array(eb, np.uint32)])
+    rec = np.zeros(t.size, dtype=np.dtype([("t", "<u4"), ("seed", "<u8"), ("a", "<u4"), ("b", "<u4")]))
+    rec["t"], rec["seed"], rec["a"], rec["b"] = t, seed, a, b
+    tmp_in = os.path.join(HERE, "_hin.bin")
+    tmp_out = os.path.join(HERE, "_hout.bin")
+    rec.tofile(tmp_in)
+    subprocess.run([HARNESS, "hash", tmp_in, tmp_out], check=True)
+    out = np.fromfile(tmp_out, dtype=np.dtype([("th", "<u8"), ("h", "<u4"), ("u", "<f4")]))
+    os.remove(tmp_in)
+    os.remove(tmp_out)
+    np.savez_compressed(os.path.join(HERE, "hash_kat.npz"), t=t, seed=seed, a=a, b=b,
+                        t_hash=out["th"], h=out["h"], u=out["u"])
+    print(f"hash_kat: {t.size} records")
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        raise SystemExit("build the reference harness first: make -C oracle/ref")
+    hash_fixture()
+    save_world_fixture("water8_seed1", W.make_water(8, seed=1), [1, 10, 100],
+                       "8^3 water, density 3 (1536 beads), a=25, gamma=4.5, dt=0.02, seed=1")
+    save_world_fixture("polymer10_seed2", W.make_polymer_box(10, chain_fraction=0.1, seed=2),
+                       [1, 10, 50],
+                       "10^3 W/H/T polymer-solvent box, 10% in H-T5 chains, k=128 r0=0.5, "
+                       "angle k=20 theta0=0, dt=0.01, seed=2")
+    save_world_fixture("water_5x7x6_seed3", W.make_water((5, 7, 6), seed=3, gen_seed=33),
+                       [1, 10], "non-cubic 5x7x6 water box")
+    save_world_fixture("water_3x3x3_seed4", W.make_water(3, seed=4, gen_seed=44), [1, 10],
+                       "3^3 box: each neighbour direction wraps onto a distinct cell")
+    save_world_fixture("water_2x2x2_seed9", W.make_water(2, seed=9, gen_seed=99), [1, 10],
+                       "2^3 box: the -1 and +1 neighbours are the same cell")
+    save_world_fixture("pair_conservative", pair_world((0.2, 0, 0), (1.0, 0, 0), 0.0), [1, 10, 40],
+                       "head-on pair collision, gamma=0")
+    save_world_fixture("pair_dissipative", pair_world((0.15, 0.15, 0.15), (0.5, 0.5, 0.5), 4.5),
+                       [1, 10, 40], "diagonal pair collision with dissipation")
+    save_world_fixture("triple_angle_theta0", triple_world(0.0), [1, 10, 100],
+                       "bent 3-bead chain, angle bond theta0=0, in water")
+    save_world_fixture("triple_angle_theta0p2", triple_world(0.2), [1, 10, 100],
+                       "bent 3-bead chain, angle bond theta0=0.2 (the sin branch), in water")
+    save_world_fixture("boundary_crossing", boundary_world(), [1, 5, 20],
+                       "beads on cell and box faces crossing the periodic boundary")
+    empty = W.WorldBuilder((4, 4, 4), 1, [[25.0]], [[4.5]], dt=0.02, seed=1)
+    empty.add_polymer_type([0])
+    save_world_fixture("empty_world", empty.build(), [1, 3], "no beads at all")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,71 @@
+"""The oracle (C restatement of the reference's half-step engine) is pinned bit for bit to
+the reference's own outputs stored in tests/golden/ (generated by make_golden.py from the
+reference's NaiveDPDEngineHalfStep, compiled unchanged)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import pdpd_world as W
+from _helpers import load_hash_kat, load_world_fixture, world_fixture_names
+
+
+def test_hash_known_answers_match_reference():
+    kat = load_hash_kat()
+    th, h, u = O.hash_batch(kat["t"], kat["seed"], kat["a"], kat["b"])
+    assert np.array_equal(th, kat["t_hash"])
+    assert np.array_equal(h, kat["h"])
+    assert np.array_equal(u.view(np.uint32), kat["u"].view(np.uint32))
+
+
+def test_hash_is_symmetric_and_in_range():
+    kat = load_hash_kat()
+    _, h1, u1 = O.hash_batch(kat["t"], kat["seed"], kat["a"], kat["b"])
+    _, h2, _ = O.hash_batch(kat["t"], kat["seed"], kat["b"], kat["a"])
+    assert np.array_equal(h1, h2)
+    assert np.all(u1 >= -0.5) and np.all(u1 < 0.5)
+
+
+@pytest.mark.parametrize("name", world_fixture_names())
+@pytest.mark.parametrize("nthreads", [1, 3])
+def test_oracle_bit_exact_vs_reference(name, nthreads):
+    world, ref = load_world_fixture(name)
+    ow = O.OracleWorld(world)
+    prev = 0
+    for k, c in enumerate(ref["checkpoints"]):
+        ow.run(int(c) - prev, nthreads=nthreads)
+        prev = int(c)
+        assert ow.t == ref["t"][k]
+        assert np.array_equal(ow.x, ref["x"][k]), f"{name}: x differs at step {c}"
+        assert np.array_equal(ow.v, ref["v"][k]), f"{name}: v differs at step {c}"
+        assert np.array_equal(ow.f, ref["f"][k]), f"{name}: f differs at step {c}"
+
+
+def test_oracle_cell_index_is_floor():
+    w = W.make_polymer_box(6, chain_fraction=0.1, seed=3)
+    ow = O.OracleWorld(w)
+    c = ow.cell_index()
+    fl = np.floor(w.x).astype(np.int64)
+    L = w.box.astype(np.int64)
+    assert np.array_equal(c, fl[:, 0] * L[1] * L[2] + fl[:, 1] * L[2] + fl[:, 2])
+
+
+def test_oracle_reports_snapped_bond():
+    b = W.WorldBuilder((6, 6, 6), 1, [[25.0]], [[4.5]], dt=0.01)
+    b.add_polymer_type([0, 0], [(0, 1, 128.0, 0.5)])
+    b.add_polymer(0, [(1.0, 1.0, 1.0), (3.5, 1.0, 1.0)])
+    ow = O.OracleWorld(b.build())
+    with pytest.raises(RuntimeError, match="snapped"):
+        ow.run(1)
+
+
+def test_observables_basic():
+    w = W.make_water(6, seed=1)
+    ow = O.OracleWorld(w)
+    obs = ow.observe(n_bins=20, n_bond_bins=10)
+    assert abs(obs["ke2"] - np.sum(w.v ** 2)) < 1e-9 * obs["ke2"]
+    assert np.allclose(obs["momentum"], 0, atol=1e-9)
+    n = w.n_beads
+    # every unordered pair with r < 1 counted once: expected count ~ N * rho * (4/3 pi) / 2
+    pairs = obs["rdf"].sum()
+    assert 0.7 * n * 3 * 4.18879 / 2 < pairs < 1.3 * n * 3 * 4.18879 / 2
