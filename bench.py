@@ -195,7 +195,7 @@ def run_engine_arm(args):
     rank, world_size, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    world = make_world(args.workload)
+    world = make_world(args.workload, side=args.side)
     n = world.n_beads
     eng = E.GB300DPDEngine(args.precision, device=local)
 
@@ -267,7 +267,7 @@ def run_engine_arm(args):
         rate, threads, steps, dt = oracle_rate(make_world(args.workload, side=sample_side))
         cpu = {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
                "sample": f"{sample_side}^3 box of the same recipe, {steps} steps in {dt:.1f} s"}
-    L = WORKLOADS[args.workload][0]
+    L = args.side or WORKLOADS[args.workload][0]
     line = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -306,6 +306,8 @@ def main():
     ap.add_argument("--ref-side", type=int, default=32,
                     help="box side of the bounded CPU sample (same recipe)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--side", type=int, default=None,
+                    help="override the box side of the workload (profiling on smaller boxes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -87,7 +87,7 @@ struct ConfigEntry {
 };
 
 const ConfigEntry kConfig[] = {
-    {"tile_cells", "Cells per work tile of the step kernels (0 = automatic)."},
+    {"list_capacity", "Neighbour-list entries per bead before a flush (0 = automatic)."},
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
@@ -106,7 +106,7 @@ struct pdpd_engine {
     uint64_t launches = 0;
 
     // configuration
-    int cfg_tile_cells = 0;
+    int cfg_list_capacity = 0;
     int cfg_grid_blocks = 0;
     int cfg_graph_steps = 0;
     int cfg_use_graphs = 1;
@@ -437,7 +437,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     e->n_cells = (uint32_t)nc;
 
     // --- world table, tiles, pair table
-    int tile_cells = e->cfg_tile_cells > 0 ? e->cfg_tile_cells : 64;
     std::vector<Tile> tiles;
     std::vector<WorldDev> wdev(n_worlds);
     const bool f64 = e->fp64();
@@ -459,8 +458,8 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
         d.scale_inv_sqrt_dt = std::sqrt(24 * 1.0 / w.dt);  // pow_half(24 kT / dt)
         d.seed = w.seed;
         d.t = w.t;
-        for (uint32_t c = 0; c < d.n_cells; c += tile_cells)
-            tiles.push_back({i, cell_base + c, cell_base + std::min<uint32_t>(d.n_cells, c + tile_cells), 0});
+        for (uint32_t b = 0; b < w.n_beads; b += TILE_BEADS)
+            tiles.push_back({i, bead_base + b, bead_base + std::min<uint32_t>(w.n_beads, b + TILE_BEADS), 0});
         for (uint32_t k = 0; k < w.n_bead_types * w.n_bead_types; k++) {
             double a = w.conservative[k], sg = std::sqrt(w.dissipative[k]);
             pair64.push_back(a);
@@ -641,6 +640,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.staging = e->d_staging[0].as<double>();
     a.block_threads = 128;
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
+    a.list_capacity = e->cfg_list_capacity;
     a.grid_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)gb, e->n_tiles));
 
     // --- bin + sort into the rest state
@@ -846,7 +846,7 @@ int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len,
 {
     if (!e) return PDPD_E_INVALID;
     if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
-    int vals[] = {e->cfg_tile_cells, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs};
+    int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs};
     if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
     if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
     if (value && value_len) snprintf(value, value_len, "%d", vals[index]);
@@ -860,7 +860,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     long v = strtol(value, &end, 10);
     if (!end || *end || v < 0 || v > (1 << 24)) return e->fail(PDPD_E_INVALID, "bad value '%s' for '%s'", value, key);
     std::string k = key;
-    if (k == "tile_cells") e->cfg_tile_cells = (int)v;
+    if (k == "list_capacity") e->cfg_list_capacity = (int)v;
     else if (k == "grid_blocks") e->cfg_grid_blocks = (int)v;
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;

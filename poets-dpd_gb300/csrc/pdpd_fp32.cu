@@ -179,137 +179,192 @@ __device__ void bond_forces32(const KArgs &a, const WorldDev &w, uint32_t id, co
     }
 }
 
+// Neighbour list of one bead, kept in shared memory: entry k of thread t is at
+// [k * TILE_BEADS + t] (consecutive threads hit consecutive banks).  An entry is a sorted
+// slot j and the direction of j's cell, packed 2 bits per axis as (d + 1).
+constexpr int LIST_MAX = 48;
+
+__device__ __forceinline__ uint32_t pack_dir(int ddx, int ddy, int ddz)
+{
+    return (uint32_t)(ddx + 1) | ((uint32_t)(ddy + 1) << 2) | ((uint32_t)(ddz + 1) << 4);
+}
+
+// Lower bound of the distance from offset o to the neighbour slab in direction d.
+__device__ __forceinline__ float slab_gap(float o, int d)
+{
+    return d == 0 ? 0.0f : (d < 0 ? o : 1.0f - o);
+}
+
+// Phase 2: the pair forces of the listed neighbours, in list order (calc_force,
+// dpd_maths_core_half_step.hpp:69-157; kT = 1, sigma = sqrt(2 gamma kT) implied).
+__device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
+                                              const float4 *__restrict__ vel,
+                                              const uint32_t *__restrict__ s_j,
+                                              const uint8_t *__restrict__ s_dir, int n,
+                                              const float4 ph, const float4 vh, uint32_t ti,
+                                              uint32_t nt, const float2 *__restrict__ pair,
+                                              uint32_t th_lo, uint32_t th_hi, float scale,
+                                              float &fx, float &fy, float &fz)
+{
+    const uint32_t hh = __float_as_uint(ph.w);
+    for (int k = 0; k < n; k++) {
+        const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
+        const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
+        const float4 pj = pos[j];
+        const float4 vj = vel[j];
+        const float dx = (ph.x - (float)((int)(d & 3u) - 1)) - pj.x;
+        const float dy = (ph.y - (float)((int)((d >> 2) & 3u) - 1)) - pj.y;
+        const float dz = (ph.z - (float)((int)((d >> 4) & 3u) - 1)) - pj.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const uint32_t hj = __float_as_uint(pj.w);
+        const float2 pp = pair[ti * nt + min(hj >> 28, nt - 1u)];
+        const float inv_r = rsqrtf(r2);
+        const float r = r2 * inv_r;
+        const float wr = 1.0f - r;
+        const float ex = dx * inv_r, ey = dy * inv_r, ez = dz * inv_r;
+        const float rdotv = ex * (vh.x - vj.x) + ey * (vh.y - vj.y) + ez * (vh.z - vj.z);
+        const float sg = pp.y * wr;
+        const float u = hash_u(th_lo, th_hi, hh, hj);
+        const float scaled = pp.x * wr - sg * sg * rdotv + (sg * scale) * u;
+        fx += ex * scaled;
+        fy += ey * scaled;
+        fz += ez * scaled;
+    }
+}
+
 // Pair forces on one bead: full-shell gather over the 27 neighbour cells in the reference's
-// direction order, beads of a cell in id order (naive_dpd_engine_half_step.hpp:300-315,
-// 358-424; calc_force dpd_maths_core_half_step.hpp:69-157).
+// direction order, the beads of a cell in id order (naive_dpd_engine_half_step.hpp:300-315,
+// 358-424).  Phase 1 keeps the candidates with r^2 in [MIN_DISTANCE_CUTOFF^2, 1) in a list;
+// phase 2 evaluates them.  Cells whose nearest face is at distance >= 1 (with margin) cannot
+// hold an in-range bead and are skipped; the list is the same as without the skip.
 __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
-                                              const float2 *s_pair, uint32_t th_lo,
+                                              const float2 *pair, uint32_t *s_j,
+                                              uint8_t *s_dir, int cap, uint32_t th_lo,
                                               uint32_t th_hi, float scale, const int c[3],
                                               const float4 ph, const float4 vh, float F[3])
 {
     const float4 *__restrict__ pos = (const float4 *)a.posA;
     const float4 *__restrict__ vel = (const float4 *)a.velA;
     const uint32_t *__restrict__ start = a.start;
-    const uint32_t hh = __float_as_uint(ph.w);
     const uint32_t nt = w.n_types;
-    const uint32_t ti = min(hh >> 28, nt - 1u);
+    const uint32_t ti = min(__float_as_uint(ph.w) >> 28, nt - 1u);
     const float min2 = min_dist_sqr_f();
+    const float PRUNE = 1.0001f;
     float fx = 0.f, fy = 0.f, fz = 0.f;
+    int n = 0;
     for (int ddx = -1; ddx <= 1; ddx++) {
+        const float gx = slab_gap(ph.x, ddx);
         const int nx = wrap_index(c[0] + ddx, w.L[0]);
         const float ax = ph.x - (float)ddx;
         for (int ddy = -1; ddy <= 1; ddy++) {
+            const float gy = slab_gap(ph.y, ddy);
+            const float gxy = gx * gx + gy * gy;
+            if (gxy >= PRUNE) continue;
             const int ny = wrap_index(c[1] + ddy, w.L[1]);
             const float ay = ph.y - (float)ddy;
             const uint32_t row = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2];
             for (int ddz = -1; ddz <= 1; ddz++) {
+                const float gz = slab_gap(ph.z, ddz);
+                if (gxy + gz * gz >= PRUNE) continue;
                 const int nz = wrap_index(c[2] + ddz, w.L[2]);
                 const float az = ph.z - (float)ddz;
                 const uint32_t nc = row + (uint32_t)nz;
                 const uint32_t j1 = start[nc + 1];
+                const uint8_t dpk = (uint8_t)pack_dir(ddx, ddy, ddz);
                 for (uint32_t j = start[nc]; j < j1; j++) {
                     const float4 pj = pos[j];
                     const float dx = ax - pj.x, dy = ay - pj.y, dz = az - pj.z;
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     if (r2 < 1.0f && r2 >= min2) {
-                        const float4 vj = vel[j];
-                        const uint32_t hj = __float_as_uint(pj.w);
-                        const float2 pp = s_pair[ti * nt + min(hj >> 28, nt - 1u)];
-                        const float inv_r = rsqrtf(r2);
-                        const float r = r2 * inv_r;
-                        const float wr = 1.0f - r;
-                        const float ex = dx * inv_r, ey = dy * inv_r, ez = dz * inv_r;
-                        const float rdotv = ex * (vh.x - vj.x) + ey * (vh.y - vj.y) + ez * (vh.z - vj.z);
-                        const float sg = pp.y * wr;
-                        const float u = hash_u(th_lo, th_hi, hh, hj);
-                        const float scaled = pp.x * wr - sg * sg * rdotv + (sg * scale) * u;
-                        fx += ex * scaled;
-                        fy += ey * scaled;
-                        fz += ez * scaled;
+                        if (n == cap) {
+                            list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo,
+                                          th_hi, scale, fx, fy, fz);
+                            n = 0;
+                        }
+                        s_j[n * TILE_BEADS + threadIdx.x] = j;
+                        s_dir[n * TILE_BEADS + threadIdx.x] = dpk;
+                        n++;
                     }
                 }
             }
         }
     }
+    list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo, th_hi, scale, fx, fy, fz);
     F[0] = fx;
     F[1] = fy;
     F[2] = fz;
 }
 
 template <int FINAL>
-__global__ void __launch_bounds__(128) k_force32(KArgs a)
+__global__ void __launch_bounds__(TILE_BEADS) k_force32(KArgs a)
 {
     __shared__ float2 s_pair[MAX_PAIR];
+    __shared__ uint32_t s_j[LIST_MAX * TILE_BEADS];
+    __shared__ uint8_t s_dir[LIST_MAX * TILE_BEADS];
     __shared__ WorldCache wc;
     if (threadIdx.x == 0) wc.world = 0xffffffffu;
     __syncthreads();
+    const int cap = (a.list_capacity > 0 && a.list_capacity < LIST_MAX) ? a.list_capacity : LIST_MAX;
     for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const Tile tl = a.tiles[tile];
         load_world(a, tl.world, wc, s_pair);
         const WorldDev &w = wc.w;
+        const uint32_t s = tl.slot_begin + threadIdx.x;
+        if (s >= tl.slot_end) continue;
         const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
         const float scale = (float)w.scale_inv_sqrt_dt;
         const uint64_t th = t_hash((uint32_t)w.t, w.seed);
         const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
-        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
         uint32_t err = 0;
-        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const float4 ph = ((const float4 *)a.posA)[s];
-            const float4 vh = ((const float4 *)a.velA)[s];
-            int c[3];
-            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-            float F[3];
-            pair_forces32(a, w, s_pair, th_lo, th_hi, scale, c, ph, vh, F);
-            float o[3] = {ph.x, ph.y, ph.z};
-            if (!(__float_as_uint(ph.w) & (1u << 27)))  // polymer bead: bonds
-                bond_forces32(a, w, a.ids[s], c, o, F, err);
-            // update_mom (dpd_maths_core_half_step.hpp:51-61)
-            float v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
-            if (FINAL) {
-                ((float4 *)a.velB)[s] = make_float4(v[0], v[1], v[2], 0.f);
-                ((float4 *)a.frc)[s] = make_float4(F[0], F[1], F[2], 0.f);
-                if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
-            } else {
-                const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
-                const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
-                ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
-                ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
-                a.keyrank[s] = make_uint2(key, rank);
-            }
-        }
-        if (err) atomicOr(&a.worlds[tl.world].err, err);
-    }
-}
-
-// First update_pos of a run, from the rest state x(t), v(t), f(t).
-__global__ void __launch_bounds__(128) k_begin32(KArgs a)
-{
-    __shared__ float2 s_pair[MAX_PAIR];
-    __shared__ WorldCache wc;
-    if (threadIdx.x == 0) wc.world = 0xffffffffu;
-    __syncthreads();
-    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
-        const Tile tl = a.tiles[tile];
-        load_world(a, tl.world, wc, s_pair);
-        const WorldDev &w = wc.w;
-        const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
-        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
-        uint32_t err = 0;
-        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const float4 ph = ((const float4 *)a.posA)[s];
-            const float4 vh = ((const float4 *)a.velA)[s];
-            const float4 fh = ((const float4 *)a.frc)[s];
-            int c[3];
-            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-            float o[3] = {ph.x, ph.y, ph.z};
-            const float v[3] = {vh.x, vh.y, vh.z};
-            const float F[3] = {fh.x, fh.y, fh.z};
+        const float4 ph = ((const float4 *)a.posA)[s];
+        const float4 vh = ((const float4 *)a.velA)[s];
+        int c[3];
+        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+        float F[3];
+        pair_forces32(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, scale, c, ph, vh, F);
+        float o[3] = {ph.x, ph.y, ph.z};
+        if (!(__float_as_uint(ph.w) & (1u << 27)))  // polymer bead: bonds
+            bond_forces32(a, w, a.ids[s], c, o, F, err);
+        // update_mom (dpd_maths_core_half_step.hpp:51-61)
+        float v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+        if (FINAL) {
+            ((float4 *)a.velB)[s] = make_float4(v[0], v[1], v[2], 0.f);
+            ((float4 *)a.frc)[s] = make_float4(F[0], F[1], F[2], 0.f);
+            if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
+        } else {
             const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
             const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
             ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
             ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
             a.keyrank[s] = make_uint2(key, rank);
         }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+// First update_pos of a run, from the rest state x(t), v(t), f(t).
+__global__ void __launch_bounds__(TILE_BEADS) k_begin32(KArgs a)
+{
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const uint32_t s = tl.slot_begin + threadIdx.x;
+        if (s >= tl.slot_end) continue;
+        const WorldDev &w = a.worlds[tl.world];
+        const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
+        uint32_t err = 0;
+        const float4 ph = ((const float4 *)a.posA)[s];
+        const float4 vh = ((const float4 *)a.velA)[s];
+        const float4 fh = ((const float4 *)a.frc)[s];
+        int c[3];
+        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+        float o[3] = {ph.x, ph.y, ph.z};
+        const float v[3] = {vh.x, vh.y, vh.z};
+        const float F[3] = {fh.x, fh.y, fh.z};
+        const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
+        const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+        ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
+        ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
+        a.keyrank[s] = make_uint2(key, rank);
         if (err) atomicOr(&a.worlds[tl.world].err, err);
     }
 }
@@ -362,29 +417,28 @@ __global__ void k_finish32(KArgs a)
 }
 
 // Rest state -> id-ordered FP64 staging (x, v, f): x = cell + offset exactly.
-__global__ void __launch_bounds__(128) k_unsort32(KArgs a)
+__global__ void __launch_bounds__(TILE_BEADS) k_unsort32(KArgs a)
 {
     for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const Tile tl = a.tiles[tile];
+        const uint32_t s = tl.slot_begin + threadIdx.x;
+        if (s >= tl.slot_end) continue;
         const WorldDev &w = a.worlds[tl.world];
-        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
-        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const float4 p = ((const float4 *)a.posA)[s];
-            const float4 v = ((const float4 *)a.velA)[s];
-            const float4 f = ((const float4 *)a.frc)[s];
-            int c[3];
-            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-            double *st = a.staging + 9 * (size_t)a.ids[s];
-            st[0] = (double)c[0] + (double)p.x;
-            st[1] = (double)c[1] + (double)p.y;
-            st[2] = (double)c[2] + (double)p.z;
-            st[3] = v.x;
-            st[4] = v.y;
-            st[5] = v.z;
-            st[6] = f.x;
-            st[7] = f.y;
-            st[8] = f.z;
-        }
+        const float4 p = ((const float4 *)a.posA)[s];
+        const float4 v = ((const float4 *)a.velA)[s];
+        const float4 f = ((const float4 *)a.frc)[s];
+        int c[3];
+        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+        double *st = a.staging + 9 * (size_t)a.ids[s];
+        st[0] = (double)c[0] + (double)p.x;
+        st[1] = (double)c[1] + (double)p.y;
+        st[2] = (double)c[2] + (double)p.z;
+        st[3] = v.x;
+        st[4] = v.y;
+        st[5] = v.z;
+        st[6] = f.x;
+        st[7] = f.y;
+        st[8] = f.z;
     }
 }
 
@@ -399,16 +453,16 @@ int launch_bin32(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
 
 int launch_begin32(const KArgs &a, cudaStream_t s)
 {
-    k_begin32<<<a.grid_blocks, 128, 0, s>>>(a);
+    k_begin32<<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 
 int launch_force32(const KArgs &a, int final_step, cudaStream_t s)
 {
     if (final_step)
-        k_force32<1><<<a.grid_blocks, 128, 0, s>>>(a);
+        k_force32<1><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     else
-        k_force32<0><<<a.grid_blocks, 128, 0, s>>>(a);
+        k_force32<0><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 
@@ -420,7 +474,7 @@ int launch_finish32(const KArgs &a, cudaStream_t s)
 
 int launch_unsort32(const KArgs &a, cudaStream_t s)
 {
-    k_unsort32<<<a.grid_blocks, 128, 0, s>>>(a);
+    k_unsort32<<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 

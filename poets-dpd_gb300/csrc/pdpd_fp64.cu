@@ -165,11 +165,87 @@ __device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, co
     }
 }
 
+constexpr int LIST_MAX = 32;
+
+// make_relative_cell_pos (naive_dpd_engine_half_step.hpp:181-196) for one direction:
+// neighbour cell and the periodic shift of its beads.
+__device__ __forceinline__ uint32_t neighbour64(const WorldDev &w, const int c[3], const int dir[3],
+                                                double delta[3])
+{
+    int op[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int raw = c[i] + dir[i];
+        const int is_left = raw < 0;
+        const int is_right = raw == w.L[i];
+        op[i] = raw + (is_left - is_right) * w.L[i];
+        delta[i] = (double)(is_right - is_left) * (double)w.L[i];
+    }
+    return w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] +
+           (uint32_t)op[2];
+}
+
+// Phase 2: calc_force (dpd_maths_core_half_step.hpp:69-157) with kappa = 0, r0 = 0.5 for the
+// listed neighbours, in list order, each term in the reference's operation order.
+__device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
+                                              const Vec4d *__restrict__ vel,
+                                              const uint32_t *__restrict__ s_j,
+                                              const uint8_t *__restrict__ s_dir, int n,
+                                              const WorldDev &w, const int c[3],
+                                              const double xh[3], const Vec4d &vh, uint32_t hh,
+                                              uint32_t ti, const Vec2d *__restrict__ pair,
+                                              uint32_t th_lo, uint32_t th_hi,
+                                              double scale_inv_sqrt_dt, double F[3])
+{
+    const uint32_t nt = w.n_types;
+    for (int k = 0; k < n; k++) {
+        const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
+        const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
+        const int dir[3] = {(int)(d & 3u) - 1, (int)((d >> 2) & 3u) - 1, (int)((d >> 4) & 3u) - 1};
+        double delta[3];
+        neighbour64(w, c, dir, delta);
+        const Vec4d pj = pos[j];
+        const Vec4d vj = vel[j];
+        const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
+        const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
+        const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+        const double dr = sqrt(dr2);
+        const uint32_t hj = hash_of(pj);
+        const Vec2d pp = pair[ti * nt + min(hj >> 28, nt - 1u)];
+        const double kappa = 0.0, r0 = 0.5;
+        const double inv_dr = 1.0 / dr;
+        const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
+        const double wr = 1.0 - dr;
+        const double con_force = pp.x * wr;
+        const double e0 = dx0 * inv_dr, e1 = dx1 * inv_dr, e2 = dx2 * inv_dr;
+        const double rdotv = e0 * dv0 + e1 * dv1 + e2 * dv2;
+        const double sqrt_gammap = pp.y * wr;
+        const double diss_force = -sqrt_gammap * sqrt_gammap * rdotv;
+        const double u = (double)hash_u(th_lo, th_hi, hh, hj);
+        const double rand_scale = sqrt_gammap * scale_inv_sqrt_dt;
+        const double rand_force = rand_scale * u;
+        const double dr0 = r0 - dr;
+        const double hookean_force = kappa * dr0;
+        const double scaled = con_force + diss_force + rand_force + hookean_force;
+        F[0] = F[0] + e0 * scaled;
+        F[1] = F[1] + e1 * scaled;
+        F[2] = F[2] + e2 * scaled;
+    }
+}
+
+__device__ __forceinline__ double slab_gap64(double o, int d)
+{
+    return d == 0 ? 0.0 : (d < 0 ? o : 1.0 - o);
+}
+
 // Pair forces on one bead: for each of the 27 directions in (-1..1)^3 order, for each bead
-// of that cell in id order: the reference's update_cell_forces + calc_force, with
-// kappa = 0, r0 = 0.5 (naive_dpd_engine_half_step.hpp:358-424).
+// of that cell in id order, the reference's update_cell_forces filter
+// (naive_dpd_engine_half_step.hpp:358-424); in-range neighbours go to the list, which is
+// evaluated in the same order.  A cell is skipped when its nearest face is further than
+// 1 + 1e-9 from the bead: no bead in it can pass dr2 < 1, so the list is unchanged.
 __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
-                                              const Vec2d *s_pair, uint32_t th_lo, uint32_t th_hi,
+                                              const Vec2d *s_pair, uint32_t *s_j, uint8_t *s_dir,
+                                              int cap, uint32_t th_lo, uint32_t th_hi,
                                               double scale_inv_sqrt_dt, const int c[3],
                                               const double xh[3], const Vec4d &vh, uint32_t hh,
                                               double F[3])
@@ -177,121 +253,86 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
     const Vec4d *__restrict__ pos = (const Vec4d *)a.posA;
     const Vec4d *__restrict__ vel = (const Vec4d *)a.velA;
     const uint32_t *__restrict__ start = a.start;
-    const uint32_t nt = w.n_types;
-    const uint32_t ti = min(hh >> 28, nt - 1u);
+    const uint32_t ti = min(hh >> 28, w.n_types - 1u);
     const double min2 = (double)min_dist_sqr_f();
+    const double PRUNE = 1.0 + 1e-9;
+    const double o[3] = {xh[0] - (double)c[0], xh[1] - (double)c[1], xh[2] - (double)c[2]};
     F[0] = F[1] = F[2] = 0.0;
+    int n = 0;
     int dir[3];
-    for (dir[0] = -1; dir[0] <= 1; dir[0]++)
-        for (dir[1] = -1; dir[1] <= 1; dir[1]++)
+    for (dir[0] = -1; dir[0] <= 1; dir[0]++) {
+        const double gx = slab_gap64(o[0], dir[0]);
+        for (dir[1] = -1; dir[1] <= 1; dir[1]++) {
+            const double gy = slab_gap64(o[1], dir[1]);
+            const double gxy = gx * gx + gy * gy;
+            if (gxy >= PRUNE) continue;
             for (dir[2] = -1; dir[2] <= 1; dir[2]++) {
-                int op[3];
+                const double gz = slab_gap64(o[2], dir[2]);
+                if (gxy + gz * gz >= PRUNE) continue;
                 double delta[3];
-#pragma unroll
-                for (int i = 0; i < 3; i++) {  // make_relative_cell_pos (:181-196)
-                    const int raw = c[i] + dir[i];
-                    const int is_left = raw < 0;
-                    const int is_right = raw == w.L[i];
-                    op[i] = raw + (is_left - is_right) * w.L[i];
-                    delta[i] = (double)(is_right - is_left) * (double)w.L[i];
-                }
-                const uint32_t nc = w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] + (uint32_t)op[2];
+                const uint32_t nc = neighbour64(w, c, dir, delta);
                 const uint32_t j1 = start[nc + 1];
+                const uint8_t dpk = (uint8_t)((dir[0] + 1) | ((dir[1] + 1) << 2) | ((dir[2] + 1) << 4));
                 for (uint32_t j = start[nc]; j < j1; j++) {
                     const Vec4d pj = pos[j];
                     const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
                     const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
                     const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
                     if (dr2 >= 1 || dr2 < min2) continue;
-                    const double dr = sqrt(dr2);
-                    const Vec4d vj = vel[j];
-                    const uint32_t hj = hash_of(pj);
-                    const Vec2d pp = s_pair[ti * nt + min(hj >> 28, nt - 1u)];
-                    const double kappa = 0.0, r0 = 0.5;
-                    const double inv_dr = 1.0 / dr;
-                    const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
-                    const double wr = 1.0 - dr;
-                    const double con_force = pp.x * wr;
-                    const double e0 = dx0 * inv_dr, e1 = dx1 * inv_dr, e2 = dx2 * inv_dr;
-                    const double rdotv = e0 * dv0 + e1 * dv1 + e2 * dv2;
-                    const double sqrt_gammap = pp.y * wr;
-                    const double diss_force = -sqrt_gammap * sqrt_gammap * rdotv;
-                    const double u = (double)hash_u(th_lo, th_hi, hh, hj);
-                    const double rand_scale = sqrt_gammap * scale_inv_sqrt_dt;
-                    const double rand_force = rand_scale * u;
-                    const double dr0 = r0 - dr;
-                    const double hookean_force = kappa * dr0;
-                    const double scaled = con_force + diss_force + rand_force + hookean_force;
-                    F[0] = F[0] + e0 * scaled;
-                    F[1] = F[1] + e1 * scaled;
-                    F[2] = F[2] + e2 * scaled;
+                    if (n == cap) {
+                        list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, th_lo,
+                                      th_hi, scale_inv_sqrt_dt, F);
+                        n = 0;
+                    }
+                    s_j[n * TILE_BEADS + threadIdx.x] = j;
+                    s_dir[n * TILE_BEADS + threadIdx.x] = dpk;
+                    n++;
                 }
             }
+        }
+    }
+    list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, th_lo, th_hi,
+                  scale_inv_sqrt_dt, F);
 }
 
 template <int FINAL>
-__global__ void __launch_bounds__(128) k_force64(KArgs a)
+__global__ void __launch_bounds__(TILE_BEADS) k_force64(KArgs a)
 {
     __shared__ Vec2d s_pair[MAX_PAIR];
+    __shared__ uint32_t s_j[LIST_MAX * TILE_BEADS];
+    __shared__ uint8_t s_dir[LIST_MAX * TILE_BEADS];
     __shared__ WorldCache wc;
     if (threadIdx.x == 0) wc.world = 0xffffffffu;
     __syncthreads();
+    const int cap = (a.list_capacity > 0 && a.list_capacity < LIST_MAX) ? a.list_capacity : LIST_MAX;
     for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const Tile tl = a.tiles[tile];
         load_world(a, tl.world, wc, s_pair);
         const WorldDev &w = wc.w;
+        const uint32_t s = tl.slot_begin + threadIdx.x;
+        if (s >= tl.slot_end) continue;
         const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
         const uint64_t th = t_hash((uint32_t)w.t, w.seed);
         const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
-        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
         uint32_t err = 0;
-        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const Vec4d ph = ((const Vec4d *)a.posA)[s];
-            const Vec4d vh = ((const Vec4d *)a.velA)[s];
-            const uint32_t hh = hash_of(ph);
-            int c[3];
-            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-            double x[3] = {ph.x, ph.y, ph.z};
-            double F[3];
-            pair_forces64(a, w, s_pair, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, vh, hh, F);
-            if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
-            // update_mom: v += f * half(dt)
-            double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
-            if (FINAL) {
-                Vec4d vo = {v[0], v[1], v[2], 0.0};
-                Vec4d fo = {F[0], F[1], F[2], 0.0};
-                ((Vec4d *)a.velB)[s] = vo;
-                ((Vec4d *)a.frc)[s] = fo;
-                if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
-            } else {
-                const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
-                const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
-                Vec4d po = {x[0], x[1], x[2], ph.w};
-                Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
-                ((Vec4d *)a.posB)[s] = po;
-                ((Vec4d *)a.velB)[s] = vo;
-                a.keyrank[s] = make_uint2(key, rank);
-            }
-        }
-        if (err) atomicOr(&a.worlds[tl.world].err, err);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_begin64(KArgs a)
-{
-    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
-        const Tile tl = a.tiles[tile];
-        const WorldDev w = a.worlds[tl.world];
-        const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
-        const uint32_t s0 = a.start[tl.cell_begin], s1 = a.start[tl.cell_end];
-        uint32_t err = 0;
-        for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            const Vec4d ph = ((const Vec4d *)a.posA)[s];
-            const Vec4d vh = ((const Vec4d *)a.velA)[s];
-            const Vec4d fh = ((const Vec4d *)a.frc)[s];
-            double x[3] = {ph.x, ph.y, ph.z};
-            const double v[3] = {vh.x, vh.y, vh.z};
-            const double F[3] = {fh.x, fh.y, fh.z};
+        const Vec4d ph = ((const Vec4d *)a.posA)[s];
+        const Vec4d vh = ((const Vec4d *)a.velA)[s];
+        const uint32_t hh = hash_of(ph);
+        int c[3];
+        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+        double x[3] = {ph.x, ph.y, ph.z};
+        double F[3];
+        pair_forces64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, vh, hh, F);
+        if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
+        // update_mom: v += f * half(dt)
+        double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+        if (FINAL) {
+            Vec4d vo = {v[0], v[1], v[2], 0.0};
+            Vec4d fo = {F[0], F[1], F[2], 0.0};
+            ((Vec4d *)a.velB)[s] = vo;
+            ((Vec4d *)a.frc)[s] = fo;
+            if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
+        } else {
             const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
             const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
             Vec4d po = {x[0], x[1], x[2], ph.w};
@@ -300,6 +341,32 @@ __global__ void __launch_bounds__(128) k_begin64(KArgs a)
             ((Vec4d *)a.velB)[s] = vo;
             a.keyrank[s] = make_uint2(key, rank);
         }
+        if (err) atomicOr(&a.worlds[tl.world].err, err);
+    }
+}
+
+__global__ void __launch_bounds__(TILE_BEADS) k_begin64(KArgs a)
+{
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const uint32_t s = tl.slot_begin + threadIdx.x;
+        if (s >= tl.slot_end) continue;
+        const WorldDev &w = a.worlds[tl.world];
+        const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+        uint32_t err = 0;
+        const Vec4d ph = ((const Vec4d *)a.posA)[s];
+        const Vec4d vh = ((const Vec4d *)a.velA)[s];
+        const Vec4d fh = ((const Vec4d *)a.frc)[s];
+        double x[3] = {ph.x, ph.y, ph.z};
+        const double v[3] = {vh.x, vh.y, vh.z};
+        const double F[3] = {fh.x, fh.y, fh.z};
+        const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
+        const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
+        Vec4d po = {x[0], x[1], x[2], ph.w};
+        Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
+        ((Vec4d *)a.posB)[s] = po;
+        ((Vec4d *)a.velB)[s] = vo;
+        a.keyrank[s] = make_uint2(key, rank);
         if (err) atomicOr(&a.worlds[tl.world].err, err);
     }
 }
@@ -379,16 +446,16 @@ int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
 
 int launch_begin64(const KArgs &a, cudaStream_t s)
 {
-    k_begin64<<<a.grid_blocks, 128, 0, s>>>(a);
+    k_begin64<<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 
 int launch_force64(const KArgs &a, int final_step, cudaStream_t s)
 {
     if (final_step)
-        k_force64<1><<<a.grid_blocks, 128, 0, s>>>(a);
+        k_force64<1><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     else
-        k_force64<0><<<a.grid_blocks, 128, 0, s>>>(a);
+        k_force64<0><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 

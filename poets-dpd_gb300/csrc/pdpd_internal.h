@@ -27,13 +27,18 @@ struct WorldDev {
     int64_t t;
 };
 
-// A run of consecutive cells of one world: the unit of work of the tile kernels.
+// A run of consecutive sorted bead slots of one world: the unit of work of the step
+// kernels.  A world's beads always occupy the same slot range [bead_base, bead_base+n)
+// (the cell list only permutes them inside it), so the tiles are fixed at attach.
 struct Tile {
     uint32_t world;
-    uint32_t cell_begin;  // global cell index
-    uint32_t cell_end;
+    uint32_t slot_begin;
+    uint32_t slot_end;
     uint32_t pad;
 };
+
+// Beads per tile = threads per block of the step kernels.
+constexpr int TILE_BEADS = 128;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
@@ -82,6 +87,7 @@ struct KArgs {
     double *staging;
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
+    int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
 };
 
 // Kernel launchers.  Each returns the number of kernels it launched.

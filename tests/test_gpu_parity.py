@@ -211,7 +211,7 @@ def test_batch_equals_alone(prec):
 def test_launch_configurations_agree(prec):
     world = W.make_polymer_box(12, chain_fraction=0.1, seed=9)
     results = []
-    for cfg in ({}, {"use_graphs": 0}, {"tile_cells": 7}, {"tile_cells": 500, "grid_blocks": 3},
+    for cfg in ({}, {"use_graphs": 0}, {"list_capacity": 1}, {"list_capacity": 5, "grid_blocks": 3},
                 {"graph_steps": 5}):
         w = world.copy()
         eng = E.GB300DPDEngine(prec)
