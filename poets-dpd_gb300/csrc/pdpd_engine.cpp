@@ -91,6 +91,7 @@ const ConfigEntry kConfig[] = {
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
+    {"force_kernel", "FP32 force kernel: 0 = shared-memory brick kernel, 1 = thread per bead."},
 };
 
 }  // namespace
@@ -110,6 +111,7 @@ struct pdpd_engine {
     int cfg_grid_blocks = 0;
     int cfg_graph_steps = 0;
     int cfg_use_graphs = 1;
+    int cfg_force_kernel = 0;
 
     // attached worlds
     bool attached = false;
@@ -117,7 +119,7 @@ struct pdpd_engine {
     uint32_t n_beads = 0, n_cells = 0, n_tiles = 0;
 
     // device arena
-    DevBuf d_worlds, d_tiles, d_start, d_cnt, d_blocksums;
+    DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
     DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash;
@@ -159,7 +161,7 @@ struct pdpd_engine {
     void release()
     {
         drop_graph();
-        DevBuf *bufs[] = {&d_worlds, &d_tiles, &d_start, &d_cnt, &d_blocksums, &d_posA, &d_velA,
+        DevBuf *bufs[] = {&d_worlds, &d_tiles, &d_bricks, &d_start, &d_cnt, &d_blocksums, &d_posA, &d_velA,
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_staging[0], &d_staging[1]};
@@ -438,6 +440,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
 
     // --- world table, tiles, pair table
     std::vector<Tile> tiles;
+    std::vector<Brick> bricks;
     std::vector<WorldDev> wdev(n_worlds);
     const bool f64 = e->fp64();
     std::vector<double> pair64;
@@ -460,6 +463,11 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
         d.t = w.t;
         for (uint32_t b = 0; b < w.n_beads; b += TILE_BEADS)
             tiles.push_back({i, bead_base + b, bead_base + std::min<uint32_t>(w.n_beads, b + TILE_BEADS), 0});
+        for (int x0 = 0; x0 < w.box[0]; x0 += BRICK_X)
+            for (int y0 = 0; y0 < w.box[1]; y0 += BRICK_Y)
+                for (int z0 = 0; z0 < w.box[2]; z0 += BRICK_Z)
+                    bricks.push_back({i, x0, y0, z0, std::min(BRICK_X, w.box[0] - x0),
+                                      std::min(BRICK_Y, w.box[1] - y0), std::min(BRICK_Z, w.box[2] - z0), 0});
         for (uint32_t k = 0; k < w.n_bead_types * w.n_bead_types; k++) {
             double a = w.conservative[k], sg = std::sqrt(w.dissipative[k]);
             pair64.push_back(a);
@@ -534,6 +542,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     };
     A(e->d_worlds, sizeof(WorldDev) * n_worlds);
     A(e->d_tiles, sizeof(Tile) * std::max<size_t>(1, tiles.size()));
+    A(e->d_bricks, sizeof(Brick) * std::max<size_t>(1, bricks.size()));
     A(e->d_start, sizeof(uint32_t) * ((size_t)nc + 1));
     A(e->d_cnt, sizeof(uint32_t) * (size_t)nc);
     A(e->d_blocksums, sizeof(uint32_t) * (scan_blocks((uint32_t)nc) + 1));
@@ -589,6 +598,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     };
     H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
     H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
+    H2D(e->d_bricks, bricks.data(), sizeof(Brick) * bricks.size());
     H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
     H2D(e->d_bond_terms, terms.data(), sizeof(BondTerm) * n_terms);
     if (f64) {
@@ -616,6 +626,8 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.worlds = e->d_worlds.as<WorldDev>();
     a.n_worlds = n_worlds;
     a.tiles = e->d_tiles.as<Tile>();
+    a.bricks = e->d_bricks.as<Brick>();
+    a.n_bricks = (uint32_t)bricks.size();
     a.n_tiles = e->n_tiles;
     a.n_beads = e->n_beads;
     a.n_cells = e->n_cells;
@@ -641,6 +653,9 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.block_threads = 128;
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
     a.list_capacity = e->cfg_list_capacity;
+    a.force_kernel = e->cfg_force_kernel;
+    a.brick_grid = f64 ? 0 : brick_grid_blocks(e->sm_count);
+    if (e->cfg_grid_blocks > 0) a.brick_grid = e->cfg_grid_blocks;
     a.grid_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)gb, e->n_tiles));
 
     // --- bin + sort into the rest state
@@ -846,7 +861,8 @@ int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len,
 {
     if (!e) return PDPD_E_INVALID;
     if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
-    int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs};
+    int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs,
+                  e->cfg_force_kernel};
     if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
     if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
     if (value && value_len) snprintf(value, value_len, "%d", vals[index]);
@@ -864,6 +880,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "grid_blocks") e->cfg_grid_blocks = (int)v;
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
+    else if (k == "force_kernel") e->cfg_force_kernel = v ? 1 : 0;
     else return e->fail(PDPD_E_INVALID, "Unknown engine config name '%s'", key);
     e->drop_graph();  // layout-dependent settings take effect at the next attach / capture
     return PDPD_OK;

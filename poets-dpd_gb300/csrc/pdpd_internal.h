@@ -40,6 +40,21 @@ struct Tile {
 // Beads per tile = threads per block of the step kernels.
 constexpr int TILE_BEADS = 128;
 
+// A brick of cells of one world: the unit of work of the FP32 force kernel, which stages
+// the brick and its one-cell halo in shared memory.  Bricks are cut at the box faces, so
+// edge bricks can be smaller than the nominal shape.
+struct Brick {
+    uint32_t world;
+    int32_t x0, y0, z0;  // first cell of the brick (world cell coordinates)
+    int32_t bx, by, bz;  // brick extent in cells
+    uint32_t pad;
+};
+
+// Nominal brick shape and the shared-memory budget of one staged brick + halo.
+constexpr int BRICK_X = 4, BRICK_Y = 4, BRICK_Z = 4;
+constexpr int BRICK_HALO_CELLS = (BRICK_X + 2) * (BRICK_Y + 2) * (BRICK_Z + 2);
+constexpr int BRICK_MAX_BEADS = 1024;
+
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
     ERR_NONFINITE = 2u,     // non-finite position / velocity / force
@@ -64,6 +79,8 @@ struct KArgs {
     uint32_t n_worlds;
     const Tile *tiles;
     uint32_t n_tiles;
+    const Brick *bricks;
+    uint32_t n_bricks;
     uint32_t n_beads;  // total over all worlds
     uint32_t n_cells;  // total over all worlds
     uint32_t *start;   // n_cells+1: first slot of each cell (sorted order); start[n_cells] = n_beads
@@ -88,6 +105,8 @@ struct KArgs {
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
+    int force_kernel;    // FP32: 0 = brick kernel (shared-memory staged), 1 = thread per bead
+    int brick_grid;      // persistent grid size of the brick kernel
 };
 
 // Kernel launchers.  Each returns the number of kernels it launched.
@@ -115,6 +134,8 @@ int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uin
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
 
 size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
+int brick_grid_blocks(int sm_count);  // resident brick-kernel blocks on the whole GPU
+size_t brick_smem_bytes();
 uint32_t scan_blocks(uint32_t n_cells);
 
 }  // namespace pdpd

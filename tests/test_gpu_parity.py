@@ -105,10 +105,12 @@ def test_fp64_bit_exact_large_box_one_step():
 
 # ---------------------------------------------------------------------------- FP32
 
+@pytest.mark.parametrize("force_kernel", [0, 1])
 @pytest.mark.parametrize("name", [n for n in world_fixture_names() if n != "empty_world"])
-def test_fp32_vs_reference(name):
+def test_fp32_vs_reference(name, force_kernel):
     world, ref = load_world_fixture(name)
     eng = E.GB300DPDEngine("fp32")
+    eng.SetConfigEntry("force_kernel", force_kernel)
     eng.Attach(world)
     eng.Run(1)
     assert world.t == ref["t"][0]
@@ -118,10 +120,12 @@ def test_fp32_vs_reference(name):
     assert np.max(np.abs(dx)) < 1e-6
 
 
-def test_fp32_polymer_box_one_and_ten_steps():
+@pytest.mark.parametrize("force_kernel", [0, 1])
+def test_fp32_polymer_box_one_and_ten_steps(force_kernel):
     world = W.make_polymer_box(32, chain_fraction=0.1, seed=2)
     ow = O.OracleWorld(world)
     eng = E.GB300DPDEngine("fp32")
+    eng.SetConfigEntry("force_kernel", force_kernel)
     eng.Attach(world)
     eng.Run(1)
     ow.run(1, nthreads=16)
@@ -207,12 +211,23 @@ def test_batch_equals_alone(prec):
         assert np.array_equal(a.f, b.f)
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64"])
-def test_launch_configurations_agree(prec):
+LAUNCH_CONFIGS = {
+    # The brick kernel's sum order depends only on the data, not on the grid or on graphs.
+    "fp32": ({}, {"use_graphs": 0}, {"grid_blocks": 3}, {"graph_steps": 5}),
+    "fp32_bead": ({"force_kernel": 1}, {"force_kernel": 1, "list_capacity": 1},
+                  {"force_kernel": 1, "list_capacity": 5, "grid_blocks": 3},
+                  {"force_kernel": 1, "use_graphs": 0}),
+    "fp64": ({}, {"use_graphs": 0}, {"list_capacity": 1}, {"list_capacity": 5, "grid_blocks": 3},
+             {"graph_steps": 5}),
+}
+
+
+@pytest.mark.parametrize("variant", sorted(LAUNCH_CONFIGS))
+def test_launch_configurations_agree(variant):
+    prec = variant.split("_")[0]
     world = W.make_polymer_box(12, chain_fraction=0.1, seed=9)
     results = []
-    for cfg in ({}, {"use_graphs": 0}, {"list_capacity": 1}, {"list_capacity": 5, "grid_blocks": 3},
-                {"graph_steps": 5}):
+    for cfg in LAUNCH_CONFIGS[variant]:
         w = world.copy()
         eng = E.GB300DPDEngine(prec)
         for k, v in cfg.items():
