@@ -91,7 +91,11 @@ const ConfigEntry kConfig[] = {
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
-    {"force_kernel", "FP32 force kernel: 0 = shared-memory brick kernel, 1 = thread per bead."},
+    {"force_kernel", "FP32 force kernel: 0 = shared-memory brick with neighbour lists, "
+                     "1 = thread per bead from global memory, 2 = shared-memory brick."},
+    {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
+    {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
+    {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
 };
 
 }  // namespace
@@ -112,6 +116,7 @@ struct pdpd_engine {
     int cfg_graph_steps = 0;
     int cfg_use_graphs = 1;
     int cfg_force_kernel = 0;
+    int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
 
     // attached worlds
     bool attached = false;
@@ -441,6 +446,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     // --- world table, tiles, pair table
     std::vector<Tile> tiles;
     std::vector<Brick> bricks;
+    double max_density = 0;
     std::vector<WorldDev> wdev(n_worlds);
     const bool f64 = e->fp64();
     std::vector<double> pair64;
@@ -463,11 +469,13 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
         d.t = w.t;
         for (uint32_t b = 0; b < w.n_beads; b += TILE_BEADS)
             tiles.push_back({i, bead_base + b, bead_base + std::min<uint32_t>(w.n_beads, b + TILE_BEADS), 0});
-        for (int x0 = 0; x0 < w.box[0]; x0 += BRICK_X)
-            for (int y0 = 0; y0 < w.box[1]; y0 += BRICK_Y)
-                for (int z0 = 0; z0 < w.box[2]; z0 += BRICK_Z)
-                    bricks.push_back({i, x0, y0, z0, std::min(BRICK_X, w.box[0] - x0),
-                                      std::min(BRICK_Y, w.box[1] - y0), std::min(BRICK_Z, w.box[2] - z0), 0});
+        for (int x0 = 0; x0 < w.box[0]; x0 += e->cfg_brick[0])
+            for (int y0 = 0; y0 < w.box[1]; y0 += e->cfg_brick[1])
+                for (int z0 = 0; z0 < w.box[2]; z0 += e->cfg_brick[2])
+                    bricks.push_back({i, x0, y0, z0, std::min(e->cfg_brick[0], w.box[0] - x0),
+                                      std::min(e->cfg_brick[1], w.box[1] - y0),
+                                      std::min(e->cfg_brick[2], w.box[2] - z0), 0});
+        max_density = std::max(max_density, (double)w.n_beads / (double)d.n_cells);
         for (uint32_t k = 0; k < w.n_bead_types * w.n_bead_types; k++) {
             double a = w.conservative[k], sg = std::sqrt(w.dissipative[k]);
             pair64.push_back(a);
@@ -654,8 +662,22 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
     a.list_capacity = e->cfg_list_capacity;
     a.force_kernel = e->cfg_force_kernel;
-    a.brick_grid = f64 ? 0 : brick_grid_blocks(e->sm_count);
-    if (e->cfg_grid_blocks > 0) a.brick_grid = e->cfg_grid_blocks;
+    if (!f64 && a.force_kernel != 1) {
+        // Staged-bead capacity: 1.5x the expected halo population of the densest world (and
+        // at most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
+        a.brick_hc_max = (uint32_t)(e->cfg_brick[0] + 2) * (e->cfg_brick[1] + 2) * (e->cfg_brick[2] + 2);
+        double want = 1.5 * max_density * a.brick_hc_max + 64;
+        a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
+        int grid = 0;
+        uint32_t bytes = 0;
+        int rc = brick_setup(e->sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, &grid, &bytes);
+        if (rc) {
+            e->release();
+            return e->fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
+                           cudaGetErrorString((cudaError_t)rc));
+        }
+        a.brick_grid = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : grid;
+    }
     a.grid_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)gb, e->n_tiles));
 
     // --- bin + sort into the rest state
@@ -862,7 +884,7 @@ int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len,
     if (!e) return PDPD_E_INVALID;
     if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
     int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs,
-                  e->cfg_force_kernel};
+                  e->cfg_force_kernel, e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2]};
     if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
     if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
     if (value && value_len) snprintf(value, value_len, "%d", vals[index]);
@@ -880,7 +902,17 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "grid_blocks") e->cfg_grid_blocks = (int)v;
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
-    else if (k == "force_kernel") e->cfg_force_kernel = v ? 1 : 0;
+    else if (k == "force_kernel") {
+        if (v > 2) return e->fail(PDPD_E_INVALID, "force_kernel must be 0, 1 or 2");
+        e->cfg_force_kernel = (int)v;
+    } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {
+        int idx = k == "brick_x" ? 0 : (k == "brick_y" ? 1 : 2);
+        int nb[3] = {e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2]};
+        nb[idx] = (int)v;
+        if (v < 1 || v > 32 || nb[0] * nb[1] > 64 || (nb[0] + 2) * (nb[1] + 2) * (nb[2] + 2) > 2048)
+            return e->fail(PDPD_E_INVALID, "brick shape %dx%dx%d out of range", nb[0], nb[1], nb[2]);
+        e->cfg_brick[idx] = (int)v;
+    }
     else return e->fail(PDPD_E_INVALID, "Unknown engine config name '%s'", key);
     e->drop_graph();  // layout-dependent settings take effect at the next attach / capture
     return PDPD_OK;

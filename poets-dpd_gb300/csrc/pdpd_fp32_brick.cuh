@@ -1,0 +1,256 @@
+// FP32 brick force kernel.  Included inside pdpd_fp32.cu's anonymous namespace (it uses the
+// helpers defined there: WorldCache, load_world, advance_position, bond_forces32, pack_dir).
+//
+// A block takes one brick of cells of one world and stages the brick plus its one-cell halo
+// -- (bx+2)(by+2)(bz+2) halo cells, z fastest -- into shared memory with coalesced float4
+// loads: for each (x, y) halo row the cells z0-1 .. z0+bz are consecutive cells of the sorted
+// state, i.e. one or (at a periodic wrap) a few contiguous runs of slots.  A halo cell that
+// is a periodic image of a cell already staged (boxes smaller than the halo) is staged again,
+// so every neighbour is seen at its own image position, as the reference's direction loop
+// sees it (naive_dpd_engine_half_step.hpp:300-315).
+//
+// Then one thread per home bead gathers its pair forces from shared memory: the 27
+// neighbour cells in the reference's direction order, each cell's beads in id order,
+// accumulated one pair at a time.  In the list variant the thread first filters the
+// candidates and keeps the in-range ones (16-bit entries: staged index + direction) in a
+// shared-memory list, then evaluates the list in order; the divergent, expensive force
+// evaluation then runs on denser warps.  Both variants, the thread-per-bead global-memory
+// kernel and the overflow fallback produce bit-identical forces: the same explicitly
+// rounded pair routine, the same order.
+
+constexpr int BRICK_THREADS = 128;
+constexpr int BRICK_WARPS = BRICK_THREADS / 32;
+constexpr int BLIST_MAX = 32;
+constexpr int BRICK_MAX_ROWS = 64;
+
+struct BrickHeader {
+    WorldCache wc;
+    float2 pair[MAX_PAIR];
+    uint32_t wsum[BRICK_WARPS];
+    uint32_t home_rows[BRICK_MAX_ROWS + 1];
+};
+
+// Shared-memory layout of one block: header, hstart[HC+1], hslot[HC], pos[maxb], vel[maxb],
+// list[BLIST_MAX][BRICK_THREADS].
+struct BrickLayout {
+    uint32_t hc_max, maxb;
+    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_list, bytes;
+};
+
+__host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, int with_list)
+{
+    BrickLayout L;
+    L.hc_max = hc_max;
+    L.maxb = maxb;
+    uint32_t off = (uint32_t)((sizeof(BrickHeader) + 15) & ~size_t(15));
+    L.off_hstart = off;
+    off += 4 * (hc_max + 1);
+    L.off_hslot = off;
+    off += 4 * hc_max;
+    off = (off + 15) & ~15u;
+    L.off_pos = off;
+    off += 16 * maxb;
+    L.off_vel = off;
+    off += 16 * maxb;
+    L.off_list = off;
+    if (with_list) off += 2 * BLIST_MAX * BRICK_THREADS;
+    L.bytes = off;
+    return L;
+}
+
+// Evaluate list entries [0, n) of this thread in order, adding to F.
+__device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
+                                                const float4 *__restrict__ svel,
+                                                const uint16_t *__restrict__ list, int n,
+                                                const float4 pi, const float4 vi,
+                                                const float2 *pair, uint32_t nt, uint32_t th_lo,
+                                                uint32_t th_hi, float scale, float F[3])
+{
+    const uint32_t hi = __float_as_uint(pi.w);
+    const uint32_t ti = min(hi >> 28, nt - 1u);
+    for (int k = 0; k < n; k++) {
+        const uint32_t e = list[k * BRICK_THREADS + threadIdx.x];
+        const uint32_t j = e & 2047u, d = e >> 11;  // d = (dx+1)*9 + (dy+1)*3 + (dz+1)
+        const float4 pj = spos[j];
+        const float ax = __fsub_rn(pi.x, (float)((int)(d / 9u) - 1));
+        const float ay = __fsub_rn(pi.y, (float)((int)((d / 3u) % 3u) - 1));
+        const float az = __fsub_rn(pi.z, (float)((int)(d % 3u) - 1));
+        float dx, dy, dz;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+        const uint32_t hj = __float_as_uint(pj.w);
+        pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj, pair[ti * nt + min(hj >> 28, nt - 1u)],
+                        th_lo, th_hi, scale, F);
+    }
+}
+
+template <int FINAL, int LIST>
+__global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickLayout lay)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
+    uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
+    uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
+    float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
+    float4 *svel = reinterpret_cast<float4 *>(smem_raw + lay.off_vel);
+    uint16_t *list = reinterpret_cast<uint16_t *>(smem_raw + lay.off_list);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) H.wc.world = 0xffffffffu;
+    __syncthreads();
+    const float min2 = min_dist_sqr_f();
+    const float PRUNE = 1.0001f;
+    const int cap = (a.list_capacity > 0 && a.list_capacity < BLIST_MAX) ? a.list_capacity : BLIST_MAX;
+    for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi += gridDim.x) {
+        const Brick br = a.bricks[bi];
+        load_world(a, br.world, H.wc, H.pair);
+        __syncthreads();
+        const WorldDev &w = H.wc.w;
+        const uint32_t nt = w.n_types;
+        const float scale = (float)w.scale_inv_sqrt_dt;
+        const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+        const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+        const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
+        const int HC = HX * HY * HZ;
+
+        // ---- 1. halo cells: first global slot and count; block exclusive scan -> hstart
+        const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
+        const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
+        uint32_t tsum = 0;
+        for (int hc = hc_begin; hc < hc_end; hc++) {
+            const int hx = hc / (HY * HZ), rem = hc - hx * HY * HZ;
+            const int hy = rem / HZ, hz = rem - hy * HZ;
+            const int gx = wrap_index(br.x0 - 1 + hx, w.L[0]);
+            const int gy = wrap_index(br.y0 - 1 + hy, w.L[1]);
+            const int gz = wrap_index(br.z0 - 1 + hz, w.L[2]);
+            const uint32_t c = w.cell_base + ((uint32_t)gx * (uint32_t)w.L[1] + (uint32_t)gy) * (uint32_t)w.L[2] + (uint32_t)gz;
+            const uint32_t s0 = a.start[c];
+            const uint32_t n = a.start[c + 1] - s0;
+            hslot[hc] = s0;
+            hstart[hc] = n;  // count for now
+            tsum += n;
+        }
+        uint32_t inc = tsum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += y;
+        }
+        if (lane == 31) H.wsum[warp] = inc;
+        __syncthreads();
+        uint32_t run = inc - tsum, total = 0;
+        for (int k = 0; k < BRICK_WARPS; k++) {
+            if (k < warp) run += H.wsum[k];
+            total += H.wsum[k];
+        }
+        for (int hc = hc_begin; hc < hc_end; hc++) {
+            const uint32_t n = hstart[hc];
+            hstart[hc] = run;
+            run += n;
+        }
+        if (tid == 0) hstart[HC] = total;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t acc = 0;
+            for (int r = 0; r < br.bx * br.by; r++) {
+                H.home_rows[r] = acc;
+                const int lx = r / br.by, ly = r - lx * br.by;
+                const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+                acc += hstart[hc0 + br.bz] - hstart[hc0];
+            }
+            H.home_rows[br.bx * br.by] = acc;
+        }
+        __syncthreads();
+        const uint32_t n_home = H.home_rows[br.bx * br.by];
+        const bool staged = total <= lay.maxb;
+
+        // ---- 2. stage the halo, one (x, y) halo row per warp iteration (coalesced)
+        if (staged) {
+            for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
+                const int hc0 = row * HZ;
+                const uint32_t base = hstart[hc0];
+                const uint32_t len = hstart[hc0 + HZ] - base;
+                for (uint32_t k = lane; k < len; k += 32) {
+                    int z = 0;
+                    while (hstart[hc0 + z + 1] - base <= k) z++;
+                    const uint32_t slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
+                    spos[base + k] = ((const float4 *)a.posA)[slot];
+                    svel[base + k] = ((const float4 *)a.velA)[slot];
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- 3. one thread per home bead: pair forces, bonds, integration
+        uint32_t err = 0;
+        for (uint32_t t = tid; t < n_home; t += BRICK_THREADS) {
+            int r = 0;
+            while (H.home_rows[r + 1] <= t) r++;
+            const int lx = r / br.by, ly = r - lx * br.by;
+            const int hx = lx + 1, hy = ly + 1;
+            const int hc0 = (hx * HY + hy) * HZ + 1;
+            const uint32_t k = t - H.home_rows[r];
+            const uint32_t s = hslot[hc0] + k;
+            float F[3] = {0.f, 0.f, 0.f};
+            if (!staged) {
+                // Halo larger than the shared-memory budget: gather from global memory.
+                const float4 ph = ((const float4 *)a.posA)[s];
+                const float4 vh = ((const float4 *)a.velA)[s];
+                int c[3];
+                decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+                pair_forces32_seq(a, w, H.pair, th_lo, th_hi, scale, c, ph, vh, F);
+                integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
+                continue;
+            }
+            const uint32_t si = hstart[hc0] + k;
+            int z = 0;
+            while (hstart[hc0 + z + 1] <= si) z++;
+            const int hz = z + 1;
+            const float4 pi = spos[si], vi = svel[si];
+            const uint32_t hi = __float_as_uint(pi.w);
+            const uint32_t ti = min(hi >> 28, nt - 1u);
+            int n = 0;
+            for (int ddx = -1; ddx <= 1; ddx++) {
+                const float gx = slab_gap(pi.x, ddx);
+                const float ax = __fsub_rn(pi.x, (float)ddx);
+                for (int ddy = -1; ddy <= 1; ddy++) {
+                    const float gy = slab_gap(pi.y, ddy);
+                    const float gxy = gx * gx + gy * gy;
+                    if (gxy >= PRUNE) continue;
+                    const float ay = __fsub_rn(pi.y, (float)ddy);
+                    const int rowc = ((hx + ddx) * HY + (hy + ddy)) * HZ + hz;
+                    for (int ddz = -1; ddz <= 1; ddz++) {
+                        const float gz = slab_gap(pi.z, ddz);
+                        if (gxy + gz * gz >= PRUNE) continue;
+                        const float az = __fsub_rn(pi.z, (float)ddz);
+                        const uint32_t j1 = hstart[rowc + ddz + 1];
+                        const uint16_t dpk = (uint16_t)(((ddx + 1) * 9 + (ddy + 1) * 3 + (ddz + 1)) << 11);
+                        for (uint32_t j = hstart[rowc + ddz]; j < j1; j++) {
+                            const float4 pj = spos[j];
+                            float dx, dy, dz;
+                            const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                            if (r2 < 1.0f && r2 >= min2) {
+                                if (LIST) {
+                                    if (n == cap) {
+                                        brick_list_eval(spos, svel, list, n, pi, vi, H.pair, nt, th_lo,
+                                                        th_hi, scale, F);
+                                        n = 0;
+                                    }
+                                    list[n * BRICK_THREADS + tid] = (uint16_t)(j | dpk);
+                                    n++;
+                                } else {
+                                    const uint32_t hj = __float_as_uint(pj.w);
+                                    pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
+                                                    H.pair[ti * nt + min(hj >> 28, nt - 1u)], th_lo,
+                                                    th_hi, scale, F);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+            const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
+            integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
+        }
+        if (err) atomicOr(&a.worlds[br.world].err, err);
+    }
+}

@@ -50,10 +50,8 @@ struct Brick {
     uint32_t pad;
 };
 
-// Nominal brick shape and the shared-memory budget of one staged brick + halo.
+// Default brick shape (cells); bx * by <= 64.
 constexpr int BRICK_X = 4, BRICK_Y = 4, BRICK_Z = 4;
-constexpr int BRICK_HALO_CELLS = (BRICK_X + 2) * (BRICK_Y + 2) * (BRICK_Z + 2);
-constexpr int BRICK_MAX_BEADS = 1024;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
@@ -105,8 +103,11 @@ struct KArgs {
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
-    int force_kernel;    // FP32: 0 = brick kernel (shared-memory staged), 1 = thread per bead
+    int force_kernel;    // FP32: 0 = brick kernel with neighbour lists, 2 = brick kernel,
+                         // 1 = thread per bead from global memory
     int brick_grid;      // persistent grid size of the brick kernel
+    uint32_t brick_hc_max;  // halo cells of the nominal brick shape
+    uint32_t brick_maxb;    // staged-bead capacity of one brick
 };
 
 // Kernel launchers.  Each returns the number of kernels it launched.
@@ -134,8 +135,8 @@ int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uin
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
 
 size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
-int brick_grid_blocks(int sm_count);  // resident brick-kernel blocks on the whole GPU
-size_t brick_smem_bytes();
+int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *grid,
+                uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
 
 }  // namespace pdpd

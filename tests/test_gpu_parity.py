@@ -105,7 +105,7 @@ def test_fp64_bit_exact_large_box_one_step():
 
 # ---------------------------------------------------------------------------- FP32
 
-@pytest.mark.parametrize("force_kernel", [0, 1])
+@pytest.mark.parametrize("force_kernel", [0, 1, 2])
 @pytest.mark.parametrize("name", [n for n in world_fixture_names() if n != "empty_world"])
 def test_fp32_vs_reference(name, force_kernel):
     world, ref = load_world_fixture(name)
@@ -212,19 +212,57 @@ def test_batch_equals_alone(prec):
 
 
 LAUNCH_CONFIGS = {
-    # The brick kernel's sum order depends only on the data, not on the grid or on graphs.
-    "fp32": ({}, {"use_graphs": 0}, {"grid_blocks": 3}, {"graph_steps": 5}),
-    "fp32_bead": ({"force_kernel": 1}, {"force_kernel": 1, "list_capacity": 1},
-                  {"force_kernel": 1, "list_capacity": 5, "grid_blocks": 3},
-                  {"force_kernel": 1, "use_graphs": 0}),
+    # Every FP32 force kernel (shared-memory brick with or without neighbour lists, any brick
+    # shape; thread per bead from global memory) adds the same pair terms in the same order
+    # with the same roundings, so all of them give bit-identical trajectories.
+    "fp32": ({}, {"use_graphs": 0}, {"grid_blocks": 3}, {"graph_steps": 5},
+             {"force_kernel": 2}, {"force_kernel": 1}, {"force_kernel": 1, "list_capacity": 1},
+             {"list_capacity": 1}, {"list_capacity": 3, "force_kernel": 0},
+             {"brick_x": 2, "brick_y": 2, "brick_z": 2}, {"brick_x": 8, "brick_y": 4, "brick_z": 8},
+             {"brick_x": 3, "brick_y": 5, "brick_z": 7, "force_kernel": 2}),
     "fp64": ({}, {"use_graphs": 0}, {"list_capacity": 1}, {"list_capacity": 5, "grid_blocks": 3},
              {"graph_steps": 5}),
 }
 
 
+def clustered_world():
+    """8^3 box with half the beads packed into a 2x2x2-cell corner: the halo of a brick there
+    holds far more beads than the shared-memory budget, so the brick kernel falls back to the
+    global-memory gather for it."""
+    w = W.make_water(8, seed=5, dt=0.005)
+    rng = np.random.default_rng(7)
+    half = w.n_beads // 2
+    w.x[:half] = 3.0 + 2.0 * rng.random((half, 3))
+    return w
+
+
+@pytest.mark.parametrize("force_kernel", [0, 2])
+def test_fp32_brick_overflow_fallback(force_kernel):
+    world = clustered_world()
+    ref = world.copy()
+    e1 = E.GB300DPDEngine("fp32")
+    e1.SetConfigEntry("force_kernel", 1)
+    e1.Attach(ref)
+    e1.Run(2)
+    w = world.copy()
+    e2 = E.GB300DPDEngine("fp32")
+    e2.SetConfigEntry("force_kernel", force_kernel)
+    e2.Attach(w)
+    e2.Run(2)
+    assert np.array_equal(w.x, ref.x) and np.array_equal(w.f, ref.f)
+    ow = O.OracleWorld(world)
+    ow.run(1)
+    w1 = world.copy()
+    e3 = E.GB300DPDEngine("fp32")
+    e3.SetConfigEntry("force_kernel", force_kernel)
+    e3.Attach(w1)
+    e3.Run(1)
+    assert force_rel_err(w1.f, ow.f) <= FP32_FORCE_TOL
+
+
 @pytest.mark.parametrize("variant", sorted(LAUNCH_CONFIGS))
 def test_launch_configurations_agree(variant):
-    prec = variant.split("_")[0]
+    prec = variant
     world = W.make_polymer_box(12, chain_fraction=0.1, seed=9)
     results = []
     for cfg in LAUNCH_CONFIGS[variant]:
