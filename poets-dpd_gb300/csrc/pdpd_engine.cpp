@@ -92,7 +92,8 @@ const ConfigEntry kConfig[] = {
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
     {"force_kernel", "FP32 force kernel: 0 = shared-memory brick with neighbour lists, "
-                     "1 = thread per bead from global memory, 2 = shared-memory brick."},
+                     "1 = thread per bead from global memory, 2 = shared-memory brick, "
+                     "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence."},
     {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
@@ -127,7 +128,7 @@ struct pdpd_engine {
     DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
-    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
@@ -169,7 +170,7 @@ struct pdpd_engine {
         DevBuf *bufs[] = {&d_worlds, &d_tiles, &d_bricks, &d_start, &d_cnt, &d_blocksums, &d_posA, &d_velA,
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
-                          &d_pair, &d_hash, &d_staging[0], &d_staging[1]};
+                          &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1]};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -570,6 +571,13 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     A(e->d_bond_params, (f64 ? sizeof(double) : sizeof(float)) * 4 * std::max<uint64_t>(1, n_bparams));
     A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
     A(e->d_hash, sizeof(uint32_t) * nb);
+    // Polymer beads (monomer bit of the hash clear), for the FP32 bond kernel.
+    std::vector<uint32_t> bonded;
+    for (uint32_t i = 0; i < n_worlds; i++)
+        for (uint32_t k = 0; k < ws[i].n_beads; k++)
+            if (!(ws[i].hash[k] & (1u << 27))) bonded.push_back(wdev[i].bead_base + k);
+    A(e->d_bonded, sizeof(uint32_t) * std::max<size_t>(1, bonded.size()));
+    A(e->d_fbond, f64 ? 16 : sizeof(float4) * std::max<uint64_t>(1, nb));
     A(e->d_staging[0], sizeof(double) * 9 * nb);
     if (ce != cudaSuccess) {
         cudaGetLastError();
@@ -618,6 +626,7 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     }
     H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
     H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
+    H2D(e->d_bonded, bonded.data(), sizeof(uint32_t) * bonded.size());
     if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_cnt.p, 0, sizeof(uint32_t) * nc, s);
     uint32_t total = (uint32_t)nb;  // start[n_cells] = total beads, fixed for the attach
     if (ce == cudaSuccess)
@@ -657,6 +666,9 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.bond_terms = e->d_bond_terms.as<BondTerm>();
     a.bond_params = e->d_bond_params.p;
     a.pair = e->d_pair.p;
+    a.bonded_ids = e->d_bonded.as<uint32_t>();
+    a.n_bonded = f64 ? 0u : (uint32_t)bonded.size();
+    a.fbond = e->d_fbond.as<float4>();
     a.staging = e->d_staging[0].as<double>();
     a.block_threads = 128;
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
@@ -903,7 +915,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
     else if (k == "force_kernel") {
-        if (v > 2) return e->fail(PDPD_E_INVALID, "force_kernel must be 0, 1 or 2");
+        if (v > 5) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..5");
         e->cfg_force_kernel = (int)v;
     } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {
         int idx = k == "brick_x" ? 0 : (k == "brick_y" ? 1 : 2);

@@ -241,7 +241,12 @@ __device__ __forceinline__ void integrate32(const KArgs &a, const WorldDev &w, u
 {
     const float dt = (float)w.dt, hdt = 0.5f * dt, hdt2 = 0.5f * dt * dt;
     float o[3] = {ph.x, ph.y, ph.z};
-    if (!(__float_as_uint(ph.w) & (1u << 27))) bond_forces32(a, w, a.ids[s], c, o, F, err);
+    if (!(__float_as_uint(ph.w) & (1u << 27))) {  // polymer bead: its bond force, from k_bonds32
+        const float4 fb = a.fbond[s];
+        F[0] = __fadd_rn(F[0], fb.x);
+        F[1] = __fadd_rn(F[1], fb.y);
+        F[2] = __fadd_rn(F[2], fb.z);
+    }
     // update_mom (dpd_maths_core_half_step.hpp:51-61)
     float v[3] = {__fmaf_rn(F[0], hdt, vh.x), __fmaf_rn(F[1], hdt, vh.y), __fmaf_rn(F[2], hdt, vh.z)};
     if (FINAL) {
@@ -256,6 +261,33 @@ __device__ __forceinline__ void integrate32(const KArgs &a, const WorldDev &w, u
                                             __fmaf_rn(F[2], hdt, v[2]), 0.f);
         a.keyrank[s] = make_uint2(key, rank);
     }
+}
+
+// Bond forces of every polymer bead (monomer bit of the hash clear), one thread per bead,
+// written by sorted slot for the force kernel to add.  Running them here, on a compact list
+// of the few bonded beads, keeps their dependent partner lookups out of the pair kernel's
+// warps.
+__global__ void __launch_bounds__(128) k_bonds32(KArgs a)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n_bonded) return;
+    const uint32_t id = a.bonded_ids[k];
+    uint32_t lo = 0, hi = a.n_worlds;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (a.worlds[mid].bead_base <= id) lo = mid; else hi = mid;
+    }
+    const WorldDev &w = a.worlds[lo];
+    const uint32_t s = a.slot_of_id[id];
+    const float4 p = ((const float4 *)a.posA)[s];
+    int c[3];
+    decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+    const float o[3] = {p.x, p.y, p.z};
+    float F[3] = {0.f, 0.f, 0.f};
+    uint32_t err = 0;
+    bond_forces32(a, w, id, c, o, F, err);
+    a.fbond[s] = make_float4(F[0], F[1], F[2], 0.f);
+    if (err) atomicOr(&a.worlds[lo].err, err);
 }
 
 // Thread-per-bead pair forces straight from global memory, summed one pair at a time in the
@@ -536,24 +568,34 @@ int launch_begin32(const KArgs &a, cudaStream_t s)
 int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *grid,
                 uint32_t *smem_bytes)
 {
-    const int list = variant == 0 ? 1 : 0;
+    int nb = 0;
+    if (variant == 5) {
+        const CellLayout C = cell_layout(hc_max, maxb);
+        cudaError_t e = cudaFuncSetAttribute(k_force32_cells<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_force32_cells<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force32_cells<0>, BRICK_THREADS, C.bytes);
+        if (e != cudaSuccess) return (int)e;
+        if (nb < 1) return (int)cudaErrorInvalidConfiguration;
+        *grid = nb * sm_count;
+        *smem_bytes = C.bytes;
+        return 0;
+    }
+    const int list = (variant == 0 || variant == 3) ? 1 : 0;
     const BrickLayout L = brick_layout(hc_max, maxb, list);
     const int bytes = (int)L.bytes;
-    int nb = 0;
-    cudaError_t e;
-    if (list) {
-        e = cudaFuncSetAttribute(k_force32_brick<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_force32_brick<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force32_brick<0, 1>, BRICK_THREADS, bytes);
-    } else {
-        e = cudaFuncSetAttribute(k_force32_brick<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_force32_brick<1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force32_brick<0, 0>, BRICK_THREADS, bytes);
+    void (*k0)(KArgs, BrickLayout) = nullptr;
+    void (*k1)(KArgs, BrickLayout) = nullptr;
+    switch (variant) {
+    case 0: k0 = k_force32_brick<0, 1, 0>; k1 = k_force32_brick<1, 1, 0>; break;
+    case 2: k0 = k_force32_brick<0, 0, 0>; k1 = k_force32_brick<1, 0, 0>; break;
+    case 3: k0 = k_force32_brick<0, 1, 1>; k1 = k_force32_brick<1, 1, 1>; break;
+    default: k0 = k_force32_brick<0, 0, 1>; k1 = k_force32_brick<1, 0, 1>; break;
     }
+    cudaError_t e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k0, BRICK_THREADS, bytes);
     if (e != cudaSuccess) return (int)e;
     if (nb < 1) return (int)cudaErrorInvalidConfiguration;
     *grid = nb * sm_count;
@@ -561,23 +603,42 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
     return 0;
 }
 
+static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s);
+
 int launch_force32(const KArgs &a, int final_step, cudaStream_t s)
 {
+    int n = 0;
+    if (a.n_bonded > 0) {
+        k_bonds32<<<(a.n_bonded + 127) / 128, 128, 0, s>>>(a);
+        n++;
+    }
+    return n + launch_pair_forces32(a, final_step, s);
+}
+
+static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
+{
+    if (a.force_kernel == 5 && a.n_bricks > 0) {
+        const CellLayout C = cell_layout(a.brick_hc_max, a.brick_maxb);
+        const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
+        if (final_step)
+            k_force32_cells<1><<<grid, BRICK_THREADS, C.bytes, s>>>(a, C);
+        else
+            k_force32_cells<0><<<grid, BRICK_THREADS, C.bytes, s>>>(a, C);
+        return 1;
+    }
     if (a.force_kernel != 1 && a.n_bricks > 0) {
-        const int list = a.force_kernel == 0 ? 1 : 0;
+        const int v = a.force_kernel;
+        const int list = (v == 0 || v == 3) ? 1 : 0;
         const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, list);
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
-        if (list) {
-            if (final_step)
-                k_force32_brick<1, 1><<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
-            else
-                k_force32_brick<0, 1><<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
-        } else {
-            if (final_step)
-                k_force32_brick<1, 0><<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
-            else
-                k_force32_brick<0, 0><<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
+        void (*k)(KArgs, BrickLayout);
+        switch (v) {
+        case 0: k = final_step ? k_force32_brick<1, 1, 0> : k_force32_brick<0, 1, 0>; break;
+        case 2: k = final_step ? k_force32_brick<1, 0, 0> : k_force32_brick<0, 0, 0>; break;
+        case 3: k = final_step ? k_force32_brick<1, 1, 1> : k_force32_brick<0, 1, 1>; break;
+        default: k = final_step ? k_force32_brick<1, 0, 1> : k_force32_brick<0, 0, 1>; break;
         }
+        k<<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
         return 1;
     }
     if (final_step)

@@ -83,7 +83,77 @@ __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
     }
 }
 
-template <int FINAL, int LIST>
+// Pair forces of one staged home bead, with the 27 neighbour cells walked as one flat
+// sequence: the 9 neighbour rows (dx, dy) in order, each row's 3 cells (dz = -1, 0, +1) being
+// one contiguous range of staged beads.  Each thread's loop then runs for its own total
+// candidate count, instead of the warp paying the largest count of every cell in turn.
+// The sequence -- rows in order, cells in order, beads in order -- is the reference's
+// direction order, and pruned cells (nearest face >= 1 away) hold no in-range bead, so the
+// accumulated force is bit-identical to the nested-loop variants.
+template <int LIST>
+__device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spos,
+                                                  const float4 *__restrict__ svel,
+                                                  uint16_t *__restrict__ list, int cap,
+                                                  const uint32_t *__restrict__ hstart, int HY,
+                                                  int HZ, int hx, int hy, int hz, const float4 pi,
+                                                  const float4 vi, const float2 *pair, uint32_t nt,
+                                                  uint32_t th_lo, uint32_t th_hi, float scale,
+                                                  float F[3])
+{
+    const float PRUNE = 1.0001f;
+    const float min2 = min_dist_sqr_f();
+    const uint32_t hi = __float_as_uint(pi.w);
+    const uint32_t ti = min(hi >> 28, nt - 1u);
+    const float azm = __fsub_rn(pi.z, -1.0f), az0 = pi.z, azp = __fsub_rn(pi.z, 1.0f);
+    const float gzm = pi.z, gzp = 1.0f - pi.z;
+    int r = -1;
+    uint32_t j = 0, jend = 0, c1 = 0, c2 = 0;
+    float ax = 0.f, ay = 0.f;
+    int rdx = 0, rdy = 0;
+    int n = 0;
+    while (true) {
+        while (j >= jend) {  // next row with candidates
+            if (++r == 9) break;
+            rdx = r / 3 - 1;
+            rdy = r - (r / 3) * 3 - 1;
+            const float gx = slab_gap(pi.x, rdx), gy = slab_gap(pi.y, rdy);
+            const float gxy = gx * gx + gy * gy;
+            if (gxy >= PRUNE) continue;
+            const int hcz = ((hx + rdx) * HY + (hy + rdy)) * HZ + hz;
+            c1 = hstart[hcz];
+            c2 = hstart[hcz + 1];
+            j = gxy + gzm * gzm >= PRUNE ? c1 : hstart[hcz - 1];
+            jend = gxy + gzp * gzp >= PRUNE ? c2 : hstart[hcz + 2];
+            ax = __fsub_rn(pi.x, (float)rdx);
+            ay = __fsub_rn(pi.y, (float)rdy);
+        }
+        if (r == 9) break;
+        const float4 pj = spos[j];
+        const float az = j < c1 ? azm : (j < c2 ? az0 : azp);
+        float dx, dy, dz;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+        if (r2 < 1.0f && r2 >= min2) {
+            if (LIST) {
+                if (n == cap) {
+                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    n = 0;
+                }
+                const int ddz = j < c1 ? -1 : (j < c2 ? 0 : 1);
+                list[n * BRICK_THREADS + threadIdx.x] =
+                    (uint16_t)(j | (uint32_t)(((rdx + 1) * 9 + (rdy + 1) * 3 + (ddz + 1)) << 11));
+                n++;
+            } else {
+                const uint32_t hj = __float_as_uint(pj.w);
+                pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
+                                pair[ti * nt + min(hj >> 28, nt - 1u)], th_lo, th_hi, scale, F);
+            }
+        }
+        j++;
+    }
+    if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+}
+
+template <int FINAL, int LIST, int FLAT>
 __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickLayout lay)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -208,6 +278,13 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             const uint32_t hi = __float_as_uint(pi.w);
             const uint32_t ti = min(hi >> 28, nt - 1u);
             int n = 0;
+            if (FLAT) {
+                brick_gather_flat<LIST>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi, vi,
+                                        H.pair, nt, th_lo, th_hi, scale, F);
+                const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
+                integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
+                continue;
+            }
             for (int ddx = -1; ddx <= 1; ddx++) {
                 const float gx = slab_gap(pi.x, ddx);
                 const float ax = __fsub_rn(pi.x, (float)ddx);
@@ -250,6 +327,356 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
             const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
             integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
+        }
+        if (err) atomicOr(&a.worlds[br.world].err, err);
+    }
+}
+
+// =======================================================================================
+// Cell kernel: one warp per home cell.
+//
+// Same staging as the brick kernel.  A warp then takes a home cell: it writes the cell's
+// neighbourhood -- the 27 neighbour cells in the reference's direction order -- once into
+// an index array (staged index + direction), and for each home bead i sweeps that array
+// 32 neighbours at a time, one per lane, against a per-warp table of i's 27
+// direction-shifted positions.  In-range pairs are compacted with a warp ballot into a
+// queue; each full queue of 32 is evaluated one pair per lane and summed per home bead with
+// a segmented shuffle scan (the order is a fixed function of the data: deterministic).  A
+// thread-per-bead pass then adds bonds and integrates.
+// =======================================================================================
+
+constexpr int CELL_NBR_MAX = 384;  // neighbourhood beads per home cell handled by a warp
+constexpr int CELL_HOME_MAX = 64;  // home beads per cell handled by a warp
+constexpr int CELL_QCAP = 64;
+
+struct CellWarp {
+    uint32_t nbr[CELL_NBR_MAX];  // staged index | direction << 16
+    float4 shome[27];            // home bead position minus each direction
+    uint32_t queue[CELL_QCAP];   // staged index | direction << 11 | home index << 16
+    float fh[3][CELL_HOME_MAX];
+};
+
+struct CellLayout {
+    uint32_t hc_max, maxb;
+    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_f, off_warp, bytes;
+};
+
+__host__ __device__ inline CellLayout cell_layout(uint32_t hc_max, uint32_t maxb)
+{
+    CellLayout L;
+    L.hc_max = hc_max;
+    L.maxb = maxb;
+    uint32_t off = (uint32_t)((sizeof(BrickHeader) + 15) & ~size_t(15));
+    L.off_hstart = off;
+    off += 4 * (hc_max + 1);
+    L.off_hslot = off;
+    off += 4 * hc_max;
+    off = (off + 15) & ~15u;
+    L.off_pos = off;
+    off += 16 * maxb;
+    L.off_vel = off;
+    off += 16 * maxb;
+    L.off_f = off;
+    off += 12 * maxb;
+    off = (off + 15) & ~15u;
+    L.off_warp = off;
+    off += (uint32_t)sizeof(CellWarp) * BRICK_WARPS;
+    L.bytes = off;
+    return L;
+}
+
+__device__ __forceinline__ void cell_eval_queue(CellWarp &cw, int lane, int n, const float4 *spos,
+                                                const float4 *svel, uint32_t h0, const float2 *pair,
+                                                uint32_t nt, uint32_t th_lo, uint32_t th_hi,
+                                                float scale)
+{
+    float F[3] = {0.f, 0.f, 0.f};
+    uint32_t key = 0xffffffffu;
+    if (lane < n) {
+        const uint32_t e = cw.queue[lane];
+        const uint32_t j = e & 2047u, d = (e >> 11) & 31u, i = e >> 16;
+        const float4 pi = spos[h0 + i], vi = svel[h0 + i];
+        const float4 pj = spos[j];
+        const float ax = __fsub_rn(pi.x, (float)((int)(d / 9u) - 1));
+        const float ay = __fsub_rn(pi.y, (float)((int)((d / 3u) % 3u) - 1));
+        const float az = __fsub_rn(pi.z, (float)((int)(d % 3u) - 1));
+        float dx, dy, dz;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+        const uint32_t hi = __float_as_uint(pi.w), hj = __float_as_uint(pj.w);
+        pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
+                        pair[min(hi >> 28, nt - 1u) * nt + min(hj >> 28, nt - 1u)], th_lo, th_hi,
+                        scale, F);
+        key = i;
+    }
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float ux = __shfl_up_sync(0xffffffffu, F[0], off);
+        const float uy = __shfl_up_sync(0xffffffffu, F[1], off);
+        const float uz = __shfl_up_sync(0xffffffffu, F[2], off);
+        const uint32_t uk = __shfl_up_sync(0xffffffffu, key, off);
+        if (lane >= off && uk == key) {
+            F[0] = __fadd_rn(F[0], ux);
+            F[1] = __fadd_rn(F[1], uy);
+            F[2] = __fadd_rn(F[2], uz);
+        }
+    }
+    const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
+    if (lane < n && (lane == n - 1 || next != key)) {
+        cw.fh[0][key] = __fadd_rn(cw.fh[0][key], F[0]);
+        cw.fh[1][key] = __fadd_rn(cw.fh[1][key], F[1]);
+        cw.fh[2][key] = __fadd_rn(cw.fh[2][key], F[2]);
+    }
+    __syncwarp();
+}
+
+template <int FINAL>
+__global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLayout lay)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
+    uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
+    uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
+    float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
+    float4 *svel = reinterpret_cast<float4 *>(smem_raw + lay.off_vel);
+    float *sfx = reinterpret_cast<float *>(smem_raw + lay.off_f);
+    float *sfy = sfx + lay.maxb;
+    float *sfz = sfy + lay.maxb;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    CellWarp &cw = reinterpret_cast<CellWarp *>(smem_raw + lay.off_warp)[warp];
+    if (tid == 0) H.wc.world = 0xffffffffu;
+    __syncthreads();
+    const float min2 = min_dist_sqr_f();
+    for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi += gridDim.x) {
+        const Brick br = a.bricks[bi];
+        load_world(a, br.world, H.wc, H.pair);
+        __syncthreads();
+        const WorldDev &w = H.wc.w;
+        const uint32_t nt = w.n_types;
+        const float scale = (float)w.scale_inv_sqrt_dt;
+        const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+        const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+        const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
+        const int HC = HX * HY * HZ;
+
+        // ---- halo cells and staging (as in k_force32_brick)
+        const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
+        const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
+        uint32_t tsum = 0;
+        for (int hc = hc_begin; hc < hc_end; hc++) {
+            const int hx = hc / (HY * HZ), rem = hc - hx * HY * HZ;
+            const int hy = rem / HZ, hz = rem - hy * HZ;
+            const int gx = wrap_index(br.x0 - 1 + hx, w.L[0]);
+            const int gy = wrap_index(br.y0 - 1 + hy, w.L[1]);
+            const int gz = wrap_index(br.z0 - 1 + hz, w.L[2]);
+            const uint32_t c = w.cell_base + ((uint32_t)gx * (uint32_t)w.L[1] + (uint32_t)gy) * (uint32_t)w.L[2] + (uint32_t)gz;
+            const uint32_t s0 = a.start[c];
+            const uint32_t n = a.start[c + 1] - s0;
+            hslot[hc] = s0;
+            hstart[hc] = n;
+            tsum += n;
+        }
+        uint32_t inc = tsum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += y;
+        }
+        if (lane == 31) H.wsum[warp] = inc;
+        __syncthreads();
+        uint32_t run = inc - tsum, total = 0;
+        for (int k = 0; k < BRICK_WARPS; k++) {
+            if (k < warp) run += H.wsum[k];
+            total += H.wsum[k];
+        }
+        for (int hc = hc_begin; hc < hc_end; hc++) {
+            const uint32_t n = hstart[hc];
+            hstart[hc] = run;
+            run += n;
+        }
+        if (tid == 0) hstart[HC] = total;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t acc = 0;
+            for (int r = 0; r < br.bx * br.by; r++) {
+                H.home_rows[r] = acc;
+                const int lx = r / br.by, ly = r - lx * br.by;
+                const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+                acc += hstart[hc0 + br.bz] - hstart[hc0];
+            }
+            H.home_rows[br.bx * br.by] = acc;
+        }
+        __syncthreads();
+        const uint32_t n_home = H.home_rows[br.bx * br.by];
+        const bool staged = total <= lay.maxb;
+        if (staged) {
+            for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
+                const int hc0 = row * HZ;
+                const uint32_t base = hstart[hc0];
+                const uint32_t len = hstart[hc0 + HZ] - base;
+                for (uint32_t k = lane; k < len; k += 32) {
+                    int z = 0;
+                    while (hstart[hc0 + z + 1] - base <= k) z++;
+                    const uint32_t slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
+                    spos[base + k] = ((const float4 *)a.posA)[slot];
+                    svel[base + k] = ((const float4 *)a.velA)[slot];
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- pair forces: one warp per home cell
+        if (staged) {
+            const int n_home_cells = br.bx * br.by * br.bz;
+            for (int hcell = warp; hcell < n_home_cells; hcell += BRICK_WARPS) {
+                const int lx = hcell / (br.by * br.bz), rem = hcell - lx * br.by * br.bz;
+                const int ly = rem / br.bz, lz = rem - ly * br.bz;
+                const int hx = lx + 1, hy = ly + 1, hz = lz + 1;
+                const int hc = (hx * HY + hy) * HZ + hz;
+                const uint32_t h0 = hstart[hc];
+                const uint32_t nh = hstart[hc + 1] - h0;
+                if (nh == 0) continue;
+                // neighbour rows: r = (dx+1)*3 + (dy+1), 3 cells each
+                uint32_t a0 = 0, c1 = 0, c2 = 0, len = 0;
+                if (lane < 9) {
+                    const int hcz = ((hx + lane / 3 - 1) * HY + (hy + lane % 3 - 1)) * HZ + hz;
+                    a0 = hstart[hcz - 1];
+                    c1 = hstart[hcz];
+                    c2 = hstart[hcz + 1];
+                    len = hstart[hcz + 2] - a0;
+                }
+                uint32_t P = len;
+#pragma unroll
+                for (int off = 1; off < 16; off <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, P, off);
+                    if (lane >= off) P += y;
+                }
+                const uint32_t M = __shfl_sync(0xffffffffu, P, 8);
+                if (M > (uint32_t)CELL_NBR_MAX || nh > (uint32_t)CELL_HOME_MAX) {
+                    // crowded cell: one lane per home bead, sequential over the neighbours
+                    for (uint32_t i = lane; i < nh; i += 32) {
+                        const float4 pi = spos[h0 + i], vi = svel[h0 + i];
+                        const uint32_t hi = __float_as_uint(pi.w);
+                        const uint32_t ti = min(hi >> 28, nt - 1u);
+                        float F[3] = {0.f, 0.f, 0.f};
+                        for (int r = 0; r < 9; r++) {
+                            const int ddx = r / 3 - 1, ddy = r % 3 - 1;
+                            const int hcz = ((hx + ddx) * HY + (hy + ddy)) * HZ + hz;
+                            const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
+                            for (int ddz = -1; ddz <= 1; ddz++) {
+                                const float az = __fsub_rn(pi.z, (float)ddz);
+                                const uint32_t j1 = hstart[hcz + ddz + 1];
+                                for (uint32_t j = hstart[hcz + ddz]; j < j1; j++) {
+                                    const float4 pj = spos[j];
+                                    float dx, dy, dz;
+                                    const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                                    if (r2 < 1.0f && r2 >= min2) {
+                                        const uint32_t hj = __float_as_uint(pj.w);
+                                        pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
+                                                        H.pair[ti * nt + min(hj >> 28, nt - 1u)],
+                                                        th_lo, th_hi, scale, F);
+                                    }
+                                }
+                            }
+                        }
+                        sfx[h0 + i] = F[0];
+                        sfy[h0 + i] = F[1];
+                        sfz[h0 + i] = F[2];
+                    }
+                    __syncwarp();
+                    continue;
+                }
+                // neighbour index array, rows in order
+                for (int r = 0; r < 9; r++) {
+                    const uint32_t rb = r == 0 ? 0u : __shfl_sync(0xffffffffu, P, r - 1);
+                    const uint32_t ra = __shfl_sync(0xffffffffu, a0, r);
+                    const uint32_t rc1 = __shfl_sync(0xffffffffu, c1, r);
+                    const uint32_t rc2 = __shfl_sync(0xffffffffu, c2, r);
+                    const uint32_t rl = __shfl_sync(0xffffffffu, len, r);
+                    for (uint32_t k = lane; k < rl; k += 32) {
+                        const uint32_t j = ra + k;
+                        const uint32_t dz = j < rc1 ? 0u : (j < rc2 ? 1u : 2u);
+                        cw.nbr[rb + k] = j | ((uint32_t)(r * 3) + dz) << 16;
+                    }
+                }
+                for (uint32_t i = lane; i < nh; i += 32) {
+                    cw.fh[0][i] = 0.f;
+                    cw.fh[1][i] = 0.f;
+                    cw.fh[2][i] = 0.f;
+                }
+                __syncwarp();
+                int qn = 0;
+                for (uint32_t i = 0; i < nh; i++) {
+                    const float4 pi = spos[h0 + i];
+                    if (lane < 27) {
+                        cw.shome[lane] = make_float4(__fsub_rn(pi.x, (float)(lane / 9 - 1)),
+                                                     __fsub_rn(pi.y, (float)((lane / 3) % 3 - 1)),
+                                                     __fsub_rn(pi.z, (float)(lane % 3 - 1)), 0.f);
+                    }
+                    __syncwarp();
+                    for (uint32_t base = 0; base < M; base += 32) {
+                        const uint32_t jj = base + lane;
+                        bool inr = false;
+                        uint32_t entry = 0;
+                        if (jj < M) {
+                            const uint32_t e = cw.nbr[jj];
+                            const uint32_t j = e & 0xffffu, d = e >> 16;
+                            const float4 sh = cw.shome[d];
+                            float dx, dy, dz;
+                            const float r2 = pair_r2(sh.x, sh.y, sh.z, spos[j], dx, dy, dz);
+                            inr = r2 < 1.0f && r2 >= min2;
+                            entry = j | (d << 11) | (i << 16);
+                        }
+                        const uint32_t mask = __ballot_sync(0xffffffffu, inr);
+                        if (inr) cw.queue[qn + __popc(mask & ((1u << lane) - 1u))] = entry;
+                        qn += __popc(mask);
+                        __syncwarp();
+                        if (qn >= 32) {
+                            cell_eval_queue(cw, lane, 32, spos, svel, h0, H.pair, nt, th_lo, th_hi, scale);
+                            const uint32_t moved = lane + 32 < qn ? cw.queue[lane + 32] : 0u;
+                            __syncwarp();
+                            if (lane + 32 < qn) cw.queue[lane] = moved;
+                            qn -= 32;
+                            __syncwarp();
+                        }
+                    }
+                    __syncwarp();
+                }
+                if (qn > 0) cell_eval_queue(cw, lane, qn, spos, svel, h0, H.pair, nt, th_lo, th_hi, scale);
+                for (uint32_t i = lane; i < nh; i += 32) {
+                    sfx[h0 + i] = cw.fh[0][i];
+                    sfy[h0 + i] = cw.fh[1][i];
+                    sfz[h0 + i] = cw.fh[2][i];
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+
+        // ---- one thread per home bead: bonds and integration
+        uint32_t err = 0;
+        for (uint32_t t = tid; t < n_home; t += BRICK_THREADS) {
+            int r = 0;
+            while (H.home_rows[r + 1] <= t) r++;
+            const int lx = r / br.by, ly = r - lx * br.by;
+            const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+            const uint32_t k = t - H.home_rows[r];
+            const uint32_t s = hslot[hc0] + k;
+            if (!staged) {
+                const float4 ph = ((const float4 *)a.posA)[s];
+                const float4 vh = ((const float4 *)a.velA)[s];
+                int c[3];
+                decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+                float F[3] = {0.f, 0.f, 0.f};
+                pair_forces32_seq(a, w, H.pair, th_lo, th_hi, scale, c, ph, vh, F);
+                integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
+                continue;
+            }
+            const uint32_t si = hstart[hc0] + k;
+            int z = 0;
+            while (hstart[hc0 + z + 1] <= si) z++;
+            const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
+            float F[3] = {sfx[si], sfy[si], sfz[si]};
+            integrate32<FINAL>(a, w, s, c, spos[si], svel[si], F, err);
         }
         if (err) atomicOr(&a.worlds[br.world].err, err);
     }

@@ -98,6 +98,9 @@ struct KArgs {
     const BondTerm *bond_terms;
     const void *bond_params;   // float4 / Vec4d: (kappa, r0 | cos theta0, sin theta0, 0)
     const void *pair;          // float2 / Vec2d: (a_ij, sqrt(gamma_ij))
+    const uint32_t *bonded_ids;  // ids of the beads that have bond terms (FP32 bond kernel)
+    uint32_t n_bonded;
+    float4 *fbond;               // FP32: bond force of each bonded bead, by sorted slot
     // id-ordered staging for upload / download: 9 doubles per bead (x, v, f)
     double *staging;
     int block_threads;
@@ -120,7 +123,7 @@ struct KArgs {
 //   sort:   B -> A counting sort (pdpd_sort.cu)
 int launch_bin32(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
 int launch_begin32(const KArgs &a, cudaStream_t s);
-int launch_force32(const KArgs &a, int final_step, cudaStream_t s);
+int launch_force32(const KArgs &a, int final_step, cudaStream_t s);  // includes the bond kernel
 int launch_finish32(const KArgs &a, cudaStream_t s);
 int launch_unsort32(const KArgs &a, cudaStream_t s);
 int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
