@@ -165,6 +165,34 @@ int pdpd_profile_run(pdpd_engine *e, uint32_t n_steps, pdpd_phase_times *out);
 int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
                   const uint32_t *b, uint32_t *h_out, float *u_out);
 
+/* Allocation-free stepping -- this entry point has no counterpart in the reference.
+ *
+ * For callers that must not allocate device memory: a host thread that is capturing a
+ * CUDA stream into a graph (cudaMalloc cannot be captured), or a framework that owns all
+ * device memory through its own pool and forbids side allocations.  It advances one
+ * bond-free world by n_steps with the FP64 integrator (bit-identical to pdpd_run's FP64
+ * engine) on caller-owned device arrays and allocates nothing: no cudaMalloc, cudaFree or
+ * allocating library call.
+ *   w       box, dt, seed, t, bead types, interaction matrices (host pointers) and n_beads;
+ *           its bead-array pointers are ignored.  Step k draws the random numbers of time
+ *           w->t + k; the caller advances its own t by n_steps afterwards.
+ *   d_x, d_v, d_f  device arrays, 3 doubles per bead in bead-id order, read and updated
+ *           in place (x(t), v(t), f(t) in; x(t+n), v(t+n), f(t+n) out).
+ *   d_hash  device array of the beads' BeadHash values.
+ *   stream  a cudaStream_t (NULL: the legacy default stream); the call returns after the
+ *           stream has finished the steps.
+ * Limits: at most PDPD_NOALLOC_MAX_BEADS beads and PDPD_NOALLOC_MAX_CELLS cells; worlds with
+ * Hookean or angle bonds are rejected (PDPD_E_UNSUPPORTED); larger worlds get PDPD_E_NOMEM.
+ * Scratch memory is one fixed array inside the library (about 1.3 MB), held on every GPU that
+ * loads the library until the process exits.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture begins.  Every call reuses the same array: calls that overlap on the GPU (on
+ * different streams or from different threads) race on it. */
+#define PDPD_NOALLOC_MAX_BEADS 65536
+#define PDPD_NOALLOC_MAX_CELLS 32768
+int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, double *d_f,
+                      const uint32_t *d_hash, uint32_t n_steps, void *stream);
+
 /* Number of kernel launches the engine has issued since creation (graph replays count
  * each kernel node).  For accounting in benchmarks. */
 uint64_t pdpd_kernel_launches(pdpd_engine *e);

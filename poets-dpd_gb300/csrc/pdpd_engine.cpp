@@ -25,6 +25,15 @@ namespace {
 
 thread_local std::string g_last_error = "";
 
+}  // namespace
+
+void pdpd::set_thread_error(const char *msg)
+{
+    g_last_error = msg ? msg : "";
+}
+
+namespace {
+
 double now_s()
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

@@ -10,7 +10,10 @@
 // State per bead (sorted): pos = (x, y, z, hash as the low bits of w), vel = (v, 0),
 // frc = (f, 0).
 #include <cmath>
+#include <cstring>
+#include <mutex>
 
+#include "../../include/pdpd_gpu.h"
 #include "pdpd_device.cuh"
 
 namespace pdpd {
@@ -473,3 +476,306 @@ int launch_unsort64(const KArgs &a, cudaStream_t s)
 }
 
 }  // namespace pdpd
+
+// =======================================================================================
+// Allocation-free stepping (pdpd_step_noalloc).
+//
+// Some callers cannot allocate device memory: code running while a CUDA stream is being
+// captured into a graph (cudaMalloc is not a capturable operation), or a host framework
+// that owns every device allocation through its own pool and forbids side allocations.
+// For them, pdpd_step_noalloc advances one small bond-free world with the FP64 integrator
+// on device arrays the caller owns, and keeps its own scratch -- the cell counts, cell
+// starts, arrival ranks and the canonical bead order of the counting sort -- in the
+// file-scope array g_noalloc_scratch below instead of allocating it.  Every GPU that loads
+// the library holds this array (about 1.3 MB) until the process exits.  All calls share
+// it: calls that overlap on the GPU (on different streams, or from different host threads
+// without ordering) race on it and corrupt each other's cell lists.
+//
+// The arithmetic is the engine's FP64 path: update_pos, counting sort with beads in id
+// order inside each cell, pair forces in the reference's direction order, update_mom,
+// compiled without fused multiply-add -- so the result equals pdpd_run's bit for bit.
+// =======================================================================================
+
+namespace pdpd {
+namespace {
+
+constexpr uint32_t NA_MAX_BEADS = 65536;
+constexpr uint32_t NA_MAX_CELLS = 32768;
+
+struct NaScratch {
+    uint32_t err;
+    uint32_t cnt[NA_MAX_CELLS];
+    uint32_t start[NA_MAX_CELLS + 1];
+    uint2 keyrank[NA_MAX_BEADS];
+    uint32_t tmp[NA_MAX_BEADS];
+    uint32_t order[NA_MAX_BEADS];
+};
+
+struct NaParams {
+    int32_t L[3];
+    uint32_t n;
+    uint32_t n_cells;
+    uint32_t nt;
+    double dt;
+    double scale_inv_sqrt_dt;
+    uint64_t seed;
+    int64_t t;
+    double pair[256][2];  // a_ij, sqrt(gamma_ij)
+};
+
+}  // namespace
+}  // namespace pdpd
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(pdpd::NaScratch)];
+
+namespace pdpd {
+namespace {
+
+__global__ void k_na_clear(NaScratch *S, uint32_t n_cells)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_cells) S->cnt[i] = 0u;
+    if (i == 0) S->err = 0u;
+}
+
+// update_pos (dpd_maths_core_half_step.hpp:22-49) and the bead's new cell and arrival rank.
+__global__ void k_na_update_pos(NaParams p, NaScratch *S, double *x, double *v, double *f)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const double dt = p.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+        const double L = (double)p.L[d];
+        double xn = x[3 * i + d] + v[3 * i + d] * dt + f[3 * i + d] * hdt2;
+        if (xn < 0) {
+            xn += L;
+            if (xn == L) xn = 0;
+        } else if (xn >= L) {
+            xn -= L;
+        }
+        if (!(xn >= 0.0 && xn < L)) {
+            atomicOr(&S->err, (uint32_t)ERR_OUT_OF_BOX);
+            xn = 0.0;
+        }
+        x[3 * i + d] = xn;
+        c[d] = (int)floor(xn);
+        v[3 * i + d] = v[3 * i + d] + f[3 * i + d] * hdt;
+        f[3 * i + d] = 0.0;
+    }
+    const uint32_t key = ((uint32_t)c[0] * (uint32_t)p.L[1] + (uint32_t)c[1]) * (uint32_t)p.L[2] + (uint32_t)c[2];
+    const uint32_t rank = atomicAdd(&S->cnt[key], 1u);
+    S->keyrank[i] = make_uint2(key, rank);
+}
+
+// Exclusive scan of the cell counts in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_na_scan(NaScratch *S, uint32_t n_cells, uint32_t n)
+{
+    __shared__ uint32_t wsum[32];
+    const uint32_t per = (n_cells + 1023) / 1024;
+    const uint32_t b = threadIdx.x * per, e = min(n_cells, b + per);
+    uint32_t tsum = 0;
+    for (uint32_t k = b; k < e; k++) tsum += S->cnt[k];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = tsum;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += y;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    uint32_t run = inc - tsum;
+    for (int k = 0; k < warp; k++) run += wsum[k];
+    for (uint32_t k = b; k < e; k++) {
+        S->start[k] = run;
+        run += S->cnt[k];
+    }
+    if (threadIdx.x == 0) S->start[n_cells] = n;
+}
+
+__global__ void k_na_place(NaScratch *S, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 kr = S->keyrank[i];
+    S->tmp[S->start[kr.x] + kr.y] = i;
+}
+
+// Canonical cell order: beads of a cell in ascending id, as the reference's cell lists.
+__global__ void k_na_canon(NaScratch *S, uint32_t n)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const uint32_t i = S->tmp[d];
+    const uint32_t key = S->keyrank[i].x;
+    const uint32_t b = S->start[key], e = S->start[key + 1];
+    uint32_t rank = 0;
+    for (uint32_t k = b; k < e; k++) rank += S->tmp[k] < i ? 1u : 0u;
+    S->order[b + rank] = i;
+}
+
+// Pair forces (update_cell_forces + calc_force, naive_dpd_engine_half_step.hpp:300-424 and
+// dpd_maths_core_half_step.hpp:69-157), the same operations in the same order as
+// pair_forces64 / list_forces64.
+__global__ void k_na_forces(NaParams p, NaScratch *S, const double *__restrict__ x,
+                            const double *__restrict__ v, double *__restrict__ f,
+                            const uint32_t *__restrict__ hash)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const uint64_t th = t_hash((uint32_t)p.t, p.seed);
+    const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+    const uint32_t key = S->keyrank[i].x;
+    const int c[3] = {(int)(key / ((uint32_t)p.L[1] * (uint32_t)p.L[2])),
+                      (int)((key / (uint32_t)p.L[2]) % (uint32_t)p.L[1]), (int)(key % (uint32_t)p.L[2])};
+    const double xh[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+    const double vh[3] = {v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+    const uint32_t hh = hash[i];
+    const uint32_t ti = min(hh >> 28, p.nt - 1u);
+    const double min2 = (double)min_dist_sqr_f();
+    double F[3] = {0.0, 0.0, 0.0};
+    int dir[3];
+    for (dir[0] = -1; dir[0] <= 1; dir[0]++)
+        for (dir[1] = -1; dir[1] <= 1; dir[1]++)
+            for (dir[2] = -1; dir[2] <= 1; dir[2]++) {
+                int op[3];
+                double delta[3];
+                for (int k = 0; k < 3; k++) {
+                    const int raw = c[k] + dir[k];
+                    const int is_left = raw < 0;
+                    const int is_right = raw == p.L[k];
+                    op[k] = raw + (is_left - is_right) * p.L[k];
+                    delta[k] = (double)(is_right - is_left) * (double)p.L[k];
+                }
+                const uint32_t nc = ((uint32_t)op[0] * (uint32_t)p.L[1] + (uint32_t)op[1]) * (uint32_t)p.L[2] + (uint32_t)op[2];
+                const uint32_t k1 = S->start[nc + 1];
+                for (uint32_t k = S->start[nc]; k < k1; k++) {
+                    const uint32_t j = S->order[k];
+                    const double obx = x[3 * j] + delta[0], oby = x[3 * j + 1] + delta[1], obz = x[3 * j + 2] + delta[2];
+                    const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
+                    const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+                    if (dr2 >= 1 || dr2 < min2) continue;
+                    const double dr = sqrt(dr2);
+                    const uint32_t hj = hash[j];
+                    const uint32_t tj = min(hj >> 28, p.nt - 1u);
+                    const double con_strength = p.pair[ti * p.nt + tj][0];
+                    const double sqrt_diss = p.pair[ti * p.nt + tj][1];
+                    const double kappa = 0.0, r0 = 0.5;
+                    const double inv_dr = 1.0 / dr;
+                    const double dv0 = vh[0] - v[3 * j], dv1 = vh[1] - v[3 * j + 1], dv2 = vh[2] - v[3 * j + 2];
+                    const double wr = 1.0 - dr;
+                    const double con_force = con_strength * wr;
+                    const double e0 = dx0 * inv_dr, e1 = dx1 * inv_dr, e2 = dx2 * inv_dr;
+                    const double rdotv = e0 * dv0 + e1 * dv1 + e2 * dv2;
+                    const double sqrt_gammap = sqrt_diss * wr;
+                    const double diss_force = -sqrt_gammap * sqrt_gammap * rdotv;
+                    const double u = (double)hash_u(th_lo, th_hi, hh, hj);
+                    const double rand_scale = sqrt_gammap * p.scale_inv_sqrt_dt;
+                    const double rand_force = rand_scale * u;
+                    const double dr0 = r0 - dr;
+                    const double hookean_force = kappa * dr0;
+                    const double scaled = con_force + diss_force + rand_force + hookean_force;
+                    F[0] = F[0] + e0 * scaled;
+                    F[1] = F[1] + e1 * scaled;
+                    F[2] = F[2] + e2 * scaled;
+                }
+            }
+    f[3 * i] = F[0];
+    f[3 * i + 1] = F[1];
+    f[3 * i + 2] = F[2];
+}
+
+// update_mom (dpd_maths_core_half_step.hpp:51-61).
+__global__ void k_na_update_mom(NaParams p, double *v, const double *f)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const double hdt = p.dt * 0.5;
+    for (int d = 0; d < 3; d++) v[3 * i + d] = v[3 * i + d] + f[3 * i + d] * hdt;
+}
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+void *g_na_scratch[NA_MAX_DEVICES];
+
+}  // namespace
+}  // namespace pdpd
+
+extern "C" int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, double *d_f,
+                                 const uint32_t *d_hash, uint32_t n_steps, void *stream)
+{
+    using namespace pdpd;
+    auto fail = [](int code, const char *msg) {
+        set_thread_error(msg);
+        return code;
+    };
+    if (!w) return fail(PDPD_E_INVALID, "pdpd_step_noalloc: no world");
+    if (w->n_bonds || w->n_angles)
+        return fail(PDPD_E_UNSUPPORTED, "pdpd_step_noalloc: worlds with bonds are not supported");
+    if (w->n_bead_types == 0 || w->n_bead_types > 16 || !w->conservative || !w->dissipative)
+        return fail(PDPD_E_INVALID, "pdpd_step_noalloc: 1..16 bead types with interaction matrices required");
+    if (w->stationary)
+        for (uint32_t k = 0; k < w->n_bead_types; k++)
+            if (w->stationary[k]) return fail(PDPD_E_UNSUPPORTED, "Engine does not support stationary bead types.");
+    if (!(w->dt > 0 && w->dt < 1)) return fail(PDPD_E_INVALID, "pdpd_step_noalloc: dt must be in (0, 1)");
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; k++) {
+        if (w->box[k] < 2) return fail(PDPD_E_INVALID, "Distance in each direction must be at least 2");
+        cells *= (uint64_t)w->box[k];
+    }
+    if (w->n_beads > NA_MAX_BEADS || cells > NA_MAX_CELLS)
+        return fail(PDPD_E_NOMEM, "pdpd_step_noalloc: at most 65536 beads and 32768 cells (the fixed scratch size)");
+    if (n_steps == 0 || w->n_beads == 0) return PDPD_OK;
+    if (!d_x || !d_v || !d_f || !d_hash) return fail(PDPD_E_INVALID, "pdpd_step_noalloc: missing device array");
+
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
+        return fail(PDPD_E_CUDA, "pdpd_step_noalloc: no current CUDA device");
+    void *scratch = nullptr;
+    {
+        // First call on a device: look up the device address of the scratch array.
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na_scratch[dev]) {
+            ce = cudaGetSymbolAddress(&g_na_scratch[dev], g_noalloc_scratch);
+            if (ce != cudaSuccess) {
+                g_na_scratch[dev] = nullptr;
+                return fail(PDPD_E_CUDA, "pdpd_step_noalloc: cudaGetSymbolAddress failed");
+            }
+        }
+        scratch = g_na_scratch[dev];
+    }
+    NaScratch *S = (NaScratch *)scratch;
+    cudaStream_t s = (cudaStream_t)stream;
+    NaParams p;
+    memset(&p, 0, sizeof p);
+    for (int k = 0; k < 3; k++) p.L[k] = w->box[k];
+    p.n = w->n_beads;
+    p.n_cells = (uint32_t)cells;
+    p.nt = w->n_bead_types;
+    p.dt = w->dt;
+    p.scale_inv_sqrt_dt = sqrt(24 * 1.0 / w->dt);
+    p.seed = w->seed;
+    for (uint32_t k = 0; k < p.nt * p.nt; k++) {
+        p.pair[k][0] = w->conservative[k];
+        p.pair[k][1] = sqrt(w->dissipative[k]);
+    }
+    const uint32_t gb = (p.n + 255) / 256, gc = (p.n_cells + 255) / 256;
+    for (uint32_t step = 0; step < n_steps; step++) {
+        p.t = w->t + (int64_t)step;
+        k_na_clear<<<gc, 256, 0, s>>>(S, p.n_cells);
+        k_na_update_pos<<<gb, 256, 0, s>>>(p, S, d_x, d_v, d_f);
+        k_na_scan<<<1, 1024, 0, s>>>(S, p.n_cells, p.n);
+        k_na_place<<<gb, 256, 0, s>>>(S, p.n);
+        k_na_canon<<<gb, 256, 0, s>>>(S, p.n);
+        k_na_forces<<<gb, 256, 0, s>>>(p, S, d_x, d_v, d_f, d_hash);
+        k_na_update_mom<<<gb, 256, 0, s>>>(p, d_v, d_f);
+    }
+    uint32_t err = 0;
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&err, &S->err, sizeof err, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return fail(PDPD_E_CUDA, cudaGetErrorString(ce));
+    if (err) return fail(PDPD_E_BEAD_LOST, "pdpd_step_noalloc: a bead left the box or became non-finite");
+    return PDPD_OK;
+}

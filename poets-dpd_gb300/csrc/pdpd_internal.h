@@ -142,4 +142,7 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
                 uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
 
+// Message returned by pdpd_last_error(NULL) on this thread.
+void set_thread_error(const char *msg);
+
 }  // namespace pdpd

@@ -37,7 +37,7 @@ EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support"
             "pdpd_max_bond_length", "pdpd_attach", "pdpd_attach_batch", "pdpd_run",
             "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
-            "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run"]
+            "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc"]
 
 
 class PdpdWorld(C.Structure):
@@ -99,6 +99,7 @@ def lib():
         "pdpd_kernel_launches": (C.c_uint64, [vp]),
         "pdpd_rng_eval": (i32, [C.c_size_t, vp, vp, vp, vp, vp, vp]),
         "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
+        "pdpd_step_noalloc": (i32, [C.POINTER(PdpdWorld), vp, vp, vp, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -165,6 +166,19 @@ def rng_eval(t, seed, a, b):
     if rc != 0:
         raise RuntimeError(f"pdpd_rng_eval: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
     return h, u
+
+
+def step_noalloc(world, d_x, d_v, d_f, d_hash, n_steps, t=None, stream=None):
+    """``pdpd_step_noalloc``: advance a bond-free world by n_steps (FP64) on device arrays
+    the caller owns (integer device addresses: x, v, f with 3 doubles per bead, hash with one
+    uint32 per bead), without the library allocating any memory.  ``t`` is the time of the
+    state in the arrays (default ``world.t``)."""
+    fl = _Flat(world)
+    if t is not None:
+        fl.struct.t = int(t)
+    rc = lib().pdpd_step_noalloc(C.byref(fl.struct), d_x, d_v, d_f, d_hash, int(n_steps), stream)
+    if rc != 0:
+        raise RuntimeError(f"pdpd_step_noalloc: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
 
 
 class GB300DPDEngine:
