@@ -14,7 +14,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 def world_fixture_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not p.endswith("hash_kat.npz"))
+                  if not p.endswith(("hash_kat.npz", "testbase_suite.npz")))
 
 
 def load_world_fixture(name):
@@ -42,3 +42,32 @@ def force_rel_err(f, f_ref):
     scale = np.sqrt(np.mean(np.sum(f_ref * f_ref, axis=1)))
     scale = max(scale, 1e-300)
     return float(np.max(np.linalg.norm(f - f_ref, axis=1)) / scale)
+
+
+def load_testbase():
+    """The reference's TestBase suite as replayable segments (tests/golden/testbase_suite.npz):
+    a list of (name, world, [(todo, t_in, state_in (n,9), t_out, state_out (n,9)), ...]) where a
+    state row is x, v, f of one bead."""
+    d = np.load(os.path.join(GOLDEN, "testbase_suite.npz"))
+    cases = []
+    names = d["names"]
+    segs_of = {}
+    for s, k in enumerate(d["seg_test"]):
+        segs_of.setdefault(int(k), []).append(s)
+    bo, wo = d["bead_off"], d["world_off"]
+    for k, name in enumerate(names):
+        world = W.read_pdw1(d["worlds"][wo[k]:wo[k + 1]].tobytes())
+        segs = []
+        for s in segs_of.get(k, []):
+            segs.append((int(d["todo"][s]), int(d["t_in"][s]), d["state_in"][bo[s]:bo[s + 1]],
+                         int(d["t_out"][s]), d["state_out"][bo[s]:bo[s + 1]]))
+        cases.append((str(name), world, segs))
+    return cases
+
+
+def world_at(world, t, state):
+    """Copy of world with time t and bead state rows (x, v, f)."""
+    w = world.copy()
+    w.t = t
+    w.x, w.v, w.f = state[:, 0:3].copy(), state[:, 3:6].copy(), state[:, 6:9].copy()
+    return w

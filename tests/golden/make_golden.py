@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import io
 import os
+import struct
 import subprocess
 import sys
 
@@ -142,10 +143,81 @@ def hash_fixture():
     print(f"hash_kat: {t.size} records")
 
 
+def testbase_fixture(max_segments=4, keep_every_multiple=1):
+    """The reference's own engine test suite (225 TestBase cases, test_engine.cpp:62-69),
+    driven with the reference's NaiveDPDEngineHalfStep by oracle/ref/testbase_export.cpp.
+    Up to max_segments segments per case (the first, the last, evenly spaced ones between);
+    keep_every_multiple > 1 thins the 121 TestMultipleMovingBeads cases."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "testbase_export")
+    tmp = os.path.join(HERE, "_tb.bin")
+    subprocess.run([exe, tmp, str(max_segments)], check=True)
+    data = open(tmp, "rb").read()
+    os.remove(tmp)
+    p = 0
+    (n,) = struct.unpack_from("<I", data, p)
+    p += 4
+    names, verdicts, worlds, seg_test, todos, t_in, t_out, s_in, s_out = ([] for _ in range(9))
+    multiple_seen = 0
+    for _ in range(n):
+        (ln,) = struct.unpack_from("<I", data, p)
+        p += 4
+        name = data[p:p + ln].decode()
+        p += ln
+        (ok,) = struct.unpack_from("<I", data, p)
+        p += 4
+        (wl,) = struct.unpack_from("<I", data, p)
+        p += 4
+        wbytes = data[p:p + wl]
+        p += wl
+        nb = W.read_pdw1(wbytes).n_beads
+        (ns,) = struct.unpack_from("<I", data, p)
+        p += 4
+        keep = True
+        if name.startswith("TestMultipleMovingBeads"):
+            keep = multiple_seen % keep_every_multiple == 0
+            multiple_seen += 1
+        segs = []
+        for _ in range(ns):
+            (todo,) = struct.unpack_from("<I", data, p)
+            p += 4
+            (ti,) = struct.unpack_from("<q", data, p)
+            p += 8
+            xin = np.frombuffer(data, "<f8", 9 * nb, p).reshape(nb, 9)
+            p += 72 * nb
+            (to,) = struct.unpack_from("<q", data, p)
+            p += 8
+            xout = np.frombuffer(data, "<f8", 9 * nb, p).reshape(nb, 9)
+            p += 72 * nb
+            segs.append((todo, ti, xin, to, xout))
+        if not keep:
+            continue
+        k = len(names)
+        names.append(name)
+        verdicts.append(ok)
+        worlds.append(np.frombuffer(wbytes, np.uint8))
+        for todo, ti, xin, to, xout in segs:
+            seg_test.append(k)
+            todos.append(todo)
+            t_in.append(ti)
+            t_out.append(to)
+            s_in.append(xin)
+            s_out.append(xout)
+    world_off = np.cumsum([0] + [w.size for w in worlds])
+    bead_off = np.cumsum([0] + [x.shape[0] for x in s_in])
+    np.savez_compressed(os.path.join(HERE, "testbase_suite.npz"),
+                        names=np.array(names), verdicts=np.array(verdicts, np.uint8),
+                        worlds=np.concatenate(worlds), world_off=world_off,
+                        seg_test=np.array(seg_test), todo=np.array(todos), t_in=np.array(t_in),
+                        t_out=np.array(t_out), bead_off=bead_off,
+                        state_in=np.concatenate(s_in), state_out=np.concatenate(s_out))
+    print(f"testbase_suite: {len(names)} of {n} cases, {len(todos)} segments")
+
+
 def main():
     if not os.path.exists(HARNESS):
         raise SystemExit("build the reference harness first: make -C oracle/ref")
     hash_fixture()
+    testbase_fixture()
     save_world_fixture("water8_seed1", W.make_water(8, seed=1), [1, 10, 100],
                        "8^3 water, density 3 (1536 beads), a=25, gamma=4.5, dt=0.02, seed=1")
     save_world_fixture("polymer10_seed2", W.make_polymer_box(10, chain_fraction=0.1, seed=2),

@@ -372,3 +372,33 @@ def test_full_size_momentum_and_determinism():
     p = res[0].v.sum(axis=0)
     assert np.max(np.abs(p)) / res[0].n_beads < 1e-5
     assert res[0].t == 20
+
+
+# ---------------------------------------------------------------------------- reference test suite
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_reference_testbase_suite_replay(prec):
+    """The reference's own 225-case engine test suite (TestBase families of test_engine.cpp),
+    replayed segment by segment from the reference engine's recorded input states: the FP64
+    engine reproduces every output bit for bit (so every property the suite checks on the
+    reference engine holds for it); the FP32 engine stays within the FP32 tolerances on the
+    short segments and finishes every segment."""
+    from _helpers import load_testbase, world_at
+    cases = load_testbase()
+    eng = E.GB300DPDEngine(prec)
+    checked = 0
+    for name, world, segs in cases:
+        for todo, t_in, s_in, t_out, s_out in segs:
+            w = world_at(world, t_in, s_in)
+            eng.Attach(w)
+            eng.Run(todo)
+            assert w.t == t_out, name
+            got = np.hstack([w.x, w.v, w.f])
+            if prec == "fp64":
+                assert np.array_equal(got, s_out), f"{name}: segment t={t_in}+{todo}"
+            else:
+                assert np.all(np.isfinite(got)), name
+                if todo == 1 and w.n_beads > 1:
+                    assert force_rel_err(w.f, s_out[:, 6:9]) <= FP32_FORCE_TOL, name
+            checked += 1
+    assert checked == 900

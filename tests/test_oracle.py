@@ -69,3 +69,20 @@ def test_observables_basic():
     # every unordered pair with r < 1 counted once: expected count ~ N * rho * (4/3 pi) / 2
     pairs = obs["rdf"].sum()
     assert 0.7 * n * 3 * 4.18879 / 2 < pairs < 1.3 * n * 3 * 4.18879 / 2
+
+
+def test_oracle_replays_reference_testbase_suite():
+    """All 225 cases of the reference's own engine test suite, segment by segment: from the
+    identical input state, the oracle reproduces the reference engine's output bit for bit."""
+    from _helpers import load_testbase, world_at
+    cases = load_testbase()
+    assert len(cases) == 225
+    n_seg = 0
+    for name, world, segs in cases:
+        for todo, t_in, s_in, t_out, s_out in segs:
+            ow = O.OracleWorld(world_at(world, t_in, s_in))
+            ow.run(todo)
+            assert ow.t == t_out, name
+            assert np.array_equal(np.hstack([ow.x, ow.v, ow.f]), s_out), name
+            n_seg += 1
+    assert n_seg == 900
