@@ -1,5 +1,5 @@
 // Test infrastructure: drives the reference's own engines, compiled unchanged from the
-// reference headers, on worlds stored in the PDW1 file format (see oracle/pdw1.md).
+// reference headers, on worlds stored in the PDW1 file format (pdw1_read.hpp).
 // Only the fixture generator (tests/golden/make_golden.py) runs this program, and only
 // in a container where the reference sources are present.
 //

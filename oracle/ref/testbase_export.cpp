@@ -47,7 +47,7 @@ struct Out {
     }
 };
 
-// PDW1 (oracle/pdw1.md): the same layout poets-dpd_gb300/pdpd_world.py writes.
+// PDW1: the same layout poets-dpd_gb300/pdpd_world.py writes and pdw1_read.hpp reads.
 void put_pdw1(Out &o, const WorldState &s)
 {
     o.bytes("PDW1", 4);

@@ -14,7 +14,7 @@ Also here:
   naive_dpd_engine_half_step.hpp:321-329).
 * generators for the synthetic worlds the engine is tested and measured on (water boxes,
   polymer-solvent boxes, batched grids), seeded, using numpy only.
-* the PDW1 binary world file format (oracle/pdw1.md) shared with the test harnesses.
+* the PDW1 binary world file format, shared with the C++ test harnesses under oracle/ref/.
 """
 
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """GPU parity: the engine, called through its C ABI, against the reference's outputs
 (tests/golden/, made by the reference's own FP64 engine) and against the oracle.
 
-Tolerances (stated here and in the design doc):
+Tolerances:
 * FP64 engine: bit-exact -- x, v, f identical to the reference / oracle after every
   checkpoint (same operation order, no fused multiply-add).
 * RNG and bead-to-cell assignment: bit-exact.
@@ -77,7 +77,7 @@ def test_fp64_bit_exact_vs_reference(name):
 
 @pytest.mark.parametrize("L,steps", [(32, 10)])
 def test_fp64_bit_exact_vs_oracle_polymer_box(L, steps):
-    """Config-2 sized polymer box (98,304 beads, 10% H-T5 chains), FP64 engine vs oracle."""
+    """32^3 polymer box (98,304 beads, 10% H-T5 chains), FP64 engine vs oracle."""
     world = W.make_polymer_box(L, chain_fraction=0.1, seed=2)
     ow = O.OracleWorld(world)
     eng = E.GB300DPDEngine("fp64")
