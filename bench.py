@@ -141,6 +141,61 @@ def oracle_rate(world, max_seconds=12.0, max_steps=200, threads=None):
     return world.n_beads * steps / dt, threads, steps, dt
 
 
+def batched_grid_metrics(steps=200, plain_steps=10, n_states=512, device=0):
+    """512 independent polymer-solvent states, cube side uniform on 8..32, per-state
+    a_WT ~ U[25,100] and gamma ~ U[3,6], 5% chains, dt = 0.01, seeds = index + 1.
+
+    FP32 batched: all states attached to one engine (one arena, one brick work queue over all
+    states, each step one CUDA-graph replay), autotuned, `steps` steps timed with CUDA events.
+    FP64 plain: the FP64 engine run one state at a time (Attach excluded from the time, as the
+    reference's bpsExec), `plain_steps` steps per state, CUDA events around each Run."""
+    import torch
+
+    import pdpd_engine as E
+
+    worlds = W.make_batched_grid(n_states)
+    total = sum(w.n_beads for w in worlds)
+    dev = torch.device("cuda", device)
+    eng = E.GB300DPDEngine("fp32", device=device)
+    eng.SetConfigEntry("autotune", 1)
+    eng.AttachBatch([w.copy() for w in worlds])
+    eng.run_async(40)  # the autotuner's trials are the first of these steps
+    eng.sync()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    eng.run_async(steps)
+    ev1.record(stream)
+    eng.sync()
+    torch.cuda.synchronize()
+    batched = total * steps / (ev0.elapsed_time(ev1) / 1e3)
+    tuned = {n: v for n, _, v in eng.GetConfigEntries()}
+    eng.close()
+
+    e64 = E.GB300DPDEngine("fp64", device=device)
+    s64 = torch.cuda.ExternalStream(e64.stream(), device=dev)
+    ms_total = 0.0
+    for w in worlds:
+        e64.Attach(w.copy())
+        e64.run_async(2)
+        e64.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s64)
+        e64.run_async(plain_steps)
+        b.record(s64)
+        e64.sync()
+        torch.cuda.synchronize()
+        ms_total += a.elapsed_time(b)
+    plain = total * plain_steps / (ms_total / 1e3)
+    e64.close()
+    return {"workload": f"{n_states} states, sides 8..32, {total} beads, 5% H-T5 chains",
+            "beads": total, "fp32_batched": batched, "fp64_plain_state_by_state": plain,
+            "ratio": batched / plain, "steps": steps, "plain_steps_per_state": plain_steps,
+            "autotuned": {k: tuned[k] for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
+                                                "autotune")}}
+
+
 def dist_setup(n_gpus):
     rank, world_size = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
     if world_size > 1:
@@ -198,6 +253,18 @@ def run_engine_arm(args):
     world = make_world(args.workload, side=args.side)
     n = world.n_beads
     eng = E.GB300DPDEngine(args.precision, device=local)
+
+    # --- autotune once (its trials are ordinary steps: the trajectory does not depend on the
+    # choice), then fix the chosen kernel and brick shape for every measurement below
+    if args.precision == "fp32":
+        eng.SetConfigEntry("autotune", 1)
+        eng.Attach(world.copy())
+        eng.run_async(64)
+        eng.sync()
+        tuned = {k: v for k, _, v in eng.GetConfigEntries()}
+        eng.SetConfigEntry("autotune", 0)
+    else:
+        tuned = {k: v for k, _, v in eng.GetConfigEntries()}
 
     # --- e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
     w_e2e = world.copy()
@@ -259,6 +326,9 @@ def run_engine_arm(args):
         if key in tj:
             traffic = tj[key] * n
 
+    batched = None
+    if not args.no_batched and world_size == 1:
+        batched = batched_grid_metrics(device=local)
     if rank != 0:
         return
     cpu = None
@@ -291,6 +361,9 @@ def run_engine_arm(args):
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "cpu_baseline": cpu,
+        "batched_grid": batched,
+        "kernel_config": {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
+                                                    "autotune")},
     }
     print(json.dumps(line), flush=True)
 
@@ -306,6 +379,8 @@ def main():
     ap.add_argument("--ref-side", type=int, default=32,
                     help="box side of the bounded CPU sample (same recipe)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 512-state batched grid (FP32 batched vs FP64 plain)")
     ap.add_argument("--side", type=int, default=None,
                     help="override the box side of the workload (profiling on smaller boxes)")
     args = ap.parse_args()

@@ -106,6 +106,8 @@ const ConfigEntry kConfig[] = {
     {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
+    {"autotune", "FP32: time the force-kernel variants and brick shapes on the first steps of "
+                 "the next run and keep the fastest (results do not depend on the choice)."},
 };
 
 }  // namespace
@@ -127,6 +129,10 @@ struct pdpd_engine {
     int cfg_use_graphs = 1;
     int cfg_force_kernel = 0;
     int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
+    int cfg_autotune = 0;
+    bool tuned = false;
+    std::string tune_log;
+    double max_density = 0;
 
     // attached worlds
     bool attached = false;
@@ -183,6 +189,7 @@ struct pdpd_engine {
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
+        tuned = false;
         n_beads = n_cells = n_tiles = 0;
     }
 
@@ -261,6 +268,111 @@ struct pdpd_engine {
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
         return PDPD_OK;
+    }
+
+    // Build the brick work queue of the FP32 force kernel for the current brick shape: every
+    // world cut into bx x by x bz bricks (edge bricks cut at the box faces), uploaded, and
+    // the kernel's shared-memory budget and persistent grid set up.
+    int configure_bricks()
+    {
+        KArgs &a = args;
+        a.force_kernel = cfg_force_kernel;
+        a.bricks = nullptr;
+        a.n_bricks = 0;
+        if (fp64() || cfg_force_kernel == 1) return PDPD_OK;
+        std::vector<Brick> bricks;
+        for (uint32_t i = 0; i < worlds.size(); i++) {
+            const int32_t *L = worlds[i].dev.L;
+            for (int x0 = 0; x0 < L[0]; x0 += cfg_brick[0])
+                for (int y0 = 0; y0 < L[1]; y0 += cfg_brick[1])
+                    for (int z0 = 0; z0 < L[2]; z0 += cfg_brick[2])
+                        bricks.push_back({i, x0, y0, z0, std::min(cfg_brick[0], L[0] - x0),
+                                          std::min(cfg_brick[1], L[1] - y0),
+                                          std::min(cfg_brick[2], L[2] - z0), 0});
+        }
+        size_t bytes_needed = sizeof(Brick) * std::max<size_t>(1, bricks.size());
+        if (d_bricks.bytes < bytes_needed) {
+            cudaStreamSynchronize(stream);
+            cudaError_t ce = d_bricks.alloc(bytes_needed);
+            if (ce != cudaSuccess) return fail(PDPD_E_NOMEM, "brick table allocation failed");
+        }
+        cudaError_t ce = cudaMemcpyAsync(d_bricks.p, bricks.data(), sizeof(Brick) * bricks.size(),
+                                         cudaMemcpyHostToDevice, stream);
+        if (ce != cudaSuccess) return cuda_fail(ce, "brick table upload");
+        a.bricks = d_bricks.as<Brick>();
+        a.n_bricks = (uint32_t)bricks.size();
+        // Staged-bead capacity: 1.5x the expected halo population of the densest world (at
+        // most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
+        a.brick_hc_max = (uint32_t)(cfg_brick[0] + 2) * (cfg_brick[1] + 2) * (cfg_brick[2] + 2);
+        double want = 1.5 * max_density * a.brick_hc_max + 64;
+        a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
+        int grid = 0;
+        uint32_t bytes = 0;
+        int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, &grid, &bytes);
+        if (rc)
+            return fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
+                        cudaGetErrorString((cudaError_t)rc));
+        a.brick_grid = cfg_grid_blocks > 0 ? cfg_grid_blocks : grid;
+        drop_graph();
+        return PDPD_OK;
+    }
+
+    // Autotuner: pick the fastest FP32 force-kernel variant and brick shape for the attached
+    // worlds by timing a few steps of each candidate on the engine's stream.  The candidates
+    // add the same pair terms in the same order with the same roundings, so the trajectory
+    // does not depend on which one runs: the trial steps are ordinary steps of the run.
+    // Returns the number of steps consumed.
+    uint32_t autotune(uint32_t n_steps)
+    {
+        static const int cand[][4] = {{0, 4, 4, 4}, {0, 2, 4, 8}, {0, 4, 4, 8}, {0, 2, 2, 8},
+                                      {2, 4, 4, 4}, {3, 4, 4, 4}, {4, 2, 4, 8}, {1, 4, 4, 4}};
+        const int n_cand = (int)(sizeof cand / sizeof cand[0]);
+        const uint32_t trial = 3;
+        if (!cfg_autotune || tuned || fp64() || n_steps < (trial + 1) * n_cand + 1) return 0;
+        const int keep[4] = {cfg_force_kernel, cfg_brick[0], cfg_brick[1], cfg_brick[2]};
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 1e30f;
+        int best_i = -1;
+        uint32_t used = 0;
+        tune_log.clear();
+        for (int i = 0; i < n_cand; i++) {
+            cfg_force_kernel = cand[i][0];
+            cfg_brick[0] = cand[i][1];
+            cfg_brick[1] = cand[i][2];
+            cfg_brick[2] = cand[i][3];
+            if (configure_bricks() != PDPD_OK) continue;
+            // one warm step, then the timed trial (steps launched one by one, no graph)
+            launches += enqueue_begin(stream);
+            for (uint32_t k = 0; k + 1 < trial; k++) launches += enqueue_step(stream);
+            cudaEventRecord(e0, stream);
+            launches += enqueue_step(stream);
+            cudaEventRecord(e1, stream);
+            launches += enqueue_final(stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            used += trial + 1;  // begin .. final completes trial + 1 timesteps
+            char line[96];
+            snprintf(line, sizeof line, "%d:%dx%dx%d=%.3fms ", cand[i][0], cand[i][1], cand[i][2],
+                     cand[i][3], ms);
+            tune_log += line;
+            if (ms < best) {
+                best = ms;
+                best_i = i;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const int *pick = best_i >= 0 ? cand[best_i] : keep;
+        cfg_force_kernel = pick[0];
+        cfg_brick[0] = pick[1];
+        cfg_brick[1] = pick[2];
+        cfg_brick[2] = pick[3];
+        configure_bricks();
+        tuned = true;
+        return used;
     }
 
     int check_device_errors()
@@ -455,7 +567,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
 
     // --- world table, tiles, pair table
     std::vector<Tile> tiles;
-    std::vector<Brick> bricks;
     double max_density = 0;
     std::vector<WorldDev> wdev(n_worlds);
     const bool f64 = e->fp64();
@@ -479,12 +590,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
         d.t = w.t;
         for (uint32_t b = 0; b < w.n_beads; b += TILE_BEADS)
             tiles.push_back({i, bead_base + b, bead_base + std::min<uint32_t>(w.n_beads, b + TILE_BEADS), 0});
-        for (int x0 = 0; x0 < w.box[0]; x0 += e->cfg_brick[0])
-            for (int y0 = 0; y0 < w.box[1]; y0 += e->cfg_brick[1])
-                for (int z0 = 0; z0 < w.box[2]; z0 += e->cfg_brick[2])
-                    bricks.push_back({i, x0, y0, z0, std::min(e->cfg_brick[0], w.box[0] - x0),
-                                      std::min(e->cfg_brick[1], w.box[1] - y0),
-                                      std::min(e->cfg_brick[2], w.box[2] - z0), 0});
         max_density = std::max(max_density, (double)w.n_beads / (double)d.n_cells);
         for (uint32_t k = 0; k < w.n_bead_types * w.n_bead_types; k++) {
             double a = w.conservative[k], sg = std::sqrt(w.dissipative[k]);
@@ -560,7 +665,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     };
     A(e->d_worlds, sizeof(WorldDev) * n_worlds);
     A(e->d_tiles, sizeof(Tile) * std::max<size_t>(1, tiles.size()));
-    A(e->d_bricks, sizeof(Brick) * std::max<size_t>(1, bricks.size()));
     A(e->d_start, sizeof(uint32_t) * ((size_t)nc + 1));
     A(e->d_cnt, sizeof(uint32_t) * (size_t)nc);
     A(e->d_blocksums, sizeof(uint32_t) * (scan_blocks((uint32_t)nc) + 1));
@@ -623,7 +727,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     };
     H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
     H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
-    H2D(e->d_bricks, bricks.data(), sizeof(Brick) * bricks.size());
     H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
     H2D(e->d_bond_terms, terms.data(), sizeof(BondTerm) * n_terms);
     if (f64) {
@@ -652,8 +755,6 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.worlds = e->d_worlds.as<WorldDev>();
     a.n_worlds = n_worlds;
     a.tiles = e->d_tiles.as<Tile>();
-    a.bricks = e->d_bricks.as<Brick>();
-    a.n_bricks = (uint32_t)bricks.size();
     a.n_tiles = e->n_tiles;
     a.n_beads = e->n_beads;
     a.n_cells = e->n_cells;
@@ -682,22 +783,15 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     a.block_threads = 128;
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;
     a.list_capacity = e->cfg_list_capacity;
-    a.force_kernel = e->cfg_force_kernel;
-    if (!f64 && a.force_kernel != 1) {
-        // Staged-bead capacity: 1.5x the expected halo population of the densest world (and
-        // at most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
-        a.brick_hc_max = (uint32_t)(e->cfg_brick[0] + 2) * (e->cfg_brick[1] + 2) * (e->cfg_brick[2] + 2);
-        double want = 1.5 * max_density * a.brick_hc_max + 64;
-        a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
-        int grid = 0;
-        uint32_t bytes = 0;
-        int rc = brick_setup(e->sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, &grid, &bytes);
+    e->max_density = max_density;
+    {
+        int rc = e->configure_bricks();
         if (rc) {
+            std::string m = e->err;
             e->release();
-            return e->fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
-                           cudaGetErrorString((cudaError_t)rc));
+            e->err = m;
+            return rc;
         }
-        a.brick_grid = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : grid;
     }
     a.grid_blocks = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)gb, e->n_tiles));
 
@@ -727,6 +821,7 @@ int pdpd_run_async(pdpd_engine *e, uint32_t n_steps)
     if (!e) return PDPD_E_INVALID;
     if (!e->attached) return e->fail(PDPD_E_STATE, "Run called with no world attached");
     cudaSetDevice(e->device);
+    n_steps -= e->autotune(n_steps);
     return e->enqueue_run(n_steps, e->stream);
 }
 
@@ -905,10 +1000,16 @@ int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len,
     if (!e) return PDPD_E_INVALID;
     if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
     int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs,
-                  e->cfg_force_kernel, e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2]};
+                  e->cfg_force_kernel, e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2],
+                  e->cfg_autotune};
     if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
     if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
-    if (value && value_len) snprintf(value, value_len, "%d", vals[index]);
+    if (value && value_len) {
+        if (std::string(kConfig[index].name) == "autotune" && e->tuned)
+            snprintf(value, value_len, "%d (trials %s)", vals[index], e->tune_log.c_str());
+        else
+            snprintf(value, value_len, "%d", vals[index]);
+    }
     return PDPD_OK;
 }
 
@@ -933,9 +1034,17 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
         if (v < 1 || v > 32 || nb[0] * nb[1] > 64 || (nb[0] + 2) * (nb[1] + 2) * (nb[2] + 2) > 2048)
             return e->fail(PDPD_E_INVALID, "brick shape %dx%dx%d out of range", nb[0], nb[1], nb[2]);
         e->cfg_brick[idx] = (int)v;
+    } else if (k == "autotune") {
+        e->cfg_autotune = v ? 1 : 0;
+        e->tuned = false;
     }
     else return e->fail(PDPD_E_INVALID, "Unknown engine config name '%s'", key);
-    e->drop_graph();  // layout-dependent settings take effect at the next attach / capture
+    e->drop_graph();  // graphs are captured again at the next run
+    if (e->attached && (k == "force_kernel" || k.rfind("brick_", 0) == 0 || k == "grid_blocks")) {
+        cudaSetDevice(e->device);
+        cudaStreamSynchronize(e->stream);
+        return e->configure_bricks();  // kernel choice and brick shape apply from the next step
+    }
     return PDPD_OK;
 }
 

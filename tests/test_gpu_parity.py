@@ -232,6 +232,28 @@ LAUNCH_CONFIGS = {
 }
 
 
+def test_autotune_and_mid_run_reconfiguration_keep_the_trajectory():
+    """The autotuner times kernel variants and brick shapes on the run's own steps, and the
+    kernel / brick shape can change between runs: none of it changes the FP32 trajectory."""
+    world = W.make_polymer_box(16, chain_fraction=0.1, seed=12)
+    ref = world.copy()
+    e1 = E.GB300DPDEngine("fp32")
+    e1.Attach(ref)
+    e1.Run(60)
+    w = world.copy()
+    e2 = E.GB300DPDEngine("fp32")
+    e2.SetConfigEntry("autotune", 1)
+    e2.Attach(w)
+    e2.Run(45)
+    cfg = {n: v for n, _, v in e2.GetConfigEntries()}
+    assert "trials" in cfg["autotune"]
+    e2.SetConfigEntry("force_kernel", 2)
+    e2.SetConfigEntry("brick_z", 8)
+    e2.Run(15)
+    assert w.t == ref.t == 60
+    assert np.array_equal(w.x, ref.x) and np.array_equal(w.v, ref.v) and np.array_equal(w.f, ref.f)
+
+
 def clustered_world():
     """8^3 box with half the beads packed into a 2x2x2-cell corner: the halo of a brick there
     holds far more beads than the shared-memory budget, so the brick kernel falls back to the
