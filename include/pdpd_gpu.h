@@ -157,6 +157,24 @@ typedef struct pdpd_phase_times {
  * pdpd_run's. */
 int pdpd_profile_run(pdpd_engine *e, uint32_t n_steps, pdpd_phase_times *out);
 
+/* Observables of attached world `world` at its current time, reduced on the GPU in FP64
+ * (no counterpart in the reference, which has no observables of its own; used to compare
+ * long runs with an FP64 oracle statistically):
+ *   ke2       sum of |v|^2 over beads (kinetic temperature kT = ke2 / (3 N), unit mass)
+ *   momentum  total momentum
+ *   virial    sum over bead pairs with r < 1 of r a_ij (1 - r) (conservative pair virial)
+ *             + sum over Hookean bonds of r kappa (r0 - r); pressure = (ke2 + virial) / (3 V)
+ * and, when the arrays are given, rdf[(ti * n_types + tj) * n_bins + b] (ti <= tj) = number
+ * of pairs of bead types ti, tj with r in [b, b+1) / n_bins, and bond_hist[b] = number of
+ * Hookean bonds with length in [2b, 2(b+1)) / n_bond_bins.  Deterministic. */
+typedef struct pdpd_observables {
+    double ke2;
+    double momentum[3];
+    double virial;
+} pdpd_observables;
+int pdpd_observe(pdpd_engine *e, uint32_t world, pdpd_observables *out, uint32_t n_bins,
+                 uint64_t *rdf, uint32_t n_bond_bins, uint64_t *bond_hist);
+
 /* Evaluate the engine's device RNG on n host-supplied records: for each i,
  * h_out[i] = hash_rng_sym(get_t_hash(t[i], seed[i]), a[i], b[i]) and
  * u_out[i] = default_hash(...) (reference include/dpd/core/hash.hpp:61-65,81-88 and

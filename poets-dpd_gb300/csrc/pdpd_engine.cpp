@@ -1048,6 +1048,59 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     return PDPD_OK;
 }
 
+}  // extern "C"
+
+namespace pdpd {
+struct ObsPartial {
+    double ke2, mx, my, mz, virial;
+};
+}  // namespace pdpd
+
+extern "C" {
+
+int pdpd_observe(pdpd_engine *e, uint32_t world, pdpd_observables *out, uint32_t n_bins,
+                 uint64_t *rdf, uint32_t n_bond_bins, uint64_t *bond_hist)
+{
+    if (!e || !out) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    cudaSetDevice(e->device);
+    const WorldDev &wd = e->worlds[world].dev;
+    const size_t n_rdf = rdf ? (size_t)wd.n_types * wd.n_types * n_bins : 0;
+    const size_t n_bh = bond_hist ? n_bond_bins : 0;
+    const uint32_t blocks = (wd.n_beads + 127) / 128;
+    DevBuf d_rdf, d_bh, d_part;
+    cudaError_t ce = d_rdf.alloc(8 * std::max<size_t>(1, n_rdf));
+    if (ce == cudaSuccess) ce = d_bh.alloc(8 * std::max<size_t>(1, n_bh));
+    if (ce == cudaSuccess) ce = d_part.alloc(sizeof(ObsPartial) * std::max<uint32_t>(1, blocks));
+    if (ce != cudaSuccess) return e->fail(PDPD_E_NOMEM, "observables: device allocation failed");
+    cudaStream_t s = e->stream;
+    cudaMemsetAsync(d_rdf.p, 0, d_rdf.bytes, s);
+    cudaMemsetAsync(d_bh.p, 0, d_bh.bytes, s);
+    e->launches += launch_observe(e->args, e->fp64(), world, wd.n_beads, n_bins,
+                                  n_rdf ? d_rdf.as<unsigned long long>() : nullptr, n_bond_bins,
+                                  n_bh ? d_bh.as<unsigned long long>() : nullptr,
+                                  d_part.as<ObsPartial>(), s);
+    std::vector<ObsPartial> part(blocks);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess && blocks)
+        ce = cudaMemcpyAsync(part.data(), d_part.p, sizeof(ObsPartial) * blocks, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess && n_rdf) ce = cudaMemcpyAsync(rdf, d_rdf.p, 8 * n_rdf, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess && n_bh) ce = cudaMemcpyAsync(bond_hist, d_bh.p, 8 * n_bh, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "observables");
+    pdpd_observables o{0, {0, 0, 0}, 0};
+    for (const ObsPartial &p : part) {  // block order: deterministic
+        o.ke2 += p.ke2;
+        o.momentum[0] += p.mx;
+        o.momentum[1] += p.my;
+        o.momentum[2] += p.mz;
+        o.virial += p.virial;
+    }
+    *out = o;
+    return PDPD_OK;
+}
+
 int pdpd_profile_run(pdpd_engine *e, uint32_t n_steps, pdpd_phase_times *out)
 {
     if (!e || !out) return PDPD_E_INVALID;

@@ -142,6 +142,12 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
                 uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
 
+// Observables of one world (pdpd_observe.cu): per-block FP64 partial sums.
+struct ObsPartial;
+int launch_observe(const KArgs &a, int fp64, uint32_t world, uint32_t n_beads, uint32_t n_bins,
+                   unsigned long long *rdf, uint32_t n_bond_bins, unsigned long long *bond_hist,
+                   ObsPartial *part, cudaStream_t s);
+
 // Message returned by pdpd_last_error(NULL) on this thread.
 void set_thread_error(const char *msg);
 

@@ -37,7 +37,8 @@ EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support"
             "pdpd_max_bond_length", "pdpd_attach", "pdpd_attach_batch", "pdpd_run",
             "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
-            "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc"]
+            "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc",
+            "pdpd_observe"]
 
 
 class PdpdWorld(C.Structure):
@@ -61,6 +62,10 @@ class PdpdTimings(C.Structure):
 class PdpdPhaseTimes(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("sort_ms", C.c_double), ("other_ms", C.c_double),
                 ("force_launches", C.c_uint32), ("sort_launches", C.c_uint32)]
+
+
+class PdpdObservables(C.Structure):
+    _fields_ = [("ke2", C.c_double), ("momentum", C.c_double * 3), ("virial", C.c_double)]
 
 
 INTERVAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)
@@ -100,6 +105,7 @@ def lib():
         "pdpd_rng_eval": (i32, [C.c_size_t, vp, vp, vp, vp, vp, vp]),
         "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
         "pdpd_step_noalloc": (i32, [C.POINTER(PdpdWorld), vp, vp, vp, vp, u32, vp]),
+        "pdpd_observe": (i32, [vp, u32, C.POINTER(PdpdObservables), u32, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -305,6 +311,19 @@ class GB300DPDEngine:
         pt = PdpdPhaseTimes()
         self._check(lib().pdpd_profile_run(self._h, int(n), C.byref(pt)), "profile_run")
         return {n_: getattr(pt, n_) for n_, _ in PdpdPhaseTimes._fields_}
+
+    def observe(self, world_index=0, n_bins=50, n_bond_bins=100):
+        """FP64 GPU reductions of the current state of one world: ke2 (sum |v|^2), momentum,
+        virial (conservative pairs + Hookean bonds), per-type-pair RDF counts over r in [0,1)
+        and the Hookean bond-length histogram over [0, 2)."""
+        nt = self._worlds[world_index].n_types
+        rdf = np.zeros(nt * nt * n_bins, np.uint64)
+        bh = np.zeros(n_bond_bins, np.uint64)
+        o = PdpdObservables()
+        self._check(lib().pdpd_observe(self._h, world_index, C.byref(o), n_bins, _p(rdf),
+                                       n_bond_bins, _p(bh)), "observe")
+        return {"ke2": o.ke2, "virial": o.virial, "momentum": np.array(o.momentum[:]),
+                "rdf": rdf.reshape(nt, nt, n_bins), "bond_hist": bh}
 
     def kernel_launches(self):
         return int(lib().pdpd_kernel_launches(self._h))
