@@ -196,6 +196,89 @@ def batched_grid_metrics(steps=200, plain_steps=10, n_states=512, device=0):
                                                 "autotune")}}
 
 
+def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed=5, device=0,
+                    seq_fp32=8, seq_fp64=4):
+    """Serving stream: Poisson arrivals at `rate` jobs/s for `window_s` seconds (seeded).  Each
+    job is pure DPD water (density 3, a = 25, gamma = 4.5, dt = 0.02) in a cube of side
+    log-uniform on [8, 64] (rounded), n_steps uniform on 100..2000, a host callback every
+    `interval` steps, `budget` bytes of admission budget.  A client thread submits each job at
+    its arrival time to the FP32 job server (continuous batching).  Served bead-steps/s = all
+    jobs' bead-steps / (first arrival -> last completion); latency = arrival -> final callback.
+    Sequential: a seeded sample of the same jobs run one at a time on the plain engines (Attach
+    + Run(intervals, callback) + the remainder, the reference's pattern), wall clock per job."""
+
+    import pdpd_engine as E
+
+    rng = np.random.default_rng(seed)
+    arrivals = []
+    t = rng.exponential(1.0 / rate)
+    while t < window_s:
+        arrivals.append(t)
+        t += rng.exponential(1.0 / rate)
+    sides = np.clip(np.rint(8.0 * 8.0 ** rng.uniform(size=len(arrivals))), 8, 64).astype(int)
+    nsteps = rng.integers(100, 2001, size=len(arrivals))
+    worlds = [W.make_water(int(L), seed=k + 1, gen_seed=10_000 + k) for k, L in enumerate(sides)]
+    total_bs = int(sum(w.n_beads * int(n) for w, n in zip(worlds, nsteps)))
+
+    srv = E.GB300DPDServer("fp32", device=device, memory_budget_bytes=budget,
+                           interval_steps=interval, keep_results=False)
+    srv.submit(W.make_water(8, seed=1), 2 * interval)  # warm-up: module load, first graph
+    srv.drain()
+    st0 = srv.stats()
+    launches0 = srv.kernel_launches()
+    t0 = time.perf_counter()
+
+    def client():
+        for a, w, n in zip(arrivals, worlds, nsteps):
+            d = t0 + a - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            srv.submit(w, int(n))
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    srv.drain()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    launches = srv.kernel_launches() - launches0
+    srv.close()
+    served = (st["bead_steps"] - st0["bead_steps"]) / wall
+
+    pick = np.random.default_rng(seed + 1).permutation(len(worlds))
+
+    def sequential(prec, count):
+        eng = E.GB300DPDEngine(prec, device=device)
+        eng.Attach(W.make_water(8, seed=1))
+        eng.Run(interval)
+        bs, secs = 0, 0.0
+        for k in pick[:count]:
+            w, n = worlds[k].copy(), int(nsteps[k])
+            t1 = time.perf_counter()
+            eng.Attach(w)
+            eng.Run(n // interval, interval, lambda: True)
+            if n % interval:
+                eng.Run(n % interval)
+            secs += time.perf_counter() - t1
+            bs += w.n_beads * n
+        eng.close()
+        return bs / secs, count
+
+    seq32, n32 = sequential("fp32", seq_fp32)
+    seq64, n64 = sequential("fp64", seq_fp64)
+    return {"workload": f"Poisson {rate:g} jobs/s for {window_s:g} s ({len(worlds)} jobs), water "
+                        f"sides log-uniform 8..64, n_steps U{{100..2000}}, callback every "
+                        f"{interval} steps, {budget / 2**30:g} GiB budget",
+            "jobs": len(worlds), "offered_bead_steps_per_s": total_bs / window_s,
+            "served_bead_steps_per_s": served, "wall_s": wall,
+            "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
+            "latency_max_s": st["latency_max_s"], "max_active_jobs": st["max_active"],
+            "repacks": st["repacks"] - st0["repacks"], "gpu_launches": launches,
+            "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
+            "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,
+            "served_vs_sequential_fp32": served / seq32, "served_vs_sequential_fp64": served / seq64}
+
+
 def dist_setup(n_gpus):
     rank, world_size = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
     if world_size > 1:
@@ -329,6 +412,9 @@ def run_engine_arm(args):
     batched = None
     if not args.no_batched and world_size == 1:
         batched = batched_grid_metrics(device=local)
+    serving = None
+    if args.serving_window > 0 and world_size == 1:
+        serving = serving_metrics(window_s=args.serving_window, device=local)
     if rank != 0:
         return
     cpu = None
@@ -362,6 +448,7 @@ def run_engine_arm(args):
         "gpu_launches": launches,
         "cpu_baseline": cpu,
         "batched_grid": batched,
+        "serving": serving,
         "kernel_config": {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
                                                     "autotune")},
     }
@@ -381,6 +468,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 512-state batched grid (FP32 batched vs FP64 plain)")
+    ap.add_argument("--serving-window", type=float, default=4.0,
+                    help="seconds of Poisson arrivals of the serving stream (0 skips it)")
     ap.add_argument("--side", type=int, default=None,
                     help="override the box side of the workload (profiling on smaller boxes)")
     args = ap.parse_args()

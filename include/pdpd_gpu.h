@@ -215,6 +215,63 @@ int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, double *d_f
  * each kernel node).  For accounting in benchmarks. */
 uint64_t pdpd_kernel_launches(pdpd_engine *e);
 
+/* ---- Job server (continuous batching) -- no counterpart in the reference. ----------------
+ *
+ * The reference serves one world per engine: a caller with many independent simulations runs
+ * them one after another (DPDEngine::Attach + Run(interval_count, interval_size, callback),
+ * dpd_engine.hpp:176-212).  A server runs many such jobs at once on one GPU: a worker thread
+ * admits submitted jobs in arrival order while their estimated device footprint fits the
+ * memory budget, attaches all admitted worlds as one batch and steps them together; jobs that
+ * finish leave and waiting jobs join at interval boundaries, continuing worlds keeping their
+ * state on the device.  Each job's results are bit-identical to running its world alone on an
+ * engine of the same precision and configuration.
+ *
+ * Job callback, called on the server's worker thread:
+ *   status 0   interval snapshot after every interval_steps steps of the job,
+ *   status 1   final state after n_steps (one call, then the job is done),
+ *   status < 0 the job failed: -PDPD_E_* code (x, v, f are NULL; the message is returned by
+ *              pdpd_server_drain's pdpd_last_error(NULL)).
+ * x, v, f point at n_beads rows stride_bytes apart, in bead-id order, valid during the call.
+ * t is the job's time after the snapshot.  Return nonzero to continue; 0 on a snapshot ends
+ * the job there (like the reference's interval callback returning false) -- the job counts as
+ * done and gets no further calls.  A callback may submit jobs; it must not drain or destroy
+ * the server. */
+typedef struct pdpd_server pdpd_server;
+typedef int (*pdpd_job_fn)(void *user, uint64_t job, int64_t t, const double *x, const double *v,
+                           const double *f, size_t stride_bytes, uint32_t n_beads, int status);
+
+typedef struct pdpd_server_stats {
+    uint64_t jobs_submitted, jobs_done, jobs_failed;
+    uint64_t bead_steps;   /* bead-steps computed (beads x steps, summed over epochs) */
+    uint64_t repacks;      /* batch re-attaches (membership changes) */
+    uint32_t max_active;   /* largest number of jobs in one batch */
+    uint32_t pad;
+    double busy_s;         /* wall time with at least one job admitted */
+    double wall_s;         /* first submit to last completion */
+    double latency_p50_s, latency_p99_s, latency_max_s;  /* submit -> final callback done */
+} pdpd_server_stats;
+
+/* Create a server with its own engine (precision, device as pdpd_create) and worker thread.
+ * memory_budget_bytes bounds the summed footprint estimate of the admitted jobs (a job larger
+ * than the budget still runs, alone); interval_steps >= 1 is the snapshot interval. */
+int pdpd_server_create(int precision, int device, size_t memory_budget_bytes,
+                       uint32_t interval_steps, pdpd_server **out);
+/* Queue a job: the world (copied; the caller's arrays may be reused at once) advanced by
+ * n_steps.  n_steps == 0 completes at once with one final callback on the calling thread. */
+int pdpd_server_submit(pdpd_server *s, const pdpd_world *w, uint32_t n_steps, pdpd_job_fn cb,
+                       void *user, uint64_t *job_id);
+/* Wait until every submitted job is done or failed.  Returns PDPD_OK, or the status of the
+ * last failure since the previous drain. */
+int pdpd_server_drain(pdpd_server *s);
+/* Set an engine configuration entry (as pdpd_set_config) while the server is idle;
+ * PDPD_E_STATE while jobs are queued or running. */
+int pdpd_server_config(pdpd_server *s, const char *key, const char *value);
+int pdpd_server_stats_get(pdpd_server *s, pdpd_server_stats *out);
+/* The server's engine, for read-only queries (pdpd_kernel_launches, pdpd_get_timings). */
+pdpd_engine *pdpd_server_engine(pdpd_server *s);
+/* Finish the queued jobs, stop the worker and free everything. */
+void pdpd_server_destroy(pdpd_server *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -403,7 +403,7 @@ struct pdpd_engine {
 // ------------------------------------------------------------------------------------------
 // validation
 
-static int check_world(const pdpd_world *w, char *reason, size_t n)
+static int check_world(const pdpd_world *w, char *reason, size_t n, bool need_beads = true)
 {
     auto say = [&](int code, const char *msg) {
         if (reason && n) snprintf(reason, n, "%s", msg);
@@ -428,7 +428,7 @@ static int check_world(const pdpd_world *w, char *reason, size_t n)
     for (uint32_t i = 0; i < w->n_bead_types * w->n_bead_types; i++)
         if (!(w->dissipative[i] >= 0) || !std::isfinite(w->conservative[i]))
             return say(PDPD_E_INVALID, "Interaction strengths must be finite and gamma >= 0.");
-    if (w->n_beads && (!w->hash || !w->x || !w->v || !w->f))
+    if (w->n_beads && (!w->hash || (need_beads && (!w->x || !w->v || !w->f))))
         return say(PDPD_E_INVALID, "Missing bead arrays.");
     for (uint32_t i = 0; i < w->n_beads; i++)
         if ((w->hash[i] >> 28) >= w->n_bead_types) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
@@ -540,18 +540,49 @@ int pdpd_attach(pdpd_engine *e, const pdpd_world *w)
     return pdpd_attach_batch(e, w, 1);
 }
 
-int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
+static int download(pdpd_engine *e, int buf, cudaStream_t s);
+
+// Attach a batch.  keep_old (optional, one entry per world): index of a world of the
+// currently attached batch whose bead state (x, v, f) the new world takes over on the device
+// -- no host round trip -- or -1 for a world whose bead arrays come from its descriptor.
+// The descriptors of kept worlds supply everything else (box, parameters, hashes, bonds, t).
+static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, const int32_t *keep_old)
 {
     if (!e) return PDPD_E_INVALID;
     if (!ws || n_worlds == 0) return e->fail(PDPD_E_INVALID, "no worlds given");
     double t0 = now_s();
     cudaSetDevice(e->device);
     cudaStreamSynchronize(e->stream);
+    // Resident re-pack: unsort the current arena into a device staging buffer first.
+    DevBuf snap;
+    std::vector<uint32_t> old_base;
+    bool any_kept = false;
+    for (uint32_t i = 0; keep_old && i < n_worlds; i++) any_kept |= keep_old[i] >= 0;
+    if (any_kept) {
+        if (!e->attached) return e->fail(PDPD_E_STATE, "re-pack without an attached batch");
+        for (uint32_t i = 0; i < n_worlds; i++)
+            if (keep_old[i] >= (int32_t)e->worlds.size())
+                return e->fail(PDPD_E_INVALID, "re-pack refers to a world that is not attached");
+        int rc = download(e, 0, e->stream);
+        if (rc) return rc;
+        cudaStreamSynchronize(e->stream);
+        snap.p = e->d_staging[0].p;
+        snap.bytes = e->d_staging[0].bytes;
+        e->d_staging[0].p = nullptr;
+        e->d_staging[0].bytes = 0;
+        for (const WorldHost &wh : e->worlds) old_base.push_back(wh.dev.bead_base);
+    }
+    struct SnapGuard {  // freed on every return; cudaFree waits for the copies reading it
+        DevBuf &b;
+        ~SnapGuard() { b.release(); }
+    } snap_guard{snap};
     e->release();
     char reason[256];
     uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
     for (uint32_t i = 0; i < n_worlds; i++) {
-        int rc = check_world(&ws[i], reason, sizeof reason);
+        const bool kept = keep_old && keep_old[i] >= 0;
+        int rc = check_world(&ws[i], reason, sizeof reason, !kept);
+        if (rc) snap.release();
         if (rc) return e->fail(rc, "world %u: %s", i, reason);
         nb += ws[i].n_beads;
         nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
@@ -708,6 +739,10 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     for (uint32_t i = 0; i < n_worlds; i++) {
         const pdpd_world &w = ws[i];
         uint32_t bb = wdev[i].bead_base;
+        if (keep_old && keep_old[i] >= 0) {  // bead state comes from the old arena (below)
+            for (uint32_t k = 0; k < w.n_beads; k++) hh[bb + k] = w.hash[k];
+            continue;
+        }
         for (uint32_t k = 0; k < w.n_beads; k++) {
             const double *x = vec_at(w.x, w.bead_stride_bytes, k);
             const double *v = vec_at(w.v, w.bead_stride_bytes, k);
@@ -736,7 +771,21 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
         H2D(e->d_bond_params, bp32.data(), sizeof(float) * bp32.size());
         H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
     }
-    H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
+    if (!any_kept) {
+        H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
+    } else {  // only the rows of the worlds that come from their descriptors
+        for (uint32_t i = 0; i < n_worlds; i++)
+            if (keep_old[i] < 0 && ws[i].n_beads && ce == cudaSuccess)
+                ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
+                                     hs + 9 * (size_t)wdev[i].bead_base, sizeof(double) * 9 * ws[i].n_beads,
+                                     cudaMemcpyHostToDevice, s);
+    }
+    for (uint32_t i = 0; any_kept && i < n_worlds; i++) {
+        if (keep_old[i] < 0 || ws[i].n_beads == 0 || ce != cudaSuccess) continue;
+        ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
+                             snap.as<double>() + 9 * (size_t)old_base[keep_old[i]],
+                             sizeof(double) * 9 * ws[i].n_beads, cudaMemcpyDeviceToDevice, s);
+    }
     H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
     H2D(e->d_bonded, bonded.data(), sizeof(uint32_t) * bonded.size());
     if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_cnt.p, 0, sizeof(uint32_t) * nc, s);
@@ -814,6 +863,11 @@ int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
     }
     e->timings = pdpd_timings{-1, -1, now_s() - t0, -1, -1, -1};
     return PDPD_OK;
+}
+
+int pdpd_attach_batch(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds)
+{
+    return attach_impl(e, ws, n_worlds, nullptr);
 }
 
 int pdpd_run_async(pdpd_engine *e, uint32_t n_steps)
@@ -1208,6 +1262,494 @@ int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint3
 uint64_t pdpd_kernel_launches(pdpd_engine *e)
 {
     return e ? e->launches : 0;
+}
+
+}  // extern "C"
+
+
+// ==========================================================================================
+// Job server: continuous batching of independent worlds on one engine.
+//
+// Jobs (a world, a number of steps, a callback) arrive from any thread.  One worker thread
+// admits them in arrival order while their estimated device footprint fits the memory
+// budget, keeps every admitted world attached in one batch, and runs the batch in epochs that
+// end at the next interval boundary of some job (every `interval` steps of it) or at its
+// completion.  When jobs leave or join, the batch is re-packed on the device: continuing
+// worlds take their state over from the old arena with no host round trip.  At a boundary
+// the snapshot is unsorted on the main stream and copied to pinned host memory on the side
+// stream; the callbacks of epoch k run on the host while epoch k+1 computes.  The worlds of a
+// batch are independent and each is stepped exactly as if it ran alone, so a job's results do
+// not depend on what else the server runs.
+// ==========================================================================================
+
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+namespace {
+
+struct ServerJob {
+    uint64_t id = 0;
+    std::vector<double> cons, diss, x, v, f, bk, br, ak, at;
+    std::vector<uint8_t> stat;
+    std::vector<uint32_t> hash, bb, ab;
+    pdpd_world desc{};
+    uint32_t n_steps = 0, done = 0;
+    int64_t t = 0;
+    pdpd_job_fn cb = nullptr;
+    void *user = nullptr;
+    double t_submit = 0;
+    size_t bytes = 0;
+    int slot = -1;           // world index in the attached batch, -1 before the first attach
+    bool stopped = false;    // the callback asked to stop
+};
+
+// A callback owed for one job: its rows start at `row` in host snapshot buffer `buf`.
+struct Delivery {
+    ServerJob *job;
+    size_t row;
+    uint32_t n_beads;
+    int64_t t;
+    int final_state;
+};
+
+size_t job_bytes(const pdpd_world &w, int precision)
+{
+    // sorted state A and B, ids / cells / ranks, two id-ordered staging rows, hashes
+    const size_t per_bead = precision == PDPD_FP64 ? 424 : 296;
+    const size_t cells = (size_t)w.box[0] * w.box[1] * w.box[2];
+    return per_bead * w.n_beads + 12 * cells +
+           48 * (2 * (size_t)w.n_bonds + 3 * (size_t)w.n_angles) + 4096;
+}
+
+}  // namespace
+
+struct pdpd_server {
+    pdpd_engine *eng = nullptr;
+    int precision = PDPD_FP32;
+    size_t budget = 0;
+    uint32_t interval = 100;
+
+    // shared with submitters (under mu)
+    std::mutex mu;
+    std::condition_variable cv, cv_idle;
+    std::deque<std::unique_ptr<ServerJob>> pending;
+    bool stop = false, busy = false;
+    int status = PDPD_OK;
+    std::string err;
+    uint64_t next_id = 1;
+    pdpd_server_stats st{};
+    std::vector<double> latencies;
+    double t_first = -1, t_last = 0, t_busy_from = 0;
+
+    // worker only
+    std::vector<std::unique_ptr<ServerJob>> active, retiring;
+    std::vector<Delivery> owed;
+    int owed_buf = 0;
+    bool changed = false;
+    HostPinned snap[2];
+    cudaEvent_t ev_unsorted = nullptr, ev_copied[2] = {nullptr, nullptr};
+    std::thread worker;
+
+    void run();
+    int repack();
+    void deliver();
+    void fail_jobs(const std::vector<ServerJob *> &jobs, int code);
+    void finish_job(ServerJob &j);
+};
+
+// Attach the active jobs as one batch, continuing worlds taking their state over on the device.
+int pdpd_server::repack()
+{
+    if (!changed) return PDPD_OK;
+    cudaStreamSynchronize(eng->side);  // no snapshot copy may still read the old arena
+    changed = false;
+    if (active.empty()) {
+        pdpd_attach(eng, nullptr);  // release the arena while idle
+        return PDPD_OK;
+    }
+    std::vector<pdpd_world> descs;
+    std::vector<int32_t> keep;
+    for (auto &j : active) {
+        pdpd_world d = j->desc;
+        d.t = j->t;
+        descs.push_back(d);
+        keep.push_back(j->slot);
+    }
+    int rc = attach_impl(eng, descs.data(), (uint32_t)descs.size(), keep.data());
+    if (rc) return rc;
+    for (size_t i = 0; i < active.size(); i++) {
+        ServerJob &j = *active[i];
+        if (j.slot < 0) {  // the initial state lives on the device from now on
+            std::vector<double>().swap(j.x);
+            std::vector<double>().swap(j.v);
+            std::vector<double>().swap(j.f);
+            j.desc.x = j.desc.v = j.desc.f = nullptr;
+        }
+        j.slot = (int)i;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    st.repacks++;
+    return PDPD_OK;
+}
+
+void pdpd_server::finish_job(ServerJob &j)
+{
+    const double now = now_s();
+    std::lock_guard<std::mutex> lk(mu);
+    latencies.push_back(now - j.t_submit);
+    st.jobs_done++;
+    t_last = now;
+}
+
+// Callbacks of the previous epoch (its snapshot copy overlapped the current epoch).
+void pdpd_server::deliver()
+{
+    if (owed.empty()) return;
+    cudaEventSynchronize(ev_copied[owed_buf]);
+    const double *base = (const double *)snap[owed_buf].p;
+    for (const Delivery &d : owed) {
+        ServerJob &j = *d.job;
+        if (j.stopped) continue;  // stopped by an earlier callback, or failed
+        const double *row = base + d.row;
+        const int status = d.final_state ? 1 : 0;
+        const int go = j.cb ? j.cb(j.user, j.id, d.t, row, row + 3, row + 6, 9 * sizeof(double),
+                                   d.n_beads, status)
+                            : 1;
+        if (d.final_state) {
+            finish_job(j);
+        } else if (!go && !j.stopped) {  // the job ends at this snapshot
+            j.stopped = true;
+            finish_job(j);
+        }
+    }
+    owed.clear();
+    retiring.clear();
+}
+
+void pdpd_server::fail_jobs(const std::vector<ServerJob *> &jobs, int code)
+{
+    for (ServerJob *j : jobs) {
+        if (j->cb && !j->stopped) j->cb(j->user, j->id, j->t, nullptr, nullptr, nullptr, 0, 0, -code);
+        j->stopped = true;
+        std::lock_guard<std::mutex> lk(mu);
+        st.jobs_failed++;
+        status = code;
+        err = eng->err;
+    }
+    for (size_t i = 0; i < active.size();)
+        if (active[i]->stopped) {
+            retiring.push_back(std::move(active[i]));
+            active.erase(active.begin() + i);
+            changed = true;
+        } else {
+            i++;
+        }
+}
+
+void pdpd_server::run()
+{
+    cudaSetDevice(eng->device);
+    int b = 0;  // host snapshot buffer of the current epoch
+    while (true) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return stop || !pending.empty() || !active.empty() || !owed.empty(); });
+            if (stop && pending.empty() && active.empty() && owed.empty()) break;
+            // Admission only where every running job is at one of its interval boundaries: the
+            // jobs' intervals then stay in phase and epochs are whole intervals (a job that
+            // ends mid-interval splits one epoch in two).
+            size_t used = 0;
+            bool in_phase = true;
+            for (auto &j : active) {
+                used += j->bytes;
+                in_phase &= j->done % interval == 0;
+            }
+            while (in_phase && !pending.empty() && (active.empty() || used + pending.front()->bytes <= budget)) {
+                used += pending.front()->bytes;
+                active.push_back(std::move(pending.front()));
+                pending.pop_front();
+                changed = true;
+            }
+            if (!busy) t_busy_from = now_s();
+            busy = true;
+            st.max_active = std::max<uint32_t>(st.max_active, (uint32_t)active.size());
+        }
+        // jobs whose callback asked to stop leave before the next epoch
+        for (size_t i = 0; i < active.size();)
+            if (active[i]->stopped) {
+                retiring.push_back(std::move(active[i]));
+                active.erase(active.begin() + i);
+                changed = true;
+            } else {
+                i++;
+            }
+        if (changed) deliver();  // the re-pack needs the snapshot buffers and the old arena
+        int rc = repack();
+        if (rc != PDPD_OK) {
+            std::vector<ServerJob *> all;
+            for (auto &j : active) all.push_back(j.get());
+            fail_jobs(all, rc);
+            pdpd_attach(eng, nullptr);
+            changed = false;
+        }
+        std::vector<Delivery> next;
+        uint32_t epoch = 0;
+        if (!active.empty()) {
+            epoch = UINT32_MAX;
+            for (auto &j : active)
+                epoch = std::min({epoch, interval - j->done % interval, j->n_steps - j->done});
+            rc = pdpd_run_async(eng, epoch);
+            std::vector<size_t> at_boundary;
+            for (size_t i = 0; i < active.size(); i++) {
+                ServerJob &j = *active[i];
+                j.done += epoch;
+                j.t += epoch;
+                if (j.done % interval == 0 || j.done == j.n_steps) at_boundary.push_back(i);
+            }
+            if (rc == PDPD_OK && !at_boundary.empty()) {
+                cudaEventSynchronize(ev_copied[b]);  // the buffer's last copy (normally long done)
+                if (snap[b].alloc(sizeof(double) * 9 * (size_t)eng->n_beads) != cudaSuccess)
+                    rc = eng->fail(PDPD_E_NOMEM, "pinned snapshot allocation failed");
+                // the previous copy out of the device staging rows must be done before the unsort
+                if (rc == PDPD_OK) cudaStreamWaitEvent(eng->stream, ev_copied[b ^ 1], 0);
+                if (rc == PDPD_OK) rc = download(eng, 1, eng->stream);
+                if (rc == PDPD_OK) {
+                    cudaEventRecord(ev_unsorted, eng->stream);
+                    cudaStreamWaitEvent(eng->side, ev_unsorted, 0);
+                    for (size_t i : at_boundary) {
+                        ServerJob &j = *active[i];
+                        const WorldDev &wd = eng->worlds[j.slot].dev;
+                        const size_t row = 9 * (size_t)wd.bead_base;
+                        if (wd.n_beads)
+                            cudaMemcpyAsync((double *)snap[b].p + row, eng->d_staging[1].as<double>() + row,
+                                            sizeof(double) * 9 * wd.n_beads, cudaMemcpyDeviceToHost, eng->side);
+                        next.push_back({&j, row, wd.n_beads, j.t, j.done == j.n_steps ? 1 : 0});
+                    }
+                    cudaEventRecord(ev_copied[b], eng->side);
+                }
+            }
+        }
+        deliver();  // host callbacks of the previous epoch while this one computes
+        if (!active.empty()) {
+            if (rc == PDPD_OK) rc = pdpd_sync(eng);
+            if (rc == PDPD_E_BOND_SNAPPED || rc == PDPD_E_BEAD_LOST) {
+                // worlds are independent: fail the ones that raised an error flag, keep the rest
+                const WorldDev *wd = (const WorldDev *)eng->h_err.p;
+                std::vector<ServerJob *> bad;
+                for (auto &j : active)
+                    if (wd[j->slot].err) bad.push_back(j.get());
+                fail_jobs(bad, rc);
+                next.erase(std::remove_if(next.begin(), next.end(), [](const Delivery &d) { return d.job->stopped; }),
+                           next.end());
+            } else if (rc != PDPD_OK) {
+                std::vector<ServerJob *> all;
+                for (auto &j : active) all.push_back(j.get());
+                fail_jobs(all, rc);
+                next.clear();
+                cudaStreamSynchronize(eng->side);
+                pdpd_attach(eng, nullptr);
+                changed = false;
+            }
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                for (auto &j : active) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
+            }
+            owed.swap(next);
+            owed_buf = b;
+            b ^= 1;
+            for (size_t i = 0; i < active.size();)
+                if (active[i]->done == active[i]->n_steps) {
+                    retiring.push_back(std::move(active[i]));
+                    active.erase(active.begin() + i);
+                    changed = true;
+                } else {
+                    i++;
+                }
+        }
+        if (active.empty() && owed.empty()) {
+            repack();  // releases the arena
+            std::lock_guard<std::mutex> lk(mu);
+            if (busy) st.busy_s += now_s() - t_busy_from;
+            busy = false;
+            if (pending.empty()) cv_idle.notify_all();
+        }
+    }
+}
+
+extern "C" {
+
+int pdpd_server_create(int precision, int device, size_t memory_budget_bytes, uint32_t interval_steps,
+                       pdpd_server **out)
+{
+    if (!out) return PDPD_E_INVALID;
+    *out = nullptr;
+    if (interval_steps == 0) {
+        g_last_error = "interval_steps must be at least 1";
+        return PDPD_E_INVALID;
+    }
+    pdpd_engine *e = nullptr;
+    int rc = pdpd_create(precision, device, &e);
+    if (rc) return rc;
+    pdpd_server *s = new pdpd_server();
+    s->eng = e;
+    s->precision = precision;
+    s->budget = memory_budget_bytes;
+    s->interval = interval_steps;
+    cudaSetDevice(e->device);
+    cudaEventCreateWithFlags(&s->ev_unsorted, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&s->ev_copied[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&s->ev_copied[1], cudaEventDisableTiming);
+    s->worker = std::thread([s] { s->run(); });
+    *out = s;
+    return PDPD_OK;
+}
+
+int pdpd_server_config(pdpd_server *s, const char *key, const char *value)
+{
+    if (!s) return PDPD_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);  // the worker touches the engine only while busy
+    if (!s->pending.empty() || s->busy) {
+        g_last_error = "the server is running jobs: drain it before changing its configuration";
+        return PDPD_E_STATE;
+    }
+    int rc = pdpd_set_config(s->eng, key, value);
+    if (rc) g_last_error = s->eng->err;
+    return rc;
+}
+
+int pdpd_server_submit(pdpd_server *s, const pdpd_world *w, uint32_t n_steps, pdpd_job_fn cb, void *user,
+                       uint64_t *job_id)
+{
+    if (job_id) *job_id = 0;
+    if (!s || !w) return PDPD_E_INVALID;
+    char reason[256];
+    int rc = check_world(w, reason, sizeof reason);
+    if (rc) {
+        g_last_error = reason;
+        return rc;
+    }
+    auto j = std::make_unique<ServerJob>();
+    const uint32_t nt = w->n_bead_types, n = w->n_beads;
+    j->cons.assign(w->conservative, w->conservative + nt * nt);
+    j->diss.assign(w->dissipative, w->dissipative + nt * nt);
+    j->stat.assign(nt, 0);
+    j->hash.assign(w->hash, w->hash + n);
+    j->x.resize(3 * (size_t)n);
+    j->v.resize(3 * (size_t)n);
+    j->f.resize(3 * (size_t)n);
+    for (uint32_t k = 0; k < n; k++)
+        for (int d = 0; d < 3; d++) {
+            j->x[3 * (size_t)k + d] = vec_at(w->x, w->bead_stride_bytes, k)[d];
+            j->v[3 * (size_t)k + d] = vec_at(w->v, w->bead_stride_bytes, k)[d];
+            j->f[3 * (size_t)k + d] = vec_at(w->f, w->bead_stride_bytes, k)[d];
+        }
+    if (w->n_bonds) {
+        j->bb.assign(w->bond_beads, w->bond_beads + 2 * (size_t)w->n_bonds);
+        j->bk.assign(w->bond_kappa, w->bond_kappa + w->n_bonds);
+        j->br.assign(w->bond_r0, w->bond_r0 + w->n_bonds);
+    }
+    if (w->n_angles) {
+        j->ab.assign(w->angle_beads, w->angle_beads + 3 * (size_t)w->n_angles);
+        j->ak.assign(w->angle_kappa, w->angle_kappa + w->n_angles);
+        j->at.assign(w->angle_theta0, w->angle_theta0 + w->n_angles);
+    }
+    pdpd_world &d = j->desc;
+    d = *w;
+    d.conservative = j->cons.data();
+    d.dissipative = j->diss.data();
+    d.stationary = j->stat.data();
+    d.hash = j->hash.data();
+    d.x = j->x.data();
+    d.v = j->v.data();
+    d.f = j->f.data();
+    d.bead_stride_bytes = 0;
+    d.bond_beads = j->bb.data();
+    d.bond_kappa = j->bk.data();
+    d.bond_r0 = j->br.data();
+    d.angle_beads = j->ab.data();
+    d.angle_kappa = j->ak.data();
+    d.angle_theta0 = j->at.data();
+    j->n_steps = n_steps;
+    j->t = w->t;
+    j->cb = cb;
+    j->user = user;
+    j->bytes = job_bytes(*w, s->precision);
+    j->t_submit = now_s();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        j->id = s->next_id++;
+        if (job_id) *job_id = j->id;
+        if (s->t_first < 0) s->t_first = j->t_submit;
+        s->st.jobs_submitted++;
+        if (n_steps > 0) {
+            s->pending.push_back(std::move(j));
+            s->cv.notify_all();
+            return PDPD_OK;
+        }
+        s->st.jobs_done++;
+        s->latencies.push_back(0.0);
+        s->t_last = now_s();
+    }
+    // nothing to run: the final state is the initial one
+    if (cb) cb(user, j->id, w->t, j->x.data(), j->v.data(), j->f.data(), 3 * sizeof(double), n, 1);
+    return PDPD_OK;
+}
+
+int pdpd_server_drain(pdpd_server *s)
+{
+    if (!s) return PDPD_E_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_idle.wait(lk, [&] { return s->pending.empty() && !s->busy; });
+    int rc = s->status;
+    if (rc) g_last_error = s->err;
+    s->status = PDPD_OK;
+    return rc;
+}
+
+int pdpd_server_stats_get(pdpd_server *s, pdpd_server_stats *out)
+{
+    if (!s || !out) return PDPD_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->st;
+    std::vector<double> l = s->latencies;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double p) {
+        return l.empty() ? 0.0 : l[std::min(l.size() - 1, (size_t)std::ceil(p * l.size()) - (p > 0 ? 1 : 0))];
+    };
+    out->latency_p50_s = pct(0.50);
+    out->latency_p99_s = pct(0.99);
+    out->latency_max_s = l.empty() ? 0.0 : l.back();
+    out->wall_s = s->t_first < 0 ? 0.0 : s->t_last - s->t_first;
+    if (s->busy) out->busy_s += now_s() - s->t_busy_from;
+    return PDPD_OK;
+}
+
+pdpd_engine *pdpd_server_engine(pdpd_server *s)
+{
+    return s ? s->eng : nullptr;
+}
+
+void pdpd_server_destroy(pdpd_server *s)
+{
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    cudaSetDevice(s->eng->device);
+    cudaStreamSynchronize(s->eng->side);
+    if (s->ev_unsorted) cudaEventDestroy(s->ev_unsorted);
+    for (cudaEvent_t ev : s->ev_copied)
+        if (ev) cudaEventDestroy(ev);
+    s->snap[0].release();
+    s->snap[1].release();
+    pdpd_destroy(s->eng);
+    delete s;
 }
 
 }  // extern "C"

@@ -38,7 +38,9 @@ EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support"
             "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
             "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc",
-            "pdpd_observe"]
+            "pdpd_observe", "pdpd_server_create", "pdpd_server_submit", "pdpd_server_drain",
+            "pdpd_server_config", "pdpd_server_stats_get", "pdpd_server_engine",
+            "pdpd_server_destroy"]
 
 
 class PdpdWorld(C.Structure):
@@ -68,7 +70,17 @@ class PdpdObservables(C.Structure):
     _fields_ = [("ke2", C.c_double), ("momentum", C.c_double * 3), ("virial", C.c_double)]
 
 
+class PdpdServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_done", C.c_uint64),
+                ("jobs_failed", C.c_uint64), ("bead_steps", C.c_uint64), ("repacks", C.c_uint64),
+                ("max_active", C.c_uint32), ("pad", C.c_uint32), ("busy_s", C.c_double),
+                ("wall_s", C.c_double), ("latency_p50_s", C.c_double),
+                ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double)]
+
+
 INTERVAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)
+JOB_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_int64, C.POINTER(C.c_double),
+                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_size_t, C.c_uint32, C.c_int)
 
 _LIB = None
 
@@ -106,6 +118,14 @@ def lib():
         "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
         "pdpd_step_noalloc": (i32, [C.POINTER(PdpdWorld), vp, vp, vp, vp, u32, vp]),
         "pdpd_observe": (i32, [vp, u32, C.POINTER(PdpdObservables), u32, vp, u32, vp]),
+        "pdpd_server_create": (i32, [i32, i32, C.c_size_t, u32, C.POINTER(vp)]),
+        "pdpd_server_submit": (i32, [vp, C.POINTER(PdpdWorld), u32, JOB_FN, vp,
+                                     C.POINTER(C.c_uint64)]),
+        "pdpd_server_drain": (i32, [vp]),
+        "pdpd_server_config": (i32, [vp, C.c_char_p, C.c_char_p]),
+        "pdpd_server_stats_get": (i32, [vp, C.POINTER(PdpdServerStats)]),
+        "pdpd_server_engine": (vp, [vp]),
+        "pdpd_server_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -340,3 +360,117 @@ class GB300DPDEngine:
         if into is not None:
             into.x, into.v, into.f, into.t = x, v, f, int(t.value)
         return x, v, f, int(t.value)
+
+
+def _rows(ptr, n, stride_bytes):
+    """Copy n vectors of 3 doubles, stride_bytes apart, out of a callback's pointer."""
+    if n == 0:
+        return np.empty((0, 3))
+    step = stride_bytes // 8
+    flat = np.ctypeslib.as_array(ptr, shape=((n - 1) * step + 3,))
+    return np.lib.stride_tricks.as_strided(flat, shape=(n, 3), strides=(stride_bytes, 8)).copy()
+
+
+class GB300DPDServer:
+    """Continuous-batching job server over the C ABI's ``pdpd_server_*`` (no counterpart in the
+    reference, which runs one world per engine).
+
+    ``submit(world, n_steps, on_interval=None)`` queues a job and returns its id; the world is
+    copied.  ``on_interval(job_id, t, x, v, f)`` (optional) is called on the server's worker
+    thread after every ``interval_steps`` steps of the job; returning ``False`` ends the job at
+    that snapshot.  ``drain()`` waits for every queued job and raises the first error.  The
+    final state of job ``i`` is ``results[i] = (x, v, f, t)``; failed jobs are in ``failed``.
+    With ``keep_results=False`` the final states are not copied (``results[i] = t`` only) and
+    snapshots are copied only for jobs with an ``on_interval`` handler.
+    """
+
+    def __init__(self, precision="fp32", device=-1, memory_budget_bytes=40 << 30,
+                 interval_steps=100, keep_results=True):
+        code = {"fp32": PDPD_FP32, "fp64": PDPD_FP64}[precision]
+        h = C.c_void_p()
+        rc = lib().pdpd_server_create(code, device, int(memory_budget_bytes), int(interval_steps),
+                                      C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"pdpd_server_create: {STATUS.get(rc)}: "
+                               f"{lib().pdpd_last_error(None).decode()}")
+        self._h = h
+        self.precision = precision
+        self.interval_steps = int(interval_steps)
+        self.keep_results = bool(keep_results)
+        self.results = {}
+        self.snapshots = {}   # job id -> number of interval callbacks seen
+        self.failed = {}      # job id -> status name
+        self._handlers = {}
+        self._errors = []
+        self._cb = JOB_FN(self._dispatch)
+
+    def _dispatch(self, user, job, t, x, v, f, stride, n, status):
+        try:
+            if status < 0:
+                self.failed[job] = STATUS.get(-status, -status)
+                self._handlers.pop(job, None)
+                return 0
+            h = self._handlers.get(job)
+            if not self.keep_results and h is None:
+                if status == 1:
+                    self.results[job] = int(t)
+                else:
+                    self.snapshots[job] = self.snapshots.get(job, 0) + 1
+                return 1
+            xs, vs, fs = _rows(x, n, stride), _rows(v, n, stride), _rows(f, n, stride)
+            if status == 1:
+                self.results[job] = (xs, vs, fs, int(t))
+                self._handlers.pop(job, None)
+                return 1
+            self.snapshots[job] = self.snapshots.get(job, 0) + 1
+            if h is not None and h(job, int(t), xs, vs, fs) is False:
+                self.results[job] = (xs, vs, fs, int(t))
+                self._handlers.pop(job, None)
+                return 0
+            return 1
+        except BaseException as e:  # noqa: BLE001 -- re-raised by drain()
+            self._errors.append(e)
+            return 0
+
+    def submit(self, world, n_steps, on_interval=None) -> int:
+        fl = _Flat(world)
+        jid = C.c_uint64(0)
+        rc = lib().pdpd_server_submit(self._h, C.byref(fl.struct), int(n_steps), self._cb, None,
+                                      C.byref(jid))
+        if rc != 0:
+            raise RuntimeError(f"submit: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
+        if on_interval is not None:
+            self._handlers[int(jid.value)] = on_interval
+        return int(jid.value)
+
+    def drain(self):
+        rc = lib().pdpd_server_drain(self._h)
+        if self._errors:
+            e, self._errors = self._errors[0], []
+            raise e
+        if rc != 0:
+            raise RuntimeError(f"drain: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
+
+    def config(self, key, value):
+        rc = lib().pdpd_server_config(self._h, str(key).encode(), str(value).encode())
+        if rc != 0:
+            raise RuntimeError(f"config: {STATUS.get(rc)}: {lib().pdpd_last_error(None).decode()}")
+
+    def stats(self) -> dict:
+        st = PdpdServerStats()
+        lib().pdpd_server_stats_get(self._h, C.byref(st))
+        return {n: getattr(st, n) for n, _ in PdpdServerStats._fields_ if n != "pad"}
+
+    def kernel_launches(self):
+        return int(lib().pdpd_kernel_launches(lib().pdpd_server_engine(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pdpd_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
