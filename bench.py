@@ -273,7 +273,8 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "served_bead_steps_per_s": served, "wall_s": wall,
             "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
             "latency_max_s": st["latency_max_s"], "max_active_jobs": st["max_active"],
-            "repacks": st["repacks"] - st0["repacks"], "gpu_launches": launches,
+            "repacks": st["repacks"] - st0["repacks"],
+            "repack_s": st["repack_s"] - st0["repack_s"], "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,
             "served_vs_sequential_fp32": served / seq32, "served_vs_sequential_fp64": served / seq64}

@@ -249,6 +249,7 @@ typedef struct pdpd_server_stats {
     double busy_s;         /* wall time with at least one job admitted */
     double wall_s;         /* first submit to last completion */
     double latency_p50_s, latency_p99_s, latency_max_s;  /* submit -> final callback done */
+    double repack_s;       /* host wall time spent in re-packs */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.

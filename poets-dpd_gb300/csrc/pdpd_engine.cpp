@@ -39,11 +39,14 @@ double now_s()
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Device buffer that keeps its allocation while a request fits (bytes = capacity), so that a
+// re-attach of a batch of similar size allocates nothing.
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
     cudaError_t alloc(size_t n)
     {
+        if (p && n <= bytes) return cudaSuccess;
         release();
         if (n == 0) n = 16;
         cudaError_t e = cudaMalloc(&p, n);
@@ -100,9 +103,11 @@ const ConfigEntry kConfig[] = {
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
-    {"force_kernel", "FP32 force kernel: 0 = shared-memory brick with neighbour lists, "
+    {"force_kernel", "FP32 force kernel (default 6): 0 = shared-memory brick with neighbour lists, "
                      "1 = thread per bead from global memory, 2 = shared-memory brick, "
-                     "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence."},
+                     "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence, "
+                     "5 = warp per home cell, 6 = as 0 with the neighbour cells walked row by row, "
+                     "7 = as 6 with the lists evaluated balanced across lanes."},
     {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
@@ -127,7 +132,7 @@ struct pdpd_engine {
     int cfg_grid_blocks = 0;
     int cfg_graph_steps = 0;
     int cfg_use_graphs = 1;
-    int cfg_force_kernel = 0;
+    int cfg_force_kernel = 6;
     int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
     int cfg_autotune = 0;
     bool tuned = false;
@@ -177,6 +182,16 @@ struct pdpd_engine {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
         graph_steps = 0;
+    }
+
+    // Forget the attached batch but keep the device buffers for the next attach.
+    void reset()
+    {
+        drop_graph();
+        worlds.clear();
+        attached = false;
+        tuned = false;
+        n_beads = n_cells = n_tiles = 0;
     }
 
     void release()
@@ -304,7 +319,10 @@ struct pdpd_engine {
         // Staged-bead capacity: 1.5x the expected halo population of the densest world (at
         // most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
         a.brick_hc_max = (uint32_t)(cfg_brick[0] + 2) * (cfg_brick[1] + 2) * (cfg_brick[2] + 2);
-        double want = 1.5 * max_density * a.brick_hc_max + 64;
+        // staged-bead capacity: the mean halo population + 8 standard deviations (Poisson) and
+        // a floor of 1.25x the mean; a fuller brick takes the (bit-identical) global path
+        const double mean = max_density * a.brick_hc_max;
+        double want = std::max(mean + 8.0 * std::sqrt(mean), 1.25 * mean) + 32;
         a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
         int grid = 0;
         uint32_t bytes = 0;
@@ -324,8 +342,8 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
-        static const int cand[][4] = {{0, 4, 4, 4}, {0, 2, 4, 8}, {0, 4, 4, 8}, {0, 2, 2, 8},
-                                      {2, 4, 4, 4}, {3, 4, 4, 4}, {4, 2, 4, 8}, {1, 4, 4, 4}};
+        static const int cand[][4] = {{6, 2, 4, 4}, {6, 2, 2, 8}, {6, 4, 4, 4}, {6, 2, 4, 8},
+                                      {0, 2, 4, 4}, {0, 4, 4, 4}, {3, 2, 4, 4}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
         if (!cfg_autotune || tuned || fp64() || n_steps < (trial + 1) * n_cand + 1) return 0;
@@ -553,8 +571,9 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     double t0 = now_s();
     cudaSetDevice(e->device);
     cudaStreamSynchronize(e->stream);
-    // Resident re-pack: unsort the current arena into a device staging buffer first.
-    DevBuf snap;
+    // Resident re-pack: unsort the current arena into device staging buffer 1 first; the new
+    // batch is staged in buffer 0 and takes the kept worlds' rows from buffer 1.
+    const double *snap = nullptr;
     std::vector<uint32_t> old_base;
     bool any_kept = false;
     for (uint32_t i = 0; keep_old && i < n_worlds; i++) any_kept |= keep_old[i] >= 0;
@@ -563,26 +582,17 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         for (uint32_t i = 0; i < n_worlds; i++)
             if (keep_old[i] >= (int32_t)e->worlds.size())
                 return e->fail(PDPD_E_INVALID, "re-pack refers to a world that is not attached");
-        int rc = download(e, 0, e->stream);
+        int rc = download(e, 1, e->stream);
         if (rc) return rc;
-        cudaStreamSynchronize(e->stream);
-        snap.p = e->d_staging[0].p;
-        snap.bytes = e->d_staging[0].bytes;
-        e->d_staging[0].p = nullptr;
-        e->d_staging[0].bytes = 0;
+        snap = e->d_staging[1].as<double>();
         for (const WorldHost &wh : e->worlds) old_base.push_back(wh.dev.bead_base);
     }
-    struct SnapGuard {  // freed on every return; cudaFree waits for the copies reading it
-        DevBuf &b;
-        ~SnapGuard() { b.release(); }
-    } snap_guard{snap};
-    e->release();
+    e->reset();
     char reason[256];
     uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
     for (uint32_t i = 0; i < n_worlds; i++) {
         const bool kept = keep_old && keep_old[i] >= 0;
         int rc = check_world(&ws[i], reason, sizeof reason, !kept);
-        if (rc) snap.release();
         if (rc) return e->fail(rc, "world %u: %s", i, reason);
         nb += ws[i].n_beads;
         nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
@@ -783,7 +793,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     for (uint32_t i = 0; any_kept && i < n_worlds; i++) {
         if (keep_old[i] < 0 || ws[i].n_beads == 0 || ce != cudaSuccess) continue;
         ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
-                             snap.as<double>() + 9 * (size_t)old_base[keep_old[i]],
+                             snap + 9 * (size_t)old_base[keep_old[i]],
                              sizeof(double) * 9 * ws[i].n_beads, cudaMemcpyDeviceToDevice, s);
     }
     H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
@@ -911,10 +921,8 @@ void *pdpd_stream(pdpd_engine *e)
 static int download(pdpd_engine *e, int buf, cudaStream_t s)
 {
     KArgs a = e->args;
-    if (!e->d_staging[buf].p) {
-        cudaError_t ce = e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads);
-        if (ce != cudaSuccess) return e->fail(PDPD_E_NOMEM, "staging allocation failed");
-    }
+    if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "staging allocation failed");
     a.staging = e->d_staging[buf].as<double>();
     e->launches += e->fp64() ? launch_unsort64(a, s) : launch_unsort32(a, s);
     return PDPD_OK;
@@ -971,7 +979,7 @@ int pdpd_run_intervals(pdpd_engine *e, int32_t interval_count, uint32_t interval
     const uint32_t n = wd0.n_beads;
     const size_t nbytes = sizeof(double) * 9 * (size_t)n;
     for (int b = 0; b < 2; b++) {
-        if (!e->d_staging[b].p && e->d_staging[b].alloc(nbytes) != cudaSuccess)
+        if (e->d_staging[b].alloc(nbytes) != cudaSuccess)
             return e->fail(PDPD_E_NOMEM, "staging allocation failed");
         if (e->h_staging[b].alloc(nbytes + sizeof(WorldDev)) != cudaSuccess)
             return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
@@ -1079,7 +1087,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
     else if (k == "force_kernel") {
-        if (v > 5) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..5");
+        if (v > 7) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..7");
         e->cfg_force_kernel = (int)v;
     } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {
         int idx = k == "brick_x" ? 0 : (k == "brick_y" ? 1 : 2);
@@ -1303,7 +1311,9 @@ struct ServerJob {
     double t_submit = 0;
     size_t bytes = 0;
     int slot = -1;           // world index in the attached batch, -1 before the first attach
-    bool stopped = false;    // the callback asked to stop
+    bool stopped = false;    // no further callbacks: the callback asked to stop, or it failed
+    bool ended = false;      // final state delivered or owed; the world leaves the batch at the
+                             // next point where every running job is at an interval boundary
 };
 
 // A callback owed for one job: its rows start at `row` in host snapshot buffer `buf`.
@@ -1378,8 +1388,10 @@ int pdpd_server::repack()
         descs.push_back(d);
         keep.push_back(j->slot);
     }
+    const double t0 = now_s();
     int rc = attach_impl(eng, descs.data(), (uint32_t)descs.size(), keep.data());
     if (rc) return rc;
+    const double t_repack = now_s() - t0;
     for (size_t i = 0; i < active.size(); i++) {
         ServerJob &j = *active[i];
         if (j.slot < 0) {  // the initial state lives on the device from now on
@@ -1392,6 +1404,7 @@ int pdpd_server::repack()
     }
     std::lock_guard<std::mutex> lk(mu);
     st.repacks++;
+    st.repack_s += t_repack;
     return PDPD_OK;
 }
 
@@ -1421,7 +1434,7 @@ void pdpd_server::deliver()
         if (d.final_state) {
             finish_job(j);
         } else if (!go && !j.stopped) {  // the job ends at this snapshot
-            j.stopped = true;
+            j.stopped = j.ended = true;
             finish_job(j);
         }
     }
@@ -1429,18 +1442,22 @@ void pdpd_server::deliver()
     retiring.clear();
 }
 
+// Jobs whose world raised an error flag: a running job gets a failure callback; every one
+// leaves the batch at the next iteration.
 void pdpd_server::fail_jobs(const std::vector<ServerJob *> &jobs, int code)
 {
     for (ServerJob *j : jobs) {
-        if (j->cb && !j->stopped) j->cb(j->user, j->id, j->t, nullptr, nullptr, nullptr, 0, 0, -code);
-        j->stopped = true;
+        const bool running = !j->ended;
+        j->stopped = j->ended = true;
+        if (!running) continue;  // an ended job's world kept stepping only to fill the epoch
+        if (j->cb) j->cb(j->user, j->id, j->t, nullptr, nullptr, nullptr, 0, 0, -code);
         std::lock_guard<std::mutex> lk(mu);
         st.jobs_failed++;
         status = code;
         err = eng->err;
     }
     for (size_t i = 0; i < active.size();)
-        if (active[i]->stopped) {
+        if (std::find(jobs.begin(), jobs.end(), active[i].get()) != jobs.end()) {
             retiring.push_back(std::move(active[i]));
             active.erase(active.begin() + i);
             changed = true;
@@ -1458,34 +1475,35 @@ void pdpd_server::run()
             std::unique_lock<std::mutex> lk(mu);
             cv.wait(lk, [&] { return stop || !pending.empty() || !active.empty() || !owed.empty(); });
             if (stop && pending.empty() && active.empty() && owed.empty()) break;
-            // Admission only where every running job is at one of its interval boundaries: the
-            // jobs' intervals then stay in phase and epochs are whole intervals (a job that
-            // ends mid-interval splits one epoch in two).
-            size_t used = 0;
+            // Membership changes only where every running job is at one of its interval
+            // boundaries: the jobs' intervals stay in phase, epochs are whole intervals (a job
+            // that ends mid-interval splits one epoch in two, with no re-pack), and ended jobs
+            // leave and waiting jobs join in one re-pack.
             bool in_phase = true;
-            for (auto &j : active) {
-                used += j->bytes;
-                in_phase &= j->done % interval == 0;
-            }
-            while (in_phase && !pending.empty() && (active.empty() || used + pending.front()->bytes <= budget)) {
-                used += pending.front()->bytes;
-                active.push_back(std::move(pending.front()));
-                pending.pop_front();
-                changed = true;
+            for (auto &j : active)
+                if (!j->ended) in_phase &= j->done % interval == 0;
+            if (in_phase) {
+                for (size_t i = 0; i < active.size();)
+                    if (active[i]->ended) {
+                        retiring.push_back(std::move(active[i]));
+                        active.erase(active.begin() + i);
+                        changed = true;
+                    } else {
+                        i++;
+                    }
+                size_t used = 0;
+                for (auto &j : active) used += j->bytes;
+                while (!pending.empty() && (active.empty() || used + pending.front()->bytes <= budget)) {
+                    used += pending.front()->bytes;
+                    active.push_back(std::move(pending.front()));
+                    pending.pop_front();
+                    changed = true;
+                }
             }
             if (!busy) t_busy_from = now_s();
             busy = true;
             st.max_active = std::max<uint32_t>(st.max_active, (uint32_t)active.size());
         }
-        // jobs whose callback asked to stop leave before the next epoch
-        for (size_t i = 0; i < active.size();)
-            if (active[i]->stopped) {
-                retiring.push_back(std::move(active[i]));
-                active.erase(active.begin() + i);
-                changed = true;
-            } else {
-                i++;
-            }
         if (changed) deliver();  // the re-pack needs the snapshot buffers and the old arena
         int rc = repack();
         if (rc != PDPD_OK) {
@@ -1496,15 +1514,16 @@ void pdpd_server::run()
             changed = false;
         }
         std::vector<Delivery> next;
-        uint32_t epoch = 0;
-        if (!active.empty()) {
-            epoch = UINT32_MAX;
-            for (auto &j : active)
-                epoch = std::min({epoch, interval - j->done % interval, j->n_steps - j->done});
+        uint32_t epoch = UINT32_MAX;
+        for (auto &j : active)
+            if (!j->ended) epoch = std::min({epoch, interval - j->done % interval, j->n_steps - j->done});
+        if (epoch == UINT32_MAX) epoch = 0;  // only ended jobs: they leave at the next iteration
+        if (epoch > 0) {
             rc = pdpd_run_async(eng, epoch);
             std::vector<size_t> at_boundary;
             for (size_t i = 0; i < active.size(); i++) {
                 ServerJob &j = *active[i];
+                if (j.ended) continue;
                 j.done += epoch;
                 j.t += epoch;
                 if (j.done % interval == 0 || j.done == j.n_steps) at_boundary.push_back(i);
@@ -1533,7 +1552,7 @@ void pdpd_server::run()
             }
         }
         deliver();  // host callbacks of the previous epoch while this one computes
-        if (!active.empty()) {
+        if (epoch > 0) {
             if (rc == PDPD_OK) rc = pdpd_sync(eng);
             if (rc == PDPD_E_BOND_SNAPPED || rc == PDPD_E_BEAD_LOST) {
                 // worlds are independent: fail the ones that raised an error flag, keep the rest
@@ -1542,8 +1561,10 @@ void pdpd_server::run()
                 for (auto &j : active)
                     if (wd[j->slot].err) bad.push_back(j.get());
                 fail_jobs(bad, rc);
-                next.erase(std::remove_if(next.begin(), next.end(), [](const Delivery &d) { return d.job->stopped; }),
+                next.erase(std::remove_if(next.begin(), next.end(),
+                                          [](const Delivery &d) { return d.job->stopped; }),
                            next.end());
+                rc = PDPD_OK;
             } else if (rc != PDPD_OK) {
                 std::vector<ServerJob *> all;
                 for (auto &j : active) all.push_back(j.get());
@@ -1555,19 +1576,14 @@ void pdpd_server::run()
             }
             {
                 std::lock_guard<std::mutex> lk(mu);
-                for (auto &j : active) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
+                for (auto &j : active)
+                    if (!j->ended) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
             }
+            for (auto &j : active)
+                if (j->done == j->n_steps) j->ended = true;  // final state is owed
             owed.swap(next);
             owed_buf = b;
             b ^= 1;
-            for (size_t i = 0; i < active.size();)
-                if (active[i]->done == active[i]->n_steps) {
-                    retiring.push_back(std::move(active[i]));
-                    active.erase(active.begin() + i);
-                    changed = true;
-                } else {
-                    i++;
-                }
         }
         if (active.empty() && owed.empty()) {
             repack();  // releases the arena

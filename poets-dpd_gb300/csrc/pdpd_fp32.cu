@@ -582,8 +582,8 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
         *smem_bytes = C.bytes;
         return 0;
     }
-    const int list = (variant == 0 || variant == 3) ? 1 : 0;
-    const BrickLayout L = brick_layout(hc_max, maxb, list);
+    const BrickLayout L = brick_layout(hc_max, maxb, brick_variant_has_list(variant),
+                                       brick_variant_balanced(variant));
     const int bytes = (int)L.bytes;
     void (*k0)(KArgs, BrickLayout) = nullptr;
     void (*k1)(KArgs, BrickLayout) = nullptr;
@@ -591,6 +591,8 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
     case 0: k0 = k_force32_brick<0, 1, 0>; k1 = k_force32_brick<1, 1, 0>; break;
     case 2: k0 = k_force32_brick<0, 0, 0>; k1 = k_force32_brick<1, 0, 0>; break;
     case 3: k0 = k_force32_brick<0, 1, 1>; k1 = k_force32_brick<1, 1, 1>; break;
+    case 6: k0 = k_force32_brick<0, 1, 2>; k1 = k_force32_brick<1, 1, 2>; break;
+    case 7: k0 = k_force32_brick<0, 1, 3>; k1 = k_force32_brick<1, 1, 3>; break;
     default: k0 = k_force32_brick<0, 0, 1>; k1 = k_force32_brick<1, 0, 1>; break;
     }
     cudaError_t e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -628,14 +630,16 @@ static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
     }
     if (a.force_kernel != 1 && a.n_bricks > 0) {
         const int v = a.force_kernel;
-        const int list = (v == 0 || v == 3) ? 1 : 0;
-        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, list);
+        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, brick_variant_has_list(v),
+                                           brick_variant_balanced(v));
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
         void (*k)(KArgs, BrickLayout);
         switch (v) {
         case 0: k = final_step ? k_force32_brick<1, 1, 0> : k_force32_brick<0, 1, 0>; break;
         case 2: k = final_step ? k_force32_brick<1, 0, 0> : k_force32_brick<0, 0, 0>; break;
         case 3: k = final_step ? k_force32_brick<1, 1, 1> : k_force32_brick<0, 1, 1>; break;
+        case 6: k = final_step ? k_force32_brick<1, 1, 2> : k_force32_brick<0, 1, 2>; break;
+        case 7: k = final_step ? k_force32_brick<1, 1, 3> : k_force32_brick<0, 1, 3>; break;
         default: k = final_step ? k_force32_brick<1, 0, 1> : k_force32_brick<0, 0, 1>; break;
         }
         k<<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);

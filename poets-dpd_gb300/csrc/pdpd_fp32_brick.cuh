@@ -34,10 +34,21 @@ struct BrickHeader {
 // list[BLIST_MAX][BRICK_THREADS].
 struct BrickLayout {
     uint32_t hc_max, maxb;
-    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_list, bytes;
+    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_list, off_bal, bytes;
 };
 
-__host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, int with_list)
+// Balanced list evaluation (variant 7): per pass of BRICK_THREADS home beads, the list
+// lengths are counting-sorted so that each warp evaluates lists of similar length.
+struct BrickBalance {
+    uint32_t hist[BLIST_MAX + 2];   // length histogram, then its exclusive prefix
+    uint16_t perm[BRICK_THREADS];   // evaluation lane -> list owner (thread)
+    uint16_t n[BRICK_THREADS];      // list length of each owner
+    uint32_t si[BRICK_THREADS];     // staged index of each owner's home bead
+    float f[3][BRICK_THREADS];      // each owner's force (partial sums of flushed entries in)
+};
+
+__host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, int with_list,
+                                                    int with_balance = 0)
 {
     BrickLayout L;
     L.hc_max = hc_max;
@@ -54,22 +65,36 @@ __host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t ma
     off += 16 * maxb;
     L.off_list = off;
     if (with_list) off += 2 * BLIST_MAX * BRICK_THREADS;
+    off = (off + 15) & ~15u;
+    L.off_bal = off;
+    if (with_balance) off += (uint32_t)sizeof(BrickBalance);
     L.bytes = off;
     return L;
 }
 
+// Brick variants (force_kernel) that keep per-thread neighbour lists in shared memory, and
+// the one that evaluates them balanced across lanes.
+inline int brick_variant_has_list(int variant)
+{
+    return (variant == 0 || variant == 3 || variant == 6 || variant == 7) ? 1 : 0;
+}
+inline int brick_variant_balanced(int variant)
+{
+    return variant == 7 ? 1 : 0;
+}
+
 // Evaluate list entries [0, n) of this thread in order, adding to F.
-__device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
-                                                const float4 *__restrict__ svel,
-                                                const uint16_t *__restrict__ list, int n,
-                                                const float4 pi, const float4 vi,
-                                                const float2 *pair, uint32_t nt, uint32_t th_lo,
-                                                uint32_t th_hi, float scale, float F[3])
+__device__ __forceinline__ void brick_list_eval_col(const float4 *__restrict__ spos,
+                                                    const float4 *__restrict__ svel,
+                                                    const uint16_t *__restrict__ list, int col, int n,
+                                                    const float4 pi, const float4 vi,
+                                                    const float2 *pair, uint32_t nt, uint32_t th_lo,
+                                                    uint32_t th_hi, float scale, float F[3])
 {
     const uint32_t hi = __float_as_uint(pi.w);
     const uint32_t ti = min(hi >> 28, nt - 1u);
     for (int k = 0; k < n; k++) {
-        const uint32_t e = list[k * BRICK_THREADS + threadIdx.x];
+        const uint32_t e = list[k * BRICK_THREADS + col];
         const uint32_t j = e & 2047u, d = e >> 11;  // d = (dx+1)*9 + (dy+1)*3 + (dz+1)
         const float4 pj = spos[j];
         const float ax = __fsub_rn(pi.x, (float)((int)(d / 9u) - 1));
@@ -81,6 +106,17 @@ __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
         pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj, pair[ti * nt + min(hj >> 28, nt - 1u)],
                         th_lo, th_hi, scale, F);
     }
+}
+
+// This thread's own list (column threadIdx.x).
+__device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
+                                                const float4 *__restrict__ svel,
+                                                const uint16_t *__restrict__ list, int n,
+                                                const float4 pi, const float4 vi,
+                                                const float2 *pair, uint32_t nt, uint32_t th_lo,
+                                                uint32_t th_hi, float scale, float F[3])
+{
+    brick_list_eval_col(spos, svel, list, threadIdx.x, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
 // Pair forces of one staged home bead, with the 27 neighbour cells walked as one flat
@@ -153,6 +189,180 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
     if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
+// Halo setup and staging of one brick, block-wide (ends with __syncthreads):
+//   hstart[hc] = first staged index of halo cell hc (hc = (hx * HY + hy) * HZ + hz, z fastest),
+//   hstart[HC] = total, hslot[hc] = its first slot in the sorted state,
+//   H.home_rows[r] = first home index of home (x, y) row r, and, if the halo fits in maxb,
+//   spos / svel = the halo's beads.  Halo coordinates lie in [-1, L] (bricks are cut at the
+//   box faces), so each wraps with one conditional add or subtract.
+__device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const WorldDev &w, const Brick &br,
+                                                     BrickHeader &H, uint32_t *hstart, uint32_t *hslot,
+                                                     float4 *spos, float4 *svel, uint32_t maxb,
+                                                     uint32_t &total, uint32_t &n_home)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
+    const int HC = HX * HY * HZ;
+    const int L0 = w.L[0], L1 = w.L[1], L2 = w.L[2];
+
+    // counts of a contiguous range of halo cells per thread, then a block exclusive scan
+    const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
+    const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
+    uint32_t tsum = 0;
+    if (hc_begin < hc_end) {
+        int hx = hc_begin / (HY * HZ);
+        const int rem = hc_begin - hx * HY * HZ;
+        int hy = rem / HZ, hz = rem - (rem / HZ) * HZ;
+        for (int hc = hc_begin; hc < hc_end; hc++) {
+            int gx = br.x0 - 1 + hx, gy = br.y0 - 1 + hy, gz = br.z0 - 1 + hz;
+            gx += gx < 0 ? L0 : 0;
+            gx -= gx >= L0 ? L0 : 0;
+            gy += gy < 0 ? L1 : 0;
+            gy -= gy >= L1 ? L1 : 0;
+            gz += gz < 0 ? L2 : 0;
+            gz -= gz >= L2 ? L2 : 0;
+            const uint32_t c = w.cell_base + ((uint32_t)gx * (uint32_t)L1 + (uint32_t)gy) * (uint32_t)L2 + (uint32_t)gz;
+            const uint32_t s0 = a.start[c];
+            const uint32_t n = a.start[c + 1] - s0;
+            hslot[hc] = s0;
+            hstart[hc] = n;  // count for now
+            tsum += n;
+            if (++hz == HZ) {
+                hz = 0;
+                if (++hy == HY) {
+                    hy = 0;
+                    ++hx;
+                }
+            }
+        }
+    }
+    uint32_t inc = tsum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += y;
+    }
+    if (lane == 31) H.wsum[warp] = inc;
+    __syncthreads();
+    uint32_t run = inc - tsum, tot = 0;
+    for (int k = 0; k < BRICK_WARPS; k++) {
+        if (k < warp) run += H.wsum[k];
+        tot += H.wsum[k];
+    }
+    for (int hc = hc_begin; hc < hc_end; hc++) {
+        const uint32_t n = hstart[hc];
+        hstart[hc] = run;
+        run += n;
+    }
+    if (tid == 0) hstart[HC] = tot;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t acc = 0;
+        for (int r = 0; r < br.bx * br.by; r++) {
+            H.home_rows[r] = acc;
+            const int lx = r / br.by, ly = r - lx * br.by;
+            const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+            acc += hstart[hc0 + br.bz] - hstart[hc0];
+        }
+        H.home_rows[br.bx * br.by] = acc;
+    }
+    // staging, one (x, y) halo row per warp iteration (coalesced); a row whose z range does not
+    // wrap is one contiguous run of slots
+    if (tot <= maxb) {
+        const bool zrun = br.z0 >= 1 && br.z0 + br.bz + 1 <= L2;
+        for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
+            const int hc0 = row * HZ;
+            const uint32_t base = hstart[hc0];
+            const uint32_t len = hstart[hc0 + HZ] - base;
+            for (uint32_t k = lane; k < len; k += 32) {
+                uint32_t slot;
+                if (zrun) {
+                    slot = hslot[hc0] + k;
+                } else {
+                    int z = 0;
+                    while (hstart[hc0 + z + 1] - base <= k) z++;
+                    slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
+                }
+                spos[base + k] = ((const float4 *)a.posA)[slot];
+                svel[base + k] = ((const float4 *)a.velA)[slot];
+            }
+        }
+    }
+    __syncthreads();
+    total = tot;
+    n_home = H.home_rows[br.bx * br.by];
+}
+
+
+// Row walk of one staged home bead (force variants 6 and 7): the 9 neighbour rows (dx, dy) in order;
+// a row's 3 cells (dz = -1, 0, +1) are one contiguous range of staged beads, trimmed at its
+// ends by the same conservative test as the per-cell loop.  The warp pays the longest row of
+// its lanes 9 times instead of the longest cell 27 times.  The in-range candidates go to this
+// thread's list in the direction order (a full list is evaluated into F first); returns the
+// number of entries left in the list.
+__device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spos,
+                                                  const float4 *__restrict__ svel,
+                                                  uint16_t *__restrict__ list, int cap,
+                                                  const uint32_t *__restrict__ hstart, int HY, int HZ,
+                                                  int hx, int hy, int hz, const float4 pi,
+                                                  const float4 vi, const float2 *pair, uint32_t nt,
+                                                  uint32_t th_lo, uint32_t th_hi, float scale,
+                                                  float F[3])
+{
+    const float PRUNE = 1.0001f;
+    const float min2 = min_dist_sqr_f();
+    const float azm = __fsub_rn(pi.z, -1.0f), azp = __fsub_rn(pi.z, 1.0f);
+    const float gzm = pi.z, gzp = 1.0f - pi.z;
+    int n = 0;
+#pragma unroll 1
+    for (int rr = 0; rr < 9; rr++) {
+        const int ddx = rr / 3 - 1, ddy = rr - (rr / 3) * 3 - 1;
+        const float gx = slab_gap(pi.x, ddx), gy = slab_gap(pi.y, ddy);
+        const float gxy = gx * gx + gy * gy;
+        if (gxy >= PRUNE) continue;
+        const int rowc = ((hx + ddx) * HY + (hy + ddy)) * HZ + hz;
+        const uint32_t c1 = hstart[rowc], c2 = hstart[rowc + 1];
+        const uint32_t j0 = gxy + gzm * gzm >= PRUNE ? c1 : hstart[rowc - 1];
+        const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : hstart[rowc + 2];
+        const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
+        const uint32_t dbase = (uint32_t)(rr * 3) << 11;
+        for (uint32_t j = j0; j < j1; j++) {
+            const float4 pj = spos[j];
+            const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
+            float dx, dy, dz;
+            const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+            if (r2 < 1.0f && r2 >= min2) {
+                if (n == cap) {
+                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    n = 0;
+                }
+                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
+                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                n++;
+            }
+        }
+    }
+    return n;
+}
+
+
+// One home bead of a brick whose halo does not fit in shared memory: pair forces gathered
+// from global memory in the same order, then integration.  Its accumulators are its own, so
+// the hot path's never have their address taken (they stay in registers).
+template <int FINAL>
+__device__ __forceinline__ void brick_fallback_bead(const KArgs &a, const WorldDev &w, const float2 *pair,
+                                                 uint32_t th_lo, uint32_t th_hi, float scale,
+                                                 uint32_t s, uint32_t &err)
+{
+    const float4 ph = ((const float4 *)a.posA)[s];
+    const float4 vh = ((const float4 *)a.velA)[s];
+    int c[3];
+    decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+    float F[3] = {0.f, 0.f, 0.f};
+    pair_forces32_seq(a, w, pair, th_lo, th_hi, scale, c, ph, vh, F);
+    integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
+}
+
 template <int FINAL, int LIST, int FLAT>
 __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickLayout lay)
 {
@@ -178,79 +388,93 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
         const float scale = (float)w.scale_inv_sqrt_dt;
         const uint64_t th = t_hash((uint32_t)w.t, w.seed);
         const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
-        const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
-        const int HC = HX * HY * HZ;
+        const int HY = br.by + 2, HZ = br.bz + 2;
 
-        // ---- 1. halo cells: first global slot and count; block exclusive scan -> hstart
-        const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
-        const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
-        uint32_t tsum = 0;
-        for (int hc = hc_begin; hc < hc_end; hc++) {
-            const int hx = hc / (HY * HZ), rem = hc - hx * HY * HZ;
-            const int hy = rem / HZ, hz = rem - hy * HZ;
-            const int gx = wrap_index(br.x0 - 1 + hx, w.L[0]);
-            const int gy = wrap_index(br.y0 - 1 + hy, w.L[1]);
-            const int gz = wrap_index(br.z0 - 1 + hz, w.L[2]);
-            const uint32_t c = w.cell_base + ((uint32_t)gx * (uint32_t)w.L[1] + (uint32_t)gy) * (uint32_t)w.L[2] + (uint32_t)gz;
-            const uint32_t s0 = a.start[c];
-            const uint32_t n = a.start[c + 1] - s0;
-            hslot[hc] = s0;
-            hstart[hc] = n;  // count for now
-            tsum += n;
-        }
-        uint32_t inc = tsum;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
-            if (lane >= off) inc += y;
-        }
-        if (lane == 31) H.wsum[warp] = inc;
-        __syncthreads();
-        uint32_t run = inc - tsum, total = 0;
-        for (int k = 0; k < BRICK_WARPS; k++) {
-            if (k < warp) run += H.wsum[k];
-            total += H.wsum[k];
-        }
-        for (int hc = hc_begin; hc < hc_end; hc++) {
-            const uint32_t n = hstart[hc];
-            hstart[hc] = run;
-            run += n;
-        }
-        if (tid == 0) hstart[HC] = total;
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t acc = 0;
-            for (int r = 0; r < br.bx * br.by; r++) {
-                H.home_rows[r] = acc;
-                const int lx = r / br.by, ly = r - lx * br.by;
-                const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
-                acc += hstart[hc0 + br.bz] - hstart[hc0];
-            }
-            H.home_rows[br.bx * br.by] = acc;
-        }
-        __syncthreads();
-        const uint32_t n_home = H.home_rows[br.bx * br.by];
+        // ---- 1-2. halo cells (hstart, hslot, home rows) and staging
+        uint32_t total = 0, n_home = 0;
+        brick_halo_and_stage(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
         const bool staged = total <= lay.maxb;
-
-        // ---- 2. stage the halo, one (x, y) halo row per warp iteration (coalesced)
-        if (staged) {
-            for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
-                const int hc0 = row * HZ;
-                const uint32_t base = hstart[hc0];
-                const uint32_t len = hstart[hc0 + HZ] - base;
-                for (uint32_t k = lane; k < len; k += 32) {
-                    int z = 0;
-                    while (hstart[hc0 + z + 1] - base <= k) z++;
-                    const uint32_t slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
-                    spos[base + k] = ((const float4 *)a.posA)[slot];
-                    svel[base + k] = ((const float4 *)a.velA)[slot];
-                }
-            }
-        }
-        __syncthreads();
 
         // ---- 3. one thread per home bead: pair forces, bonds, integration
         uint32_t err = 0;
+        if (FLAT == 3 && staged) {
+            // Variant 7, per pass of BRICK_THREADS home beads: (a) each thread walks the rows of
+            // its bead into its list; (b) the lists are counting-sorted by length and lane l
+            // evaluates list perm[l], so a warp's lanes run lists of about the same length; (c)
+            // each thread integrates its own bead.  Every list is still summed by one thread
+            // in its own order: the forces are those of the other variants, bit for bit.
+            BrickBalance &B = *reinterpret_cast<BrickBalance *>(smem_raw + lay.off_bal);
+            for (uint32_t t0 = 0; t0 < n_home; t0 += BRICK_THREADS) {
+                const uint32_t t = t0 + tid;
+                const bool act = t < n_home;
+                float F[3] = {0.f, 0.f, 0.f};
+                int n = 0, lx = 0, ly = 0, z = 0;
+                uint32_t s = 0, si = 0;
+                float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = pi;
+                if (act) {
+                    int r = 0;
+                    while (H.home_rows[r + 1] <= t) r++;
+                    lx = r / br.by;
+                    ly = r - lx * br.by;
+                    const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+                    const uint32_t k = t - H.home_rows[r];
+                    s = hslot[hc0] + k;
+                    si = hstart[hc0] + k;
+                    while (hstart[hc0 + z + 1] <= si) z++;
+                    pi = spos[si];
+                    vi = svel[si];
+                    n = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, lx + 1, ly + 1, z + 1,
+                                           pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+                }
+                if (tid < BLIST_MAX + 2) B.hist[tid] = 0u;
+                B.n[tid] = (uint16_t)n;
+                B.si[tid] = si;
+                B.f[0][tid] = F[0];
+                B.f[1][tid] = F[1];
+                B.f[2][tid] = F[2];
+                __syncthreads();
+                const uint32_t rank = atomicAdd(&B.hist[n], 1u);  // n <= BLIST_MAX
+                __syncthreads();
+                if (warp == 0) {  // exclusive prefix of the BLIST_MAX + 1 bins
+                    const uint32_t v = B.hist[lane];
+                    uint32_t inc = v;
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+                        if (lane >= off) inc += y;
+                    }
+                    B.hist[lane] = inc - v;
+                    if (lane == 31) B.hist[32] = inc;
+                }
+                __syncthreads();
+                B.perm[B.hist[n] + rank] = (uint16_t)tid;
+                __syncthreads();
+                {
+                    const uint32_t o = B.perm[tid];
+                    const int no = B.n[o];
+                    if (no > 0) {
+                        const uint32_t so = B.si[o];
+                        float G[3] = {B.f[0][o], B.f[1][o], B.f[2][o]};
+                        brick_list_eval_col(spos, svel, list, (int)o, no, spos[so], svel[so], H.pair, nt,
+                                            th_lo, th_hi, scale, G);
+                        B.f[0][o] = G[0];
+                        B.f[1][o] = G[1];
+                        B.f[2][o] = G[2];
+                    }
+                }
+                __syncthreads();
+                if (act) {
+                    F[0] = B.f[0][tid];
+                    F[1] = B.f[1][tid];
+                    F[2] = B.f[2][tid];
+                    const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
+                    integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
+                }
+                if (t0 + BRICK_THREADS < n_home) __syncthreads();  // the lists are reused
+            }
+            if (err) atomicOr(&a.worlds[br.world].err, err);
+            continue;
+        }
         for (uint32_t t = tid; t < n_home; t += BRICK_THREADS) {
             int r = 0;
             while (H.home_rows[r + 1] <= t) r++;
@@ -259,17 +483,11 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             const int hc0 = (hx * HY + hy) * HZ + 1;
             const uint32_t k = t - H.home_rows[r];
             const uint32_t s = hslot[hc0] + k;
-            float F[3] = {0.f, 0.f, 0.f};
-            if (!staged) {
-                // Halo larger than the shared-memory budget: gather from global memory.
-                const float4 ph = ((const float4 *)a.posA)[s];
-                const float4 vh = ((const float4 *)a.velA)[s];
-                int c[3];
-                decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-                pair_forces32_seq(a, w, H.pair, th_lo, th_hi, scale, c, ph, vh, F);
-                integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
+            if (!staged) {  // halo larger than the shared-memory budget: gather from global memory
+                brick_fallback_bead<FINAL>(a, w, H.pair, th_lo, th_hi, scale, s, err);
                 continue;
             }
+            float F[3] = {0.f, 0.f, 0.f};
             const uint32_t si = hstart[hc0] + k;
             int z = 0;
             while (hstart[hc0 + z + 1] <= si) z++;
@@ -278,6 +496,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             const uint32_t hi = __float_as_uint(pi.w);
             const uint32_t ti = min(hi >> 28, nt - 1u);
             int n = 0;
+            if (FLAT >= 2) {  // variant 6 (and 7 when not staged, never reached)
+                const int nl = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi,
+                                                  vi, H.pair, nt, th_lo, th_hi, scale, F);
+                brick_list_eval(spos, svel, list, nl, pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+                const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
+                integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
+                continue;
+            }
             if (FLAT) {
                 brick_gather_flat<LIST>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi, vi,
                                         H.pair, nt, th_lo, th_hi, scale, F);
@@ -455,74 +681,12 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
         const float scale = (float)w.scale_inv_sqrt_dt;
         const uint64_t th = t_hash((uint32_t)w.t, w.seed);
         const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
-        const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
-        const int HC = HX * HY * HZ;
+        const int HY = br.by + 2, HZ = br.bz + 2;
 
-        // ---- halo cells and staging (as in k_force32_brick)
-        const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
-        const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
-        uint32_t tsum = 0;
-        for (int hc = hc_begin; hc < hc_end; hc++) {
-            const int hx = hc / (HY * HZ), rem = hc - hx * HY * HZ;
-            const int hy = rem / HZ, hz = rem - hy * HZ;
-            const int gx = wrap_index(br.x0 - 1 + hx, w.L[0]);
-            const int gy = wrap_index(br.y0 - 1 + hy, w.L[1]);
-            const int gz = wrap_index(br.z0 - 1 + hz, w.L[2]);
-            const uint32_t c = w.cell_base + ((uint32_t)gx * (uint32_t)w.L[1] + (uint32_t)gy) * (uint32_t)w.L[2] + (uint32_t)gz;
-            const uint32_t s0 = a.start[c];
-            const uint32_t n = a.start[c + 1] - s0;
-            hslot[hc] = s0;
-            hstart[hc] = n;
-            tsum += n;
-        }
-        uint32_t inc = tsum;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
-            if (lane >= off) inc += y;
-        }
-        if (lane == 31) H.wsum[warp] = inc;
-        __syncthreads();
-        uint32_t run = inc - tsum, total = 0;
-        for (int k = 0; k < BRICK_WARPS; k++) {
-            if (k < warp) run += H.wsum[k];
-            total += H.wsum[k];
-        }
-        for (int hc = hc_begin; hc < hc_end; hc++) {
-            const uint32_t n = hstart[hc];
-            hstart[hc] = run;
-            run += n;
-        }
-        if (tid == 0) hstart[HC] = total;
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t acc = 0;
-            for (int r = 0; r < br.bx * br.by; r++) {
-                H.home_rows[r] = acc;
-                const int lx = r / br.by, ly = r - lx * br.by;
-                const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
-                acc += hstart[hc0 + br.bz] - hstart[hc0];
-            }
-            H.home_rows[br.bx * br.by] = acc;
-        }
-        __syncthreads();
-        const uint32_t n_home = H.home_rows[br.bx * br.by];
+        // ---- 1-2. halo cells (hstart, hslot, home rows) and staging
+        uint32_t total = 0, n_home = 0;
+        brick_halo_and_stage(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
         const bool staged = total <= lay.maxb;
-        if (staged) {
-            for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
-                const int hc0 = row * HZ;
-                const uint32_t base = hstart[hc0];
-                const uint32_t len = hstart[hc0 + HZ] - base;
-                for (uint32_t k = lane; k < len; k += 32) {
-                    int z = 0;
-                    while (hstart[hc0 + z + 1] - base <= k) z++;
-                    const uint32_t slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
-                    spos[base + k] = ((const float4 *)a.posA)[slot];
-                    svel[base + k] = ((const float4 *)a.velA)[slot];
-                }
-            }
-        }
-        __syncthreads();
 
         // ---- pair forces: one warp per home cell
         if (staged) {

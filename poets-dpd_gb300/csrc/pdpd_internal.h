@@ -50,8 +50,8 @@ struct Brick {
     uint32_t pad;
 };
 
-// Default brick shape (cells); bx * by <= 64.
-constexpr int BRICK_X = 4, BRICK_Y = 4, BRICK_Z = 4;
+// Default brick shape (cells), the autotuner's usual pick on GB300; bx * by <= 64.
+constexpr int BRICK_X = 2, BRICK_Y = 4, BRICK_Z = 4;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
@@ -106,8 +106,10 @@ struct KArgs {
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
-    int force_kernel;    // FP32: 0 = brick kernel with neighbour lists, 2 = brick kernel,
-                         // 1 = thread per bead from global memory
+    int force_kernel;    // FP32: 6 (default) = brick kernel, neighbour lists, row walk;
+                         // 0 = as 6 with a cell walk, 2 = brick kernel without lists,
+                         // 3 / 4 = flat walk, 5 = warp per cell, 7 = as 6, balanced lists,
+                         // 1 = thread per bead (global)
     int brick_grid;      // persistent grid size of the brick kernel
     uint32_t brick_hc_max;  // halo cells of the nominal brick shape
     uint32_t brick_maxb;    // staged-bead capacity of one brick
