@@ -340,7 +340,7 @@ def run_engine_arm(args):
 
     # --- autotune once (its trials are ordinary steps: the trajectory does not depend on the
     # choice), then fix the chosen kernel and brick shape for every measurement below
-    if args.precision == "fp32":
+    if args.precision == "fp32" and args.autotune:
         eng.SetConfigEntry("autotune", 1)
         eng.Attach(world.copy())
         eng.run_async(64)
@@ -469,6 +469,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 512-state batched grid (FP32 batched vs FP64 plain)")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: autotune the FP32 force kernel first (default); 0: default kernel")
     ap.add_argument("--serving-window", type=float, default=4.0,
                     help="seconds of Poisson arrivals of the serving stream (0 skips it)")
     ap.add_argument("--side", type=int, default=None,
