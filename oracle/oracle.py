@@ -26,7 +26,7 @@ class _World(C.Structure):
         ("x", C.c_void_p), ("v", C.c_void_p), ("f", C.c_void_p),
         ("n_bonds", C.c_uint32), ("bond_beads", C.c_void_p), ("bond_kappa", C.c_void_p),
         ("bond_r0", C.c_void_p), ("n_angles", C.c_uint32), ("angle_beads", C.c_void_p),
-        ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p),
+        ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p), ("stationary", C.c_uint32),
     ]
 
 
@@ -89,6 +89,7 @@ class OracleWorld:
         self.ab, self.ak, self.at = (np.ascontiguousarray(ab, np.uint32),
                                      np.ascontiguousarray(ak), np.ascontiguousarray(at))
         self.t = int(world.t)
+        self.stationary = sum(1 << k for k, st in enumerate(np.asarray(world.stationary, bool)) if st)
 
     def _struct(self):
         s = _World()
@@ -104,6 +105,7 @@ class OracleWorld:
         s.bond_beads, s.bond_kappa, s.bond_r0 = _ptr(self.bb), _ptr(self.bk), _ptr(self.br)
         s.n_angles = self.ab.shape[0]
         s.angle_beads, s.angle_kappa, s.angle_theta0 = _ptr(self.ab), _ptr(self.ak), _ptr(self.at)
+        s.stationary = self.stationary
         return s
 
     def run(self, nsteps, nthreads=1):

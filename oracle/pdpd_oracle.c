@@ -179,6 +179,10 @@ static void *force_worker(void *arg)
                         for (int d = 0; d < 3; d++) ob_x[d] = w->x[3 * o + d] + delta[d];
                         for (uint32_t kh = cl->start[c]; kh < cl->start[c + 1]; kh++) {
                             uint32_t h = cl->beads[kh];
+                            /* two stationary beads do not interact
+                               (naive_dpd_engine_half_merge.hpp:440-449, 516-522) */
+                            if ((w->stationary >> (w->hash[h] >> 28)) & (w->stationary >> (w->hash[o] >> 28)) & 1u)
+                                continue;
                             double dx[3];
                             for (int d = 0; d < 3; d++) dx[d] = w->x[3 * h + d] - ob_x[d];
                             double dr2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
@@ -340,6 +344,8 @@ int pdo_run(pdo_world *w, uint32_t nsteps, int nthreads, char *err, size_t errle
         /* update_pos (dpd_maths_core_half_step.hpp:22-49) */
         const double hdt2 = (dt * dt) * 0.5, hdt = dt * 0.5;
         for (uint32_t i = 0; i < w->n_beads; i++) {
+            /* stationary bead types are not moved (naive_dpd_engine_half_merge.hpp:329-333) */
+            if ((w->stationary >> (w->hash[i] >> 28)) & 1u) continue;
             for (int d = 0; d < 3; d++) {
                 double L = (double)w->box[d];
                 double x = w->x[3 * i + d] + w->v[3 * i + d] * dt + w->f[3 * i + d] * hdt2;
@@ -386,9 +392,15 @@ int pdo_run(pdo_world *w, uint32_t nsteps, int nthreads, char *err, size_t errle
         if (rc) break;
         for (uint32_t k = 0; k < w->n_angles; k++) angle_bond(w, k);
 
-        /* update_mom (dpd_maths_core_half_step.hpp:51-61) */
-        for (uint32_t i = 0; i < w->n_beads; i++)
+        /* update_mom (dpd_maths_core_half_step.hpp:51-61); a stationary bead's v and f are
+           cleared instead (naive_dpd_engine_half_merge.hpp:387-394) */
+        for (uint32_t i = 0; i < w->n_beads; i++) {
+            if ((w->stationary >> (w->hash[i] >> 28)) & 1u) {
+                for (int d = 0; d < 3; d++) w->v[3 * i + d] = w->f[3 * i + d] = 0.0;
+                continue;
+            }
             for (int d = 0; d < 3; d++) w->v[3 * i + d] = w->v[3 * i + d] + w->f[3 * i + d] * hdt;
+        }
 
         w->t += 1;
     }

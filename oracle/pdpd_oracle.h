@@ -40,6 +40,7 @@ typedef struct pdo_world {
     uint32_t n_angles;
     const uint32_t *angle_beads; /* 3*n_angles: head, middle, tail */
     const double *angle_kappa, *angle_theta0;
+    uint32_t stationary;         /* bit k set: bead type k is stationary (BeadType::stationary) */
 } pdo_world;
 
 /* hash.hpp:20-30 */

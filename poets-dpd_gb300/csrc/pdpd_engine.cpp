@@ -440,9 +440,6 @@ static int check_world(const pdpd_world *w, char *reason, size_t n, bool need_be
         return say(PDPD_E_UNSUPPORTED, "Engine supports 1..16 bead types (4-bit BeadHash type field).");
     if (!w->conservative || !w->dissipative)
         return say(PDPD_E_INVALID, "Missing interaction matrices.");
-    if (w->stationary)
-        for (uint32_t i = 0; i < w->n_bead_types; i++)
-            if (w->stationary[i]) return say(PDPD_E_UNSUPPORTED, "Engine does not support stationary bead types.");
     for (uint32_t i = 0; i < w->n_bead_types * w->n_bead_types; i++)
         if (!(w->dissipative[i] >= 0) || !std::isfinite(w->conservative[i]))
             return say(PDPD_E_INVALID, "Interaction strengths must be finite and gamma >= 0.");
@@ -625,6 +622,9 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         d.n_beads = w.n_beads;
         d.n_types = w.n_bead_types;
         d.param_base = param_base;
+        d.stationary = 0;
+        for (uint32_t k = 0; w.stationary && k < w.n_bead_types; k++)
+            if (w.stationary[k]) d.stationary |= 1u << k;
         d.dt = w.dt;
         d.scale_inv_sqrt_dt = std::sqrt(24 * 1.0 / w.dt);  // pow_half(24 kT / dt)
         d.seed = w.seed;
@@ -1652,6 +1652,7 @@ int pdpd_server_submit(pdpd_server *s, const pdpd_world *w, uint32_t n_steps, pd
     j->cons.assign(w->conservative, w->conservative + nt * nt);
     j->diss.assign(w->dissipative, w->dissipative + nt * nt);
     j->stat.assign(nt, 0);
+    if (w->stationary) j->stat.assign(w->stationary, w->stationary + nt);
     j->hash.assign(w->hash, w->hash + n);
     j->x.resize(3 * (size_t)n);
     j->v.resize(3 * (size_t)n);

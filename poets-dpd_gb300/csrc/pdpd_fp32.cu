@@ -249,6 +249,12 @@ __device__ __forceinline__ void integrate32(const KArgs &a, const WorldDev &w, u
     }
     // update_mom (dpd_maths_core_half_step.hpp:51-61)
     float v[3] = {__fmaf_rn(F[0], hdt, vh.x), __fmaf_rn(F[1], hdt, vh.y), __fmaf_rn(F[2], hdt, vh.z)};
+    if ((w.stationary >> (__float_as_uint(ph.w) >> 28)) & 1u) {
+        // stationary type: v and f cleared (naive_dpd_engine_half_merge.hpp:387-394), so the
+        // next update_pos leaves it where it is
+        v[0] = v[1] = v[2] = 0.f;
+        F[0] = F[1] = F[2] = 0.f;
+    }
     if (FINAL) {
         ((float4 *)a.velB)[s] = make_float4(v[0], v[1], v[2], 0.f);
         ((float4 *)a.frc)[s] = make_float4(F[0], F[1], F[2], 0.f);
@@ -462,12 +468,15 @@ __global__ void __launch_bounds__(TILE_BEADS) k_begin32(KArgs a)
         int c[3];
         decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
         float o[3] = {ph.x, ph.y, ph.z};
-        const float v[3] = {vh.x, vh.y, vh.z};
-        const float F[3] = {fh.x, fh.y, fh.z};
+        // a stationary type is not moved and keeps its v (naive_dpd_engine_half_merge.hpp:329-333)
+        const bool st = (w.stationary >> (__float_as_uint(ph.w) >> 28)) & 1u;
+        const float v[3] = {st ? 0.f : vh.x, st ? 0.f : vh.y, st ? 0.f : vh.z};
+        const float F[3] = {st ? 0.f : fh.x, st ? 0.f : fh.y, st ? 0.f : fh.z};
         const uint32_t key = advance_position(w, dt, hdt2, c, o, v, F, err);
         const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
         ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
-        ((float4 *)a.velB)[s] = make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
+        ((float4 *)a.velB)[s] = st ? make_float4(vh.x, vh.y, vh.z, 0.f)
+                                   : make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
         a.keyrank[s] = make_uint2(key, rank);
         if (err) atomicOr(&a.worlds[tl.world].err, err);
     }

@@ -327,8 +327,13 @@ __global__ void __launch_bounds__(TILE_BEADS) k_force64(KArgs a)
         double F[3];
         pair_forces64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, vh, hh, F);
         if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
-        // update_mom: v += f * half(dt)
+        // update_mom: v += f * half(dt); a stationary type's v and f are cleared instead
+        // (naive_dpd_engine_half_merge.hpp:387-394), so the next update_pos leaves it in place
         double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+        if ((w.stationary >> (hh >> 28)) & 1u) {
+            v[0] = v[1] = v[2] = 0.0;
+            F[0] = F[1] = F[2] = 0.0;
+        }
         if (FINAL) {
             Vec4d vo = {v[0], v[1], v[2], 0.0};
             Vec4d fo = {F[0], F[1], F[2], 0.0};
@@ -361,12 +366,15 @@ __global__ void __launch_bounds__(TILE_BEADS) k_begin64(KArgs a)
         const Vec4d vh = ((const Vec4d *)a.velA)[s];
         const Vec4d fh = ((const Vec4d *)a.frc)[s];
         double x[3] = {ph.x, ph.y, ph.z};
-        const double v[3] = {vh.x, vh.y, vh.z};
-        const double F[3] = {fh.x, fh.y, fh.z};
+        // a stationary type is not moved and keeps its v (naive_dpd_engine_half_merge.hpp:329-333)
+        const bool st = (w.stationary >> (hash_of(ph) >> 28)) & 1u;
+        const double v[3] = {st ? 0.0 : vh.x, st ? 0.0 : vh.y, st ? 0.0 : vh.z};
+        const double F[3] = {st ? 0.0 : fh.x, st ? 0.0 : fh.y, st ? 0.0 : fh.z};
         const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
         const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
         Vec4d po = {x[0], x[1], x[2], ph.w};
-        Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
+        Vec4d vo = st ? Vec4d{vh.x, vh.y, vh.z, 0.0}
+                      : Vec4d{v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
         ((Vec4d *)a.posB)[s] = po;
         ((Vec4d *)a.velB)[s] = vo;
         a.keyrank[s] = make_uint2(key, rank);

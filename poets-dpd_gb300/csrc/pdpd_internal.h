@@ -21,6 +21,7 @@ struct WorldDev {
     uint32_t n_types;
     uint32_t param_base;  // first entry of this world's n_types^2 pair parameters
     uint32_t err;         // device-side error flags (ERR_*)
+    uint32_t stationary;  // bit k: bead type k is stationary (not moved; v, f cleared each step)
     double dt;
     double scale_inv_sqrt_dt;  // sqrt(24 kT / dt), kT = 1 (dpd_maths_core.hpp:24)
     uint64_t seed;

@@ -227,6 +227,7 @@ public:
 protected:
     bool CanSupportHookeanBonds() const override { return true; }
     bool CanSupportAngleBonds() const override { return true; }
+    bool CanSupportStationaryBeadTypes() const override { return true; }
 
 private:
     int m_precision;

@@ -13,8 +13,24 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def world_fixture_names():
+    """Fixtures made by the reference's half-step engine (the FP64 engine matches them bit for
+    bit)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not p.endswith(("hash_kat.npz", "testbase_suite.npz")))
+                  if not p.endswith(("hash_kat.npz", "testbase_suite.npz"))
+                  and not os.path.basename(p).startswith("merge_"))
+
+
+def merge_fixture_names():
+    """Fixtures made by the reference's half-merge engine (worlds with stationary bead types,
+    which the half-step engine does not support): same terms, another summation order."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "merge_*.npz")))
+
+
+def state_rel_err(a, b):
+    """max |a - b| / rms |b| over all beads and components (0 when both are zero)."""
+    scale = np.sqrt(np.mean(np.sum(b * b, axis=1))) if b.size else 0.0
+    d = np.max(np.abs(a - b)) if b.size else 0.0
+    return 0.0 if d == 0 else float(d / max(scale, 1e-300))
 
 
 def load_world_fixture(name):

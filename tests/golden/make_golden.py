@@ -36,8 +36,9 @@ def run_reference(world, checkpoints, engine=ENGINE):
     tmp_in = os.path.join(HERE, "_in.pdw1")
     tmp_out = os.path.join(HERE, "_out.bin")
     W.write_pdw1(world, tmp_in)
+    # the half-merge engine reports every stationary bead on stderr at each step
     subprocess.run([HARNESS, "step", engine, tmp_in, tmp_out, str(len(checkpoints))]
-                   + [str(c) for c in checkpoints], check=True)
+                   + [str(c) for c in checkpoints], check=True, stderr=subprocess.DEVNULL)
     data = open(tmp_out, "rb").read()
     os.remove(tmp_in)
     os.remove(tmp_out)
@@ -56,14 +57,14 @@ def run_reference(world, checkpoints, engine=ENGINE):
     return np.array(ts), np.stack(xs), np.stack(vs), np.stack(fs)
 
 
-def save_world_fixture(name, world, checkpoints, note):
-    ts, xs, vs, fs = run_reference(world, checkpoints)
+def save_world_fixture(name, world, checkpoints, note, engine=ENGINE):
+    ts, xs, vs, fs = run_reference(world, checkpoints, engine)
     buf = io.BytesIO()
     W.write_pdw1(world, buf)
     np.savez_compressed(os.path.join(HERE, name + ".npz"),
                         world=np.frombuffer(buf.getvalue(), np.uint8),
                         checkpoints=np.array(checkpoints), t=ts, x=xs, v=vs, f=fs,
-                        engine=np.array(ENGINE), note=np.array(note))
+                        engine=np.array(engine), note=np.array(note))
     print(f"{name}: {world.n_beads} beads, checkpoints {checkpoints}")
 
 
@@ -103,6 +104,46 @@ def boundary_world(seed=5):
            (-2.0, 2.0, 0.0), (2.0, -2.0, 0.0), (0.0, 0.0, 0.0), (0.5, -0.5, 0.5)]
     for p, v in zip(pts, vel):
         b.add_polymer(0, [p], [v])
+    return b.build()
+
+
+def stationary_wall_world(seed=13):
+    """8^3 water (type 0) against a stationary wall (type 1: the slab 0 <= x < 1, density 3)
+    whose beads start with non-zero velocities and forces: they must not move, and their v
+    and f are cleared by the first step."""
+    rng = np.random.default_rng(77)
+    b = W.WorldBuilder((8, 8, 8), 2, [[25.0, 40.0], [40.0, 25.0]], [[4.5, 4.5], [4.5, 4.5]],
+                       dt=0.02, seed=seed, stationary=[False, True])
+    b.add_polymer_type([0])
+    b.add_polymer_type([1])
+    for _ in range(3 * 64):
+        b.add_polymer(1, [tuple(rng.random(3) * np.array([1.0, 8.0, 8.0]))],
+                      [tuple(rng.standard_normal(3))], [tuple(rng.standard_normal(3))])
+    for _ in range(3 * 7 * 64):
+        b.add_polymer(0, [tuple(np.array([1.0, 0.0, 0.0]) + rng.random(3) * np.array([7.0, 8.0, 8.0]))],
+                      [tuple(rng.standard_normal(3))])
+    return b.build()
+
+
+def stationary_anchor_world(seed=17):
+    """Chains whose head bead type is stationary (anchored), with Hookean and angle bonds to
+    mobile beads, in 8^3 water: bonds across the stationary / mobile boundary."""
+    rng = np.random.default_rng(78)
+    a = [[25.0, 30.0, 60.0], [30.0, 25.0, 50.0], [60.0, 50.0, 25.0]]
+    g = [[4.5] * 3] * 3
+    b = W.WorldBuilder((8, 8, 8), 3, a, g, dt=0.01, seed=seed, stationary=[False, True, False])
+    b.add_polymer_type([1, 2, 2, 2], [(0, 1, 128.0, 0.5), (1, 2, 128.0, 0.5), (2, 3, 128.0, 0.5)],
+                       [(0, 1, 20.0, 0.0), (1, 2, 20.0, 0.0)])
+    b.add_polymer_type([0])
+    for _ in range(24):
+        p0 = rng.random(3) * 8.0
+        xs = [p0]
+        for _k in range(3):
+            d = rng.standard_normal(3)
+            xs.append((xs[-1] + 0.5 * d / np.linalg.norm(d)) % 8.0)
+        b.add_polymer(0, [tuple(x) for x in xs], [tuple(rng.standard_normal(3)) for _ in xs])
+    for _ in range(3 * 512 - 96):
+        b.add_polymer(1, [tuple(rng.random(3) * 8.0)], [tuple(rng.standard_normal(3))])
     return b.build()
 
 
@@ -240,6 +281,16 @@ def main():
                        "bent 3-bead chain, angle bond theta0=0.2 (the sin branch), in water")
     save_world_fixture("boundary_crossing", boundary_world(), [1, 5, 20],
                        "beads on cell and box faces crossing the periodic boundary")
+    # Stationary bead types: the half-step engine does not support them
+    # (dpd_engine.hpp:86-87), the half-merge engine does (naive_dpd_engine_half_merge.hpp:35);
+    # it adds the same pair terms in another order, so these fixtures pin the engine to a
+    # tolerance, not bit for bit.
+    merge = "naive_dpd_engine_half_merge"
+    save_world_fixture("merge_stationary_wall", stationary_wall_world(), [1, 5, 20],
+                       "8^3 water against a stationary wall slab (half-merge engine)", merge)
+    save_world_fixture("merge_stationary_anchor", stationary_anchor_world(), [1, 5, 20],
+                       "chains with stationary heads bonded to mobile beads, in 8^3 water "
+                       "(half-merge engine)", merge)
     empty = W.WorldBuilder((4, 4, 4), 1, [[25.0]], [[4.5]], dt=0.02, seed=1)
     empty.add_polymer_type([0])
     save_world_fixture("empty_world", empty.build(), [1, 3], "no beads at all")

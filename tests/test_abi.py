@@ -46,8 +46,8 @@ def test_can_support_accepts_configs():
 def test_can_support_rejections():
     _ensure_built()
     w = W.make_water(4)
-    w.stationary = np.array([True])
-    assert "stationary" in E.can_support(w)
+    w.stationary = np.array([True])  # supported
+    assert E.can_support(w) == ""
     w = W.make_water(4)
     w.box = np.array([4, 1, 4], np.int32)
     assert "at least 2" in E.can_support(w)

@@ -54,10 +54,15 @@ def test_can_support(exe, tmp_path):
     out = run(exe, "cansupport", "gb300_dpd_engine_fp32", str(p))
     assert "[]" in out and "max_bond_length 2" in out
     w = W.make_water(4)
-    w.stationary = np.array([True])
+    w.stationary = np.array([True])  # stationary bead types are supported
     W.write_pdw1(w, str(p))
     out = run(exe, "cansupport", "gb300_dpd_engine_fp64", str(p))
-    assert "[Engine does not support stationary bead types.]" in out
+    assert "[]" in out
+    w = W.make_water(4)
+    w.box = np.array([4, 1, 4], np.int32)
+    W.write_pdw1(w, str(p))
+    out = run(exe, "cansupport", "gb300_dpd_engine_fp64", str(p))
+    assert "at least 2" in out
 
 
 def read_vectors(path):

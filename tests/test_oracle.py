@@ -7,7 +7,8 @@ import pytest
 
 import oracle as O
 import pdpd_world as W
-from _helpers import load_hash_kat, load_world_fixture, world_fixture_names
+from _helpers import (load_hash_kat, load_world_fixture, merge_fixture_names, state_rel_err,
+                      world_fixture_names)
 
 
 def test_hash_known_answers_match_reference():
@@ -86,3 +87,25 @@ def test_oracle_replays_reference_testbase_suite():
             assert np.array_equal(np.hstack([ow.x, ow.v, ow.f]), s_out), name
             n_seg += 1
     assert n_seg == 900
+
+
+@pytest.mark.parametrize("name", merge_fixture_names())
+def test_oracle_stationary_types_vs_reference_half_merge(name):
+    """Stationary bead types against the reference's half-merge engine (the reference engine
+    family member that supports them): stationary beads stay exactly where they are with v and
+    f exactly zero after every step; every other bead agrees to summation-order roundoff."""
+    world, ref = load_world_fixture(name)
+    st = np.asarray(world.stationary, bool)[world.bead_type]
+    assert st.any() and (~st).any()
+    ow = O.OracleWorld(world)
+    prev = 0
+    for k, c in enumerate(ref["checkpoints"]):
+        ow.run(int(c) - prev, nthreads=4)
+        prev = int(c)
+        assert ow.t == ref["t"][k]
+        assert np.array_equal(ow.x[st], world.x[st]) and np.array_equal(ref["x"][k][st], world.x[st])
+        assert not ow.v[st].any() and not ow.f[st].any()
+        assert not ref["v"][k][st].any() and not ref["f"][k][st].any()
+        assert np.max(np.abs(ow.x - ref["x"][k])) < 1e-12
+        assert state_rel_err(ow.v, ref["v"][k]) < 1e-12
+        assert state_rel_err(ow.f, ref["f"][k]) < 1e-12
