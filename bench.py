@@ -397,6 +397,26 @@ def run_engine_arm(args):
 
     # --- dominant kernel: per-phase CUDA-event times over the same number of steps
     phases = eng.profile_run(args.steps)
+
+    # --- interval snapshots: the v2binary section encoded on the GPU vs the full read-back
+    snapshot = None
+    if world_size == 1 and args.precision in ("fp32", "fp64"):
+        sec_bytes = eng.v2binary_prepare()
+        eng.v2binary_encode()
+        eng.read_state(0)
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            eng.v2binary_encode()
+        t_v2 = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            eng.read_state(0)
+        t_rs = (time.perf_counter() - t0) / reps
+        snapshot = {"v2binary_bytes_per_bead": sec_bytes / n, "v2binary_ms": 1e3 * t_v2,
+                    "read_state_bytes_per_bead": 72.0, "read_state_ms": 1e3 * t_rs,
+                    "note": "one snapshot of the whole box: GPU-encoded v2binary section vs x, v, f "
+                            "read back as doubles (wall clock, host buffers)"}
     force_ms = phases["force_ms"] / max(1, phases["force_launches"])
     peak, peak_kind = measured_peaks()
     algo = ALGO_BYTES[args.precision] * n
@@ -450,6 +470,7 @@ def run_engine_arm(args):
         "cpu_baseline": cpu,
         "batched_grid": batched,
         "serving": serving,
+        "snapshot": snapshot,
         "kernel_config": {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
                                                     "autotune")},
     }

@@ -215,6 +215,36 @@ int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, double *d_f
  * each kernel node).  For accounting in benchmarks. */
 uint64_t pdpd_kernel_launches(pdpd_engine *e);
 
+/* ---- v2binary snapshots encoded on the GPU. ------------------------------------------------
+ *
+ * The reference writes a world state as text plus, in its "WorldState v2binary" form, a
+ * BinaryData section of about 22 bytes per bead (write_world_state, dpd_state_io.hpp:408-466;
+ * write_polymer_binary :182-247; CVec3Half, cvec3.hpp:132-252): per polymer a 16-bit header
+ * and id deltas, per bead its position as 3 x uint32 with 16 fractional bits and v, f as
+ * CVec3Half.  These calls produce and consume that section (the bytes after "BinaryData\n"
+ * and its zero byte) straight from and to the device state, byte for byte what the
+ * reference's writer produces for the same state (the text header stays the caller's, e.g.
+ * the reference's own writer).
+ *
+ * prepare: the world's polymers in the order they are written (WorldState::polymers):
+ *   polymer_types[p], bead ids polymer_beads[polymer_start[p] .. polymer_start[p+1]) in
+ *   offset order, polymer_ids[p] (NULL: p).  Every bead must appear exactly once.
+ *   *section_bytes receives the section size.  Valid until the next attach.
+ * encode: write the section of the world's current state (x(t), v(t), f(t) after the last
+ *   Run) into out[0..capacity); out == NULL only reports the size.  PDPD_E_INVALID if a
+ *   velocity or force is not representable (non-finite, magnitude >= 2^15 after rounding).
+ * decode: set the world's x, v, f from a section with the prepared structure (headers and
+ *   deltas must match; PDPD_E_INVALID otherwise) -- the reference's reader
+ *   (read_polymer_binary, dpd_state_io.hpp:249-330) -- and rebuild its cell list; t and the
+ *   parameters are unchanged. */
+int pdpd_v2binary_prepare(pdpd_engine *e, uint32_t world, uint32_t n_polymers,
+                          const uint32_t *polymer_ids, const uint32_t *polymer_types,
+                          const uint32_t *polymer_start, const uint32_t *polymer_beads,
+                          size_t *section_bytes);
+int pdpd_v2binary_encode(pdpd_engine *e, uint32_t world, uint8_t *out, size_t capacity,
+                         size_t *bytes);
+int pdpd_v2binary_decode(pdpd_engine *e, uint32_t world, const uint8_t *in, size_t bytes);
+
 /* ---- Job server (continuous batching) -- no counterpart in the reference. ----------------
  *
  * The reference serves one world per engine: a caller with many independent simulations runs

@@ -17,11 +17,17 @@
 //       Print the engine's CanSupport() string.
 //   ref_harness time <engine> <in.pdw1> <steps>
 //       Attach + Run(steps), print bead-steps/s of the Run call.
+//   ref_harness v2binary <in.pdw1> <out.bin>
+//       write_world_state(binary=true) (dpd_state_io.hpp:408-466): the reference's own
+//       v2binary snapshot of the world as read.
+//   ref_harness v2read <in.v2> <out.bin>
+//       read_world_state (dpd_state_io.hpp:481-586) of a v2binary file; dump t, x, v, f.
 
 #include "dpd/core/dpd_engine.hpp"
 #include "dpd/core/dpd_state_validator.hpp"
 #include "dpd/core/logging.hpp"
 #include "dpd/core/logging_impl.hpp"
+#include "dpd/core/dpd_state_io.hpp"
 #include "dpd/engines/naive/naive_dpd_engine.hpp"
 #include "dpd/engines/naive/naive_dpd_engine_half_step.hpp"
 #include "dpd/engines/naive/naive_dpd_engine_half_merge.hpp"
@@ -30,6 +36,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <chrono>
+#include <fstream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -130,6 +137,27 @@ int cmd_time(int argc, char **argv)
     return 0;
 }
 
+int cmd_v2binary(int argc, char **argv)
+{
+    if (argc < 4) throw std::runtime_error("usage: v2binary in out");
+    WorldState s = read_pdw1(argv[2]);
+    std::ofstream out(argv[3], std::ios::binary);
+    if (!out) throw std::runtime_error("cannot open output");
+    write_world_state(out, s, true);
+    return 0;
+}
+
+int cmd_v2read(int argc, char **argv)
+{
+    if (argc < 4) throw std::runtime_error("usage: v2read in out");
+    WorldState s = read_world_state(std::string(argv[2]));
+    FILE *out = fopen(argv[3], "wb");
+    if (!out) throw std::runtime_error("cannot open output");
+    dump(out, s);
+    fclose(out);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -141,6 +169,8 @@ int main(int argc, char **argv)
         if (cmd == "hash") return cmd_hash(argc, argv);
         if (cmd == "cansupport") return cmd_cansupport(argc, argv);
         if (cmd == "time") return cmd_time(argc, argv);
+        if (cmd == "v2binary") return cmd_v2binary(argc, argv);
+        if (cmd == "v2read") return cmd_v2read(argc, argv);
         throw std::runtime_error("unknown command " + cmd);
     } catch (std::exception &e) {
         fprintf(stderr, "ref_harness: %s\n", e.what());

@@ -11,7 +11,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -89,8 +91,24 @@ struct HostPinned {
     }
 };
 
+// v2binary section layout of one world: the section bytes with every polymer header and id
+// delta written and the bead records left to the encoder, the byte offset of each bead's
+// record, and the (offset, length) runs of structure bytes (for checking a stream to decode).
+struct V2Layout {
+    DevBuf d_buf, d_off;
+    size_t bytes = 0;
+    std::vector<uint8_t> tmpl;
+    std::vector<std::pair<uint32_t, uint32_t>> structure;
+    ~V2Layout()
+    {
+        d_buf.release();
+        d_off.release();
+    }
+};
+
 struct WorldHost {
     WorldDev dev;
+    std::shared_ptr<V2Layout> v2;
 };
 
 struct ConfigEntry {
@@ -152,6 +170,7 @@ struct pdpd_engine {
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
+    DevBuf d_v2err;
     cudaEvent_t ev_snap[2] = {nullptr, nullptr};
     cudaEvent_t ev_copied[2] = {nullptr, nullptr};
 
@@ -200,7 +219,8 @@ struct pdpd_engine {
         DevBuf *bufs[] = {&d_worlds, &d_tiles, &d_bricks, &d_start, &d_cnt, &d_blocksums, &d_posA, &d_velA,
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
-                          &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1]};
+                          &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
+                          &d_v2err};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -1274,6 +1294,163 @@ uint64_t pdpd_kernel_launches(pdpd_engine *e)
 
 }  // extern "C"
 
+
+// ==========================================================================================
+// v2binary snapshots (the BinaryData section of the reference's v2binary state format)
+// ==========================================================================================
+
+extern "C" {
+
+int pdpd_v2binary_prepare(pdpd_engine *e, uint32_t world, uint32_t n_polymers,
+                          const uint32_t *polymer_ids, const uint32_t *polymer_types,
+                          const uint32_t *polymer_start, const uint32_t *polymer_beads,
+                          size_t *section_bytes)
+{
+    if (section_bytes) *section_bytes = 0;
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    if (n_polymers && (!polymer_types || !polymer_start || !polymer_beads))
+        return e->fail(PDPD_E_INVALID, "missing polymer arrays");
+    const uint32_t n = e->worlds[world].dev.n_beads;
+    if (n_polymers && polymer_start[0] != 0) return e->fail(PDPD_E_INVALID, "polymer_start[0] must be 0");
+    auto L = std::make_shared<V2Layout>();
+    std::vector<uint32_t> off(n, 0xFFFFFFFFu);
+    std::vector<uint8_t> &t = L->tmpl;
+    auto put16 = [&](uint32_t v) {
+        t.push_back((uint8_t)(v & 0xFF));
+        t.push_back((uint8_t)(v >> 8));
+    };
+    auto put32 = [&](uint32_t v) {
+        for (int k = 0; k < 4; k++) t.push_back((uint8_t)(v >> (8 * k)));
+    };
+    auto mark = [&](size_t begin) {
+        if (t.size() > begin) L->structure.push_back({(uint32_t)begin, (uint32_t)(t.size() - begin)});
+    };
+    // write_polymer_binary (dpd_state_io.hpp:182-247), per polymer in order
+    uint32_t prev_pid = 0xFFFFFFFFu, prev_bid = 0xFFFFFFFFu;
+    for (uint32_t p = 0; p < n_polymers; p++) {
+        const uint32_t b0 = polymer_start[p], b1 = polymer_start[p + 1];
+        if (b1 <= b0) return e->fail(PDPD_E_INVALID, "polymer %u has no beads", p);
+        if (polymer_types[p] >= (1u << 13)) return e->fail(PDPD_E_INVALID, "polymer type does not fit 13 bits");
+        const uint32_t pid = polymer_ids ? polymer_ids[p] : p;
+        const bool nsp = pid != prev_pid + 1u;
+        const bool nsi = polymer_beads[b0] != prev_bid + 1u;
+        bool nsa = false;
+        for (uint32_t k = b0 + 1; k < b1; k++) nsa |= polymer_beads[k - 1] + 1u != polymer_beads[k];
+        size_t begin = t.size();
+        put16(polymer_types[p] | (nsp ? 1u << 13 : 0u) | (nsi ? 1u << 14 : 0u) | (nsa ? 1u << 15 : 0u));
+        if (nsp) put32(pid - prev_pid);
+        prev_pid = pid;
+        for (uint32_t k = b0; k < b1; k++) {
+            const uint32_t bid = polymer_beads[k];
+            if (bid >= n) return e->fail(PDPD_E_INVALID, "polymer %u refers to bead %u of %u", p, bid, n);
+            if (off[bid] != 0xFFFFFFFFu) return e->fail(PDPD_E_INVALID, "bead %u appears twice", bid);
+            if ((k == b0 && nsi) || (k > b0 && nsa)) put32(bid - prev_bid);
+            prev_bid = bid;
+            mark(begin);
+            off[bid] = (uint32_t)t.size();
+            t.resize(t.size() + 20, 0);
+            begin = t.size();
+        }
+        if (t.size() >= 0xFFFFFFF0u) return e->fail(PDPD_E_UNSUPPORTED, "section larger than 4 GB");
+    }
+    for (uint32_t i = 0; i < n; i++)
+        if (off[i] == 0xFFFFFFFFu) return e->fail(PDPD_E_INVALID, "bead %u belongs to no polymer", i);
+    L->bytes = t.size();
+    cudaSetDevice(e->device);
+    if (L->d_buf.alloc(std::max<size_t>(L->bytes, 16)) != cudaSuccess ||
+        L->d_off.alloc(sizeof(uint32_t) * std::max<uint32_t>(n, 1)) != cudaSuccess ||
+        e->d_v2err.alloc(16) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "v2binary layout allocation failed");
+    cudaError_t ce = cudaMemcpyAsync(L->d_buf.p, t.data(), L->bytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess && n)
+        ce = cudaMemcpyAsync(L->d_off.p, off.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "v2binary layout upload");
+    e->worlds[world].v2 = L;
+    if (section_bytes) *section_bytes = L->bytes;
+    return PDPD_OK;
+}
+
+int pdpd_v2binary_encode(pdpd_engine *e, uint32_t world, uint8_t *out, size_t capacity, size_t *bytes)
+{
+    if (bytes) *bytes = 0;
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    V2Layout *L = e->worlds[world].v2.get();
+    if (!L) return e->fail(PDPD_E_STATE, "pdpd_v2binary_prepare was not called for this world");
+    if (bytes) *bytes = L->bytes;
+    if (!out) return PDPD_OK;
+    if (capacity < L->bytes) return e->fail(PDPD_E_INVALID, "output buffer too small (%zu < %zu bytes)", capacity, L->bytes);
+    cudaSetDevice(e->device);
+    const WorldDev &wd = e->worlds[world].dev;
+    uint32_t herr = 0;
+    cudaError_t ce = cudaMemsetAsync(e->d_v2err.p, 0, sizeof(uint32_t), e->stream);
+    e->launches += launch_v2_encode(e->args, e->fp64(), world, wd.n_beads, L->d_buf.as<uint8_t>(),
+                                    L->d_off.as<uint32_t>(), e->d_v2err.as<uint32_t>(), e->stream);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, L->d_buf.p, L->bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&herr, e->d_v2err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "v2binary encode");
+    if (herr & 2u) return e->fail(PDPD_E_INVALID, "Bead is out of bounds.");
+    if (herr & 1u)
+        return e->fail(PDPD_E_INVALID, "A velocity or force is not finite or has magnitude 65536 or more "
+                                       "(not representable as CVec3Half).");
+    return PDPD_OK;
+}
+
+static int rebin_from_staging(pdpd_engine *e);
+
+int pdpd_v2binary_decode(pdpd_engine *e, uint32_t world, const uint8_t *in, size_t bytes)
+{
+    if (!e) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    V2Layout *L = e->worlds[world].v2.get();
+    if (!L) return e->fail(PDPD_E_STATE, "pdpd_v2binary_prepare was not called for this world");
+    if (!in || bytes != L->bytes)
+        return e->fail(PDPD_E_INVALID, "section of %zu bytes, the world's layout has %zu", bytes, L->bytes);
+    for (const auto &r : L->structure)
+        if (memcmp(in + r.first, L->tmpl.data() + r.first, r.second) != 0)
+            return e->fail(PDPD_E_INVALID, "section structure (polymer headers or id deltas) at byte %u "
+                                           "differs from the world's polymers", r.first);
+    cudaSetDevice(e->device);
+    // every world's rows to staging buffer 0, this world's rows from the section, re-bin
+    int rc = download(e, 0, e->stream);
+    if (rc) return rc;
+    uint32_t herr = 0;
+    cudaError_t ce = cudaMemsetAsync(e->d_v2err.p, 0, sizeof(uint32_t), e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(L->d_buf.p, in, bytes, cudaMemcpyHostToDevice, e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "v2binary upload");
+    e->launches += launch_v2_decode(e->args, world, e->worlds[world].dev.n_beads, L->d_buf.as<uint8_t>(),
+                                    L->d_off.as<uint32_t>(), e->d_staging[0].as<double>(),
+                                    e->d_v2err.as<uint32_t>(), e->stream);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&herr, e->d_v2err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "v2binary decode");
+    if (herr) return e->fail(PDPD_E_INVALID, "Bead was out of box.");
+    return rebin_from_staging(e);
+}
+
+}  // extern "C"
+
+// Rebuild the sorted state from the id-ordered staging rows in buffer 0 (as the end of an
+// attach does); t and the parameters are unchanged.
+static int rebin_from_staging(pdpd_engine *e)
+{
+    KArgs a = e->args;
+    a.staging = e->d_staging[0].as<double>();
+    const uint32_t *hash_in = e->d_hash.as<uint32_t>();
+    e->launches += e->fp64() ? launch_bin64(a, hash_in, e->stream) : launch_bin32(a, hash_in, e->stream);
+    e->launches += launch_sort(a, e->fp64(), 0, 1, e->stream);
+    cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "re-bin kernels");
+    return e->check_device_errors();
+}
 
 // ==========================================================================================
 // Job server: continuous batching of independent worlds on one engine.

@@ -151,6 +151,14 @@ int launch_observe(const KArgs &a, int fp64, uint32_t world, uint32_t n_beads, u
                    unsigned long long *rdf, uint32_t n_bond_bins, unsigned long long *bond_hist,
                    ObsPartial *part, cudaStream_t s);
 
+// v2binary codec (pdpd_codec.cu): encode one world's bead records into a prepared section
+// buffer at the given per-bead byte offsets, or decode them into the id-ordered staging rows.
+// err (device) collects 1 = unrepresentable vector, 2 = position outside the box.
+int launch_v2_encode(const KArgs &a, int fp64, uint32_t world, uint32_t n, uint8_t *buf,
+                     const uint32_t *off, uint32_t *err, cudaStream_t s);
+int launch_v2_decode(const KArgs &a, uint32_t world, uint32_t n, const uint8_t *buf,
+                     const uint32_t *off, double *staging, uint32_t *err, cudaStream_t s);
+
 // Message returned by pdpd_last_error(NULL) on this thread.
 void set_thread_error(const char *msg);
 

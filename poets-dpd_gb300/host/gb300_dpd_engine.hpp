@@ -144,6 +144,7 @@ public:
     {
         engine();
         m_state = state;
+        m_v2_state = nullptr;
         if (!state) {
             check(pdpd_attach(m_engine, nullptr), "Attach");
             return;
@@ -224,6 +225,35 @@ public:
             throw std::runtime_error(pdpd_last_error(m_engine));
     }
 
+    // The BinaryData section of a "WorldState v2binary" file for the attached state as the
+    // engine holds it after the last Run, encoded on the GPU (about 22 bytes per bead cross
+    // the bus instead of 72).  Not a DPDEngine member: gb300_v2binary.hpp writes the whole
+    // file with it.  The polymer layout is built on the first call after an Attach.
+    std::vector<uint8_t> EncodeV2BinarySection()
+    {
+        engine();
+        require_state();
+        if (m_v2_state != m_state) {
+            std::vector<uint32_t> types, start{0}, beads, ids;
+            for (const Polymer &p : m_state->polymers) {
+                ids.push_back(p.polymer_id);
+                types.push_back(p.polymer_type);
+                beads.insert(beads.end(), p.bead_ids.begin(), p.bead_ids.end());
+                start.push_back((uint32_t)beads.size());
+            }
+            size_t n = 0;
+            check(pdpd_v2binary_prepare(m_engine, 0, (uint32_t)types.size(), ids.data(), types.data(),
+                                        start.data(), beads.data(), &n),
+                  "v2binary");
+            m_v2_state = m_state;
+        }
+        size_t n = 0;
+        check(pdpd_v2binary_encode(m_engine, 0, nullptr, 0, &n), "v2binary");
+        std::vector<uint8_t> out(n);
+        check(pdpd_v2binary_encode(m_engine, 0, out.data(), out.size(), &n), "v2binary");
+        return out;
+    }
+
 protected:
     bool CanSupportHookeanBonds() const override { return true; }
     bool CanSupportAngleBonds() const override { return true; }
@@ -233,6 +263,7 @@ private:
     int m_precision;
     pdpd_engine *m_engine = nullptr;
     WorldState *m_state = nullptr;
+    WorldState *m_v2_state = nullptr;  // state the v2binary layout was built for
 
     pdpd_engine *engine()
     {

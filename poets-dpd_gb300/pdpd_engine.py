@@ -38,7 +38,8 @@ EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support"
             "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
             "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc",
-            "pdpd_observe", "pdpd_server_create", "pdpd_server_submit", "pdpd_server_drain",
+            "pdpd_observe", "pdpd_v2binary_prepare", "pdpd_v2binary_encode",
+            "pdpd_v2binary_decode", "pdpd_server_create", "pdpd_server_submit", "pdpd_server_drain",
             "pdpd_server_config", "pdpd_server_stats_get", "pdpd_server_engine",
             "pdpd_server_destroy"]
 
@@ -119,6 +120,9 @@ def lib():
         "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
         "pdpd_step_noalloc": (i32, [C.POINTER(PdpdWorld), vp, vp, vp, vp, u32, vp]),
         "pdpd_observe": (i32, [vp, u32, C.POINTER(PdpdObservables), u32, vp, u32, vp]),
+        "pdpd_v2binary_prepare": (i32, [vp, u32, u32, vp, vp, vp, vp, C.POINTER(C.c_size_t)]),
+        "pdpd_v2binary_encode": (i32, [vp, u32, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "pdpd_v2binary_decode": (i32, [vp, u32, vp, C.c_size_t]),
         "pdpd_server_create": (i32, [i32, i32, C.c_size_t, u32, C.POINTER(vp)]),
         "pdpd_server_submit": (i32, [vp, C.POINTER(PdpdWorld), u32, JOB_FN, vp,
                                      C.POINTER(C.c_uint64)]),
@@ -348,6 +352,38 @@ class GB300DPDEngine:
 
     def kernel_launches(self):
         return int(lib().pdpd_kernel_launches(self._h))
+
+    # -- v2binary snapshots ---------------------------------------------------------------
+    def v2binary_prepare(self, world_index=0, polymer_ids=None) -> int:
+        """Lay out the v2binary section of attached world ``world_index`` from its polymers
+        (the World's ``poly_type`` / ``poly_start`` / ``poly_beads``); returns its size."""
+        w = self._worlds[world_index]
+        pt = np.ascontiguousarray(w.poly_type, np.uint32)
+        ps = np.ascontiguousarray(w.poly_start, np.uint32)
+        pb = np.ascontiguousarray(w.poly_beads, np.uint32)
+        pid = None if polymer_ids is None else np.ascontiguousarray(polymer_ids, np.uint32)
+        size = C.c_size_t(0)
+        self._check(lib().pdpd_v2binary_prepare(self._h, world_index, len(pt), _p(pid), _p(pt),
+                                                _p(ps), _p(pb), C.byref(size)), "v2binary_prepare")
+        return int(size.value)
+
+    def v2binary_encode(self, world_index=0) -> bytes:
+        """The BinaryData section of the world's current state, encoded on the GPU."""
+        size = C.c_size_t(0)
+        self._check(lib().pdpd_v2binary_encode(self._h, world_index, None, 0, C.byref(size)),
+                    "v2binary_encode")
+        out = np.empty(max(1, size.value), np.uint8)
+        self._check(lib().pdpd_v2binary_encode(self._h, world_index, out.ctypes.data, out.size,
+                                               C.byref(size)), "v2binary_encode")
+        return out[:size.value].tobytes()
+
+    def v2binary_decode(self, section: bytes, world_index=0):
+        """Set the world's x, v, f from a BinaryData section (decoded on the GPU)."""
+        buf = np.frombuffer(section, np.uint8)
+        self._check(lib().pdpd_v2binary_decode(self._h, world_index, buf.ctypes.data if buf.size else None,
+                                               buf.size), "v2binary_decode")
+        if self._worlds:
+            self.read_state(world_index, into=self._worlds[world_index])
 
     def read_state(self, world_index=0, into=None):
         """Copy world ``world_index``'s x, v, f, t to numpy (into a World when given)."""

@@ -17,7 +17,7 @@ def world_fixture_names():
     bit)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                   if not p.endswith(("hash_kat.npz", "testbase_suite.npz"))
-                  and not os.path.basename(p).startswith("merge_"))
+                  and not os.path.basename(p).startswith(("merge_", "v2_")))
 
 
 def merge_fixture_names():
@@ -87,3 +87,14 @@ def world_at(world, t, state):
     w.t = t
     w.x, w.v, w.f = state[:, 0:3].copy(), state[:, 3:6].copy(), state[:, 6:9].copy()
     return w
+
+
+def v2_fixture_names():
+    """v2binary fixtures: a world, the reference's v2binary file of it, and the state the
+    reference's reader returns for that file."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "v2_*.npz")))
+
+
+def load_v2_fixture(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return W.read_pdw1(d["world"].tobytes()), d["v2"].tobytes(), d["x"], d["v"], d["f"]

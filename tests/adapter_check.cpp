@@ -7,14 +7,19 @@
 //   adapter_check factories
 //   adapter_check cansupport <engine> <world.pdw1>
 //   adapter_check flatten <world.pdw1> <out.bin>
+//   adapter_check v2file <world.pdw1> <section.bin> <out.v2>
+//       gb300_v2binary.hpp's file writer around a given BinaryData section
 #include "dpd/core/dpd_state_validator.hpp"
 #include "dpd/core/logging.hpp"
 #include "dpd/core/logging_impl.hpp"
 
 #include "gb300_dpd_engine.hpp"
+#include "gb300_v2binary.hpp"
 #include "pdw1_read.hpp"
 
 #include <cstdio>
+#include <fstream>
+#include <iterator>
 #include <string>
 #include <vector>
 
@@ -71,7 +76,16 @@ int main(int argc, char **argv)
             fclose(f);
             return 0;
         }
-        fprintf(stderr, "usage: adapter_check factories | cansupport <engine> <pdw1> | flatten <pdw1> <out>\n");
+        if (cmd == "v2file" && argc > 4) {
+            WorldState s = pdw1::read_pdw1(argv[2]);
+            std::ifstream in(argv[3], std::ios::binary);
+            std::vector<uint8_t> section((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+            std::ofstream out(argv[4], std::ios::binary);
+            write_world_state_v2binary(out, s, section);
+            return 0;
+        }
+        fprintf(stderr, "usage: adapter_check factories | cansupport <engine> <pdw1> | flatten <pdw1> <out>"
+                        " | v2file <pdw1> <section> <out>\n");
         return 1;
     } catch (std::exception &e) {
         fprintf(stderr, "adapter_check: %s\n", e.what());

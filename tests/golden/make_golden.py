@@ -147,6 +147,74 @@ def stationary_anchor_world(seed=17):
     return b.build()
 
 
+def permute_bead_ids(world, seed=5):
+    """The same world with its bead ids shuffled: polymers then hold non-consecutive ids (the
+    v2binary writer's non-sequential bead-id flags)."""
+    rng = np.random.default_rng(seed)
+    n = world.n_beads
+    new_of_old = rng.permutation(n).astype(np.uint32)
+    old_of_new = np.argsort(new_of_old)
+    w = world.copy()
+    for k in ("polymer_id", "polymer_offset", "bead_type", "polymer_type_of_bead", "is_monomer",
+              "x", "v", "f"):
+        setattr(w, k, getattr(world, k)[old_of_new].copy())
+    w.poly_beads = new_of_old[world.poly_beads]
+    return w
+
+
+def v2binary_edge_world():
+    """4^3 water whose velocities and forces hit the CVec3Half cases: zero and subnormal
+    components, vectors below 2^-14 (encode as zero), exact small integers, mantissas that
+    round up to 256 (exponent + 1), ties (round half away from zero), mixed magnitudes;
+    positions at 0, at a tie, and just below the box side (rounds to the side: wraps to 0)."""
+    w = W.make_water(4, seed=3, gen_seed=5)
+    n = w.n_beads
+    rng = np.random.default_rng(9)
+    special = [
+        (0.0, 0.0, 0.0), (5e-324, 0.0, -5e-324), (1e-5, -2e-5, 3e-6), (2.0 ** -15, 0.0, 0.0),
+        (2.0 ** -14, 2.0 ** -15, -(2.0 ** -16)), (255.0, -255.0, 17.0), (1.0, 2.0, 3.0),
+        (0.9999, 0.5, -0.25), (-0.99999, 0.001, 0.0), (0.5 + 1.0 / 512, 0.0, 0.0),
+        (-(0.5 + 1.0 / 512), 0.25 + 1.0 / 1024, 0.0), (32000.0, -1.0, 1e-3),
+        (1e4, 1e-9, -1e4), (-3.0e-3, 7.0e-4, 2.5e-3), (0.0, -0.0, 1.0), (-7.5, 0.0, 0.1)]
+    v = rng.standard_normal((n, 3)) * np.exp(rng.uniform(-8, 8, (n, 1)))
+    f = rng.standard_normal((n, 3)) * np.exp(rng.uniform(-12, 9, (n, 1)))
+    for k, s in enumerate(special):
+        v[k] = s
+        f[len(special) + k] = s
+    w.v, w.f = v, f
+    x = w.x.copy()
+    x[0] = (0.0, 0.0, 0.0)
+    x[1] = (1.0 + 0.5 / 65536, 2.0 + 1.5 / 65536, 3.0 - 0.5 / 65536)
+    x[2] = (4.0 - 1e-9, 4.0 - 1e-12, 0.5)
+    x[3] = (3.9999999, 0.0000001, 2.0)
+    w.x = x
+    return w
+
+
+def v2binary_fixture(name, world, note):
+    """The reference's own v2binary file of the world (write_world_state, binary) and the
+    state its reader returns for that file."""
+    tmp_in = os.path.join(HERE, "_v2in.pdw1")
+    tmp_v2 = os.path.join(HERE, "_v2.bin")
+    tmp_dump = os.path.join(HERE, "_v2.dump")
+    W.write_pdw1(world, tmp_in)
+    subprocess.run([HARNESS, "v2binary", tmp_in, tmp_v2], check=True)
+    subprocess.run([HARNESS, "v2read", tmp_v2, tmp_dump], check=True)
+    v2 = open(tmp_v2, "rb").read()
+    dump = open(tmp_dump, "rb").read()
+    for f in (tmp_in, tmp_v2, tmp_dump):
+        os.remove(f)
+    n = int(np.frombuffer(dump, np.uint32, 1, 8)[0])
+    rec = np.frombuffer(dump, np.float64, 9 * n, 12).reshape(n, 9)
+    buf = io.BytesIO()
+    W.write_pdw1(world, buf)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        world=np.frombuffer(buf.getvalue(), np.uint8),
+                        v2=np.frombuffer(v2, np.uint8), x=rec[:, 0:3], v=rec[:, 3:6], f=rec[:, 6:9],
+                        note=np.array(note))
+    print(f"{name}: {n} beads, {len(v2)} bytes")
+
+
 def hash_fixture():
     rng = np.random.default_rng(2024)
     n = 4096
@@ -291,6 +359,12 @@ def main():
     save_world_fixture("merge_stationary_anchor", stationary_anchor_world(), [1, 5, 20],
                        "chains with stationary heads bonded to mobile beads, in 8^3 water "
                        "(half-merge engine)", merge)
+    # v2binary snapshots (the reference's writer and reader)
+    v2binary_fixture("v2_polymer8", W.make_polymer_box(8, chain_fraction=0.1, seed=2),
+                     "8^3 polymer box, 10% H-T5 chains, initial state")
+    v2binary_fixture("v2_edges", v2binary_edge_world(), "CVec3Half and position edge cases")
+    v2binary_fixture("v2_permuted", permute_bead_ids(W.make_polymer_box(6, chain_fraction=0.3, seed=4)),
+                     "6^3 polymer box with shuffled bead ids (non-sequential id records)")
     empty = W.WorldBuilder((4, 4, 4), 1, [[25.0]], [[4.5]], dt=0.02, seed=1)
     empty.add_polymer_type([0])
     save_world_fixture("empty_world", empty.build(), [1, 3], "no beads at all")

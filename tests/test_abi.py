@@ -22,7 +22,7 @@ def _ensure_built():
 def header_symbols():
     text = open(os.path.join(ROOT, "include", "pdpd_gpu.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pdpd_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pdpd_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_and_binding_agree():

@@ -11,6 +11,8 @@ import numpy as np
 import pytest
 
 import pdpd_world as W
+import v2binary as V
+from _helpers import load_v2_fixture, v2_fixture_names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_INCLUDE = os.environ.get("PDPD_REFERENCE_INCLUDE", "/root/reference/include")
@@ -95,3 +97,16 @@ def test_flatten_matches_python_mirror(exe, tmp_path):
     assert list(head[:3]) == list(world.box) and head[5] == 17 and head[6] == world.n_beads
     assert head[7] == 88  # sizeof(Bead): x/v/f read in place from the reference's beads
     assert np.array_equal(x.reshape(-1, 3), world.x)
+
+
+@pytest.mark.parametrize("name", v2_fixture_names())
+def test_v2binary_file_writer_matches_reference(exe, tmp_path, name):
+    """gb300_v2binary.hpp writes the reference's text header around a GPU-encoded section:
+    with the reference's own section, the file equals the reference writer's byte for byte."""
+    world, v2, _, _, _ = load_v2_fixture(name)
+    _, section = V.split_file(v2)
+    pw, ps, po = tmp_path / "w.pdw1", tmp_path / "s.bin", tmp_path / "o.v2"
+    W.write_pdw1(world, str(pw))
+    ps.write_bytes(section)
+    run(exe, "v2file", str(pw), str(ps), str(po))
+    assert po.read_bytes() == v2
