@@ -65,6 +65,13 @@ typedef struct pdpd_world {
     uint32_t n_angles;             /* angle bonds (BondPair), polymer-major */
     const uint32_t *angle_beads;   /* 3*n_angles: head, middle, tail bead ids */
     const double *angle_kappa, *angle_theta0;
+    /* Spatially varying DPD parameters (InteractionStrength Parameters that are expressions of
+     * x, y, z, ux, uy, uz; dpd_engine.hpp:59-82): per cell, x-major with z fastest, the
+     * n_bead_types^2 values of a_ij and of gamma_ij as the reference evaluates them per cell
+     * (naive_dpd_engine_half_merge.hpp:221-236).  A pair then uses the mean of the two beads'
+     * cell values of a_ij and of sqrt(gamma_ij) (:570-583).  NULL (both): the matrices above
+     * apply everywhere.  The FP32 engine runs such worlds with force_kernel 1. */
+    const double *cell_conservative, *cell_dissipative;
 } pdpd_world;
 
 /* Phase timings, same meaning as DPDEngine::timings_t (dpd_engine.hpp:38-46); -1 = unset. */

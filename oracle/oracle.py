@@ -27,6 +27,7 @@ class _World(C.Structure):
         ("n_bonds", C.c_uint32), ("bond_beads", C.c_void_p), ("bond_kappa", C.c_void_p),
         ("bond_r0", C.c_void_p), ("n_angles", C.c_uint32), ("angle_beads", C.c_void_p),
         ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p), ("stationary", C.c_uint32),
+        ("cell_conservative", C.c_void_p), ("cell_dissipative", C.c_void_p),
     ]
 
 
@@ -90,6 +91,10 @@ class OracleWorld:
                                      np.ascontiguousarray(ak), np.ascontiguousarray(at))
         self.t = int(world.t)
         self.stationary = sum(1 << k for k, st in enumerate(np.asarray(world.stationary, bool)) if st)
+        cc = getattr(world, "cell_conservative", None)
+        cd = getattr(world, "cell_dissipative", None)
+        self.cell_a = None if cc is None else np.ascontiguousarray(cc, np.float64)
+        self.cell_g = None if cd is None else np.ascontiguousarray(cd, np.float64)
 
     def _struct(self):
         s = _World()
@@ -106,6 +111,8 @@ class OracleWorld:
         s.n_angles = self.ab.shape[0]
         s.angle_beads, s.angle_kappa, s.angle_theta0 = _ptr(self.ab), _ptr(self.ak), _ptr(self.at)
         s.stationary = self.stationary
+        s.cell_conservative = None if self.cell_a is None else _ptr(self.cell_a)
+        s.cell_dissipative = None if self.cell_g is None else _ptr(self.cell_g)
         return s
 
     def run(self, nsteps, nthreads=1):

@@ -194,8 +194,17 @@ static void *force_worker(void *arg)
                             double inv_dr = 1.0 / dr;
                             uint32_t hh = w->hash[h], ho = w->hash[o];
                             uint32_t th = hh >> 28, to = ho >> 28;
-                            double con_strength = w->conservative[th * nt + to];
-                            double sqrt_diss = sqrt(w->dissipative[th * nt + to]);
+                            double con_strength, sqrt_diss;
+                            if (w->cell_conservative) {
+                                /* per-cell strengths, averaged over the two beads' cells
+                                   (naive_dpd_engine_half_merge.hpp:221-236, 570-583) */
+                                const size_t n2 = (size_t)nt * nt, k = (size_t)th * nt + to;
+                                con_strength = (w->cell_conservative[c * n2 + k] + w->cell_conservative[oc * n2 + k]) * 0.5;
+                                sqrt_diss = (sqrt(w->cell_dissipative[c * n2 + k]) + sqrt(w->cell_dissipative[oc * n2 + k])) * 0.5;
+                            } else {
+                                con_strength = w->conservative[th * nt + to];
+                                sqrt_diss = sqrt(w->dissipative[th * nt + to]);
+                            }
                             double dv[3];
                             for (int d = 0; d < 3; d++) dv[d] = w->v[3 * h + d] - w->v[3 * o + d];
                             double wr = 1.0 - dr;
@@ -453,6 +462,10 @@ static void *obs_worker(void *arg)
                             double dr = sqrt(dr2);
                             uint32_t th = w->hash[h] >> 28, to = w->hash[o] >> 28;
                             double a = w->conservative[th * nt + to];
+                            if (w->cell_conservative) { /* spatial: mean of the two cells' values */
+                                const size_t n2 = (size_t)nt * nt, k = (size_t)th * nt + to;
+                                a = (w->cell_conservative[c * n2 + k] + w->cell_conservative[oc * n2 + k]) * 0.5;
+                            }
                             vir += a * (1.0 - dr) * dr; /* r . F^C = a (1-r) r */
                             if (job->rdf) {
                                 uint32_t lo = th < to ? th : to, hi = th < to ? to : th;

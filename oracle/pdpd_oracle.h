@@ -41,6 +41,9 @@ typedef struct pdo_world {
     const uint32_t *angle_beads; /* 3*n_angles: head, middle, tail */
     const double *angle_kappa, *angle_theta0;
     uint32_t stationary;         /* bit k set: bead type k is stationary (BeadType::stationary) */
+    /* Spatially varying strengths (NULL: the matrices above everywhere): per cell (x-major, z
+       fastest) n_types^2 values of a_ij and of gamma_ij. */
+    const double *cell_conservative, *cell_dissipative;
 } pdo_world;
 
 /* hash.hpp:20-30 */

@@ -20,6 +20,15 @@
 //   ref_harness v2binary <in.pdw1> <out.bin>
 //       write_world_state(binary=true) (dpd_state_io.hpp:408-466): the reference's own
 //       v2binary snapshot of the world as read.
+//   ref_harness stepx <engine> <in.pdw1> <exprs.txt> <out.bin> <n_checkpoints> <steps...>
+//       As step, with the interaction strengths replaced by Parameter expressions read from
+//       exprs.txt (n^2 conservative lines, then n^2 dissipative lines, row-major) -- the
+//       reference's spatially varying DPD parameters (expression.hpp:328-431).
+//   ref_harness tables <in.pdw1> <exprs.txt> <out.bin>
+//       The per-cell values of those expressions, evaluated as the half-merge engine does at
+//       Attach (naive_dpd_engine_half_merge.hpp:221-236: x, y, z = cell coordinates,
+//       ux = (x + 0.5) / Lx, ...): for each cell (x-major, z fastest) n^2 conservative then
+//       n^2 dissipative doubles.
 //   ref_harness v2read <in.v2> <out.bin>
 //       read_world_state (dpd_state_io.hpp:481-586) of a v2binary file; dump t, x, v, f.
 
@@ -40,6 +49,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "pdw1_read.hpp"
@@ -147,6 +157,77 @@ int cmd_v2binary(int argc, char **argv)
     return 0;
 }
 
+void load_exprs(WorldState &s, const char *path)
+{
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("cannot open expressions");
+    const size_t n2 = s.interactions.size();
+    std::vector<std::string> lines;
+    std::string line;
+    while (std::getline(in, line))
+        if (!line.empty()) lines.push_back(line);
+    if (lines.size() != 2 * n2) throw std::runtime_error("expression file needs 2 n^2 lines");
+    for (size_t k = 0; k < n2; k++) {
+        s.interactions[k].conservative = Parameter(lines[k]);
+        s.interactions[k].dissipative = Parameter(lines[n2 + k]);
+    }
+}
+
+int cmd_stepx(int argc, char **argv)
+{
+    if (argc < 7) throw std::runtime_error("usage: stepx engine in exprs out n steps...");
+    std::string engine_name = argv[2];
+    WorldState s = read_pdw1(argv[3]);
+    load_exprs(s, argv[4]);
+    FILE *out = fopen(argv[5], "wb");
+    if (!out) throw std::runtime_error("cannot open output");
+    unsigned n = atoi(argv[6]);
+    auto e = make_engine(engine_name);
+    std::string why = e->CanSupport(&s);
+    if (!why.empty()) throw std::runtime_error("CanSupport: " + why);
+    e->Attach(&s);
+    unsigned done = 0;
+    for (unsigned k = 0; k < n; k++) {
+        unsigned target = atoi(argv[7 + k]);
+        if (target > done) e->Run(target - done);
+        done = target;
+        dump(out, s);
+    }
+    fclose(out);
+    return 0;
+}
+
+int cmd_tables(int argc, char **argv)
+{
+    if (argc < 5) throw std::runtime_error("usage: tables in exprs out");
+    WorldState s = read_pdw1(argv[2]);
+    load_exprs(s, argv[3]);
+    FILE *out = fopen(argv[4], "wb");
+    if (!out) throw std::runtime_error("cannot open output");
+    const int L[3] = {(int)s.box[0], (int)s.box[1], (int)s.box[2]};
+    for (int x = 0; x < L[0]; x++)
+        for (int y = 0; y < L[1]; y++)
+            for (int z = 0; z < L[2]; z++) {
+                std::unordered_map<std::string, double> b;
+                b["x"] = x;
+                b["y"] = y;
+                b["z"] = z;
+                b["ux"] = (x + 0.5) / s.box[0];
+                b["uy"] = (y + 0.5) / s.box[1];
+                b["uz"] = (z + 0.5) / s.box[2];
+                for (auto &ii : s.interactions) {
+                    double a = ii.conservative.evaluate(b);
+                    fwrite(&a, 8, 1, out);
+                }
+                for (auto &ii : s.interactions) {
+                    double g = ii.dissipative.evaluate(b);
+                    fwrite(&g, 8, 1, out);
+                }
+            }
+    fclose(out);
+    return 0;
+}
+
 int cmd_v2read(int argc, char **argv)
 {
     if (argc < 4) throw std::runtime_error("usage: v2read in out");
@@ -171,6 +252,8 @@ int main(int argc, char **argv)
         if (cmd == "time") return cmd_time(argc, argv);
         if (cmd == "v2binary") return cmd_v2binary(argc, argv);
         if (cmd == "v2read") return cmd_v2read(argc, argv);
+        if (cmd == "stepx") return cmd_stepx(argc, argv);
+        if (cmd == "tables") return cmd_tables(argc, argv);
         throw std::runtime_error("unknown command " + cmd);
     } catch (std::exception &e) {
         fprintf(stderr, "ref_harness: %s\n", e.what());

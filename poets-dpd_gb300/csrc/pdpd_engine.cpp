@@ -166,7 +166,7 @@ struct pdpd_engine {
     DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
-    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
@@ -220,7 +220,7 @@ struct pdpd_engine {
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
-                          &d_v2err};
+                          &d_v2err, &d_cellpair};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -229,6 +229,12 @@ struct pdpd_engine {
     }
 
     bool fp64() const { return precision == PDPD_FP64; }
+    bool any_spatial() const
+    {
+        for (const WorldHost &wh : worlds)
+            if (wh.dev.spatial) return true;
+        return false;
+    }
 
     // ---- step sequences ------------------------------------------------------------------
     int enqueue_begin(cudaStream_t s)
@@ -311,10 +317,11 @@ struct pdpd_engine {
     int configure_bricks()
     {
         KArgs &a = args;
-        a.force_kernel = cfg_force_kernel;
+        // worlds with per-cell strengths run on the thread-per-bead kernel
+        a.force_kernel = any_spatial() ? 1 : cfg_force_kernel;
         a.bricks = nullptr;
         a.n_bricks = 0;
-        if (fp64() || cfg_force_kernel == 1) return PDPD_OK;
+        if (fp64() || a.force_kernel == 1) return PDPD_OK;
         std::vector<Brick> bricks;
         for (uint32_t i = 0; i < worlds.size(); i++) {
             const int32_t *L = worlds[i].dev.L;
@@ -366,7 +373,7 @@ struct pdpd_engine {
                                       {0, 2, 4, 4}, {0, 4, 4, 4}, {3, 2, 4, 4}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
-        if (!cfg_autotune || tuned || fp64() || n_steps < (trial + 1) * n_cand + 1) return 0;
+        if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;
         const int keep[4] = {cfg_force_kernel, cfg_brick[0], cfg_brick[1], cfg_brick[2]};
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
@@ -463,6 +470,16 @@ static int check_world(const pdpd_world *w, char *reason, size_t n, bool need_be
     for (uint32_t i = 0; i < w->n_bead_types * w->n_bead_types; i++)
         if (!(w->dissipative[i] >= 0) || !std::isfinite(w->conservative[i]))
             return say(PDPD_E_INVALID, "Interaction strengths must be finite and gamma >= 0.");
+    if (!w->cell_conservative != !w->cell_dissipative)
+        return say(PDPD_E_INVALID, "Per-cell strengths need both a_ij and gamma_ij tables.");
+    if (w->cell_conservative) {
+        const uint64_t nv = cells * (uint64_t)w->n_bead_types * w->n_bead_types;
+        if (nv >= (1ull << 32)) return say(PDPD_E_UNSUPPORTED, "Per-cell strength tables larger than 2^32 entries.");
+        for (uint64_t k = 0; k < nv; k++)
+            if (!std::isfinite(w->cell_conservative[k]) || !(w->cell_dissipative[k] >= 0) ||
+                !std::isfinite(w->cell_dissipative[k]))
+                return say(PDPD_E_INVALID, "Per-cell interaction strengths must be finite and gamma >= 0.");
+    }
     if (w->n_beads && (!w->hash || (need_beads && (!w->x || !w->v || !w->f))))
         return say(PDPD_E_INVALID, "Missing bead arrays.");
     for (uint32_t i = 0; i < w->n_beads; i++)
@@ -645,6 +662,8 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         d.stationary = 0;
         for (uint32_t k = 0; w.stationary && k < w.n_bead_types; k++)
             if (w.stationary[k]) d.stationary |= 1u << k;
+        d.spatial = w.cell_conservative ? 1u : 0u;
+        d.cellpair_base = 0;
         d.dt = w.dt;
         d.scale_inv_sqrt_dt = std::sqrt(24 * 1.0 / w.dt);  // pow_half(24 kT / dt)
         d.seed = w.seed;
@@ -667,6 +686,27 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         e->worlds.push_back(wh);
     }
     e->n_tiles = (uint32_t)tiles.size();
+
+    // --- per-cell strengths of spatial worlds: (a_ij, sqrt(gamma_ij)) per (cell, type pair)
+    std::vector<double> cp64;
+    std::vector<float> cp32;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        if (!w.cell_conservative) continue;
+        wdev[i].cellpair_base = f64 ? cp64.size() / 2 : cp32.size() / 2;
+        e->worlds[i].dev.cellpair_base = wdev[i].cellpair_base;
+        const uint64_t nv = (uint64_t)wdev[i].n_cells * w.n_bead_types * w.n_bead_types;
+        for (uint64_t k = 0; k < nv; k++) {
+            const double a = w.cell_conservative[k], sg = std::sqrt(w.cell_dissipative[k]);
+            if (f64) {
+                cp64.push_back(a);
+                cp64.push_back(sg);
+            } else {
+                cp32.push_back((float)a);
+                cp32.push_back((float)sg);
+            }
+        }
+    }
 
     // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
     // the flat list order.
@@ -744,6 +784,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_bond_terms, sizeof(BondTerm) * std::max<uint64_t>(1, n_terms));
     A(e->d_bond_params, (f64 ? sizeof(double) : sizeof(float)) * 4 * std::max<uint64_t>(1, n_bparams));
     A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
+    A(e->d_cellpair, std::max<size_t>(16, f64 ? sizeof(double) * cp64.size() : sizeof(float) * cp32.size()));
     A(e->d_hash, sizeof(uint32_t) * nb);
     // Polymer beads (monomer bit of the hash clear), for the FP32 bond kernel.
     std::vector<uint32_t> bonded;
@@ -797,9 +838,11 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     if (f64) {
         H2D(e->d_bond_params, bp64.data(), sizeof(double) * bp64.size());
         H2D(e->d_pair, pair64.data(), sizeof(double) * pair64.size());
+        H2D(e->d_cellpair, cp64.data(), sizeof(double) * cp64.size());
     } else {
         H2D(e->d_bond_params, bp32.data(), sizeof(float) * bp32.size());
         H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
+        H2D(e->d_cellpair, cp32.data(), sizeof(float) * cp32.size());
     }
     if (!any_kept) {
         H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
@@ -855,6 +898,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     a.bond_terms = e->d_bond_terms.as<BondTerm>();
     a.bond_params = e->d_bond_params.p;
     a.pair = e->d_pair.p;
+    a.cellpair = e->d_cellpair.p;
     a.bonded_ids = e->d_bonded.as<uint32_t>();
     a.n_bonded = f64 ? 0u : (uint32_t)bonded.size();
     a.fbond = e->d_fbond.as<float4>();
@@ -1477,7 +1521,7 @@ namespace {
 
 struct ServerJob {
     uint64_t id = 0;
-    std::vector<double> cons, diss, x, v, f, bk, br, ak, at;
+    std::vector<double> cons, diss, x, v, f, bk, br, ak, at, cell_a, cell_g;
     std::vector<uint8_t> stat;
     std::vector<uint32_t> hash, bb, ab;
     pdpd_world desc{};
@@ -1845,6 +1889,11 @@ int pdpd_server_submit(pdpd_server *s, const pdpd_world *w, uint32_t n_steps, pd
         j->bk.assign(w->bond_kappa, w->bond_kappa + w->n_bonds);
         j->br.assign(w->bond_r0, w->bond_r0 + w->n_bonds);
     }
+    if (w->cell_conservative) {
+        const size_t nv = (size_t)w->box[0] * w->box[1] * w->box[2] * nt * nt;
+        j->cell_a.assign(w->cell_conservative, w->cell_conservative + nv);
+        j->cell_g.assign(w->cell_dissipative, w->cell_dissipative + nv);
+    }
     if (w->n_angles) {
         j->ab.assign(w->angle_beads, w->angle_beads + 3 * (size_t)w->n_angles);
         j->ak.assign(w->angle_kappa, w->angle_kappa + w->n_angles);
@@ -1866,6 +1915,8 @@ int pdpd_server_submit(pdpd_server *s, const pdpd_world *w, uint32_t n_steps, pd
     d.angle_beads = j->ab.data();
     d.angle_kappa = j->ak.data();
     d.angle_theta0 = j->at.data();
+    d.cell_conservative = w->cell_conservative ? j->cell_a.data() : nullptr;
+    d.cell_dissipative = w->cell_conservative ? j->cell_g.data() : nullptr;
     j->n_steps = n_steps;
     j->t = w->t;
     j->cb = cb;

@@ -343,9 +343,12 @@ __device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
                                               const float4 ph, const float4 vh, uint32_t ti,
                                               uint32_t nt, const float2 *__restrict__ pair,
                                               uint32_t th_lo, uint32_t th_hi, float scale,
-                                              float F[3])
+                                              float F[3], const float2 *__restrict__ cp = nullptr,
+                                              uint32_t hc = 0, const uint32_t *__restrict__ cellg = nullptr,
+                                              uint32_t cell_base = 0)
 {
     const uint32_t hh = __float_as_uint(ph.w);
+    const uint32_t n2 = nt * nt;
     for (int k = 0; k < n; k++) {
         const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
         const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
@@ -356,8 +359,13 @@ __device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
         float dx, dy, dz;
         const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
         const uint32_t hj = __float_as_uint(pj.w);
-        pair_accumulate(dx, dy, dz, r2, vh, vel[j], hh, hj, pair[ti * nt + min(hj >> 28, nt - 1u)],
-                        th_lo, th_hi, scale, F);
+        const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
+        float2 pp = pair[pk];
+        if (cp) {  // spatial strengths: mean of the two beads' cell values
+            const float2 h = cp[(size_t)hc * n2 + pk], o = cp[(size_t)(cellg[j] - cell_base) * n2 + pk];
+            pp = make_float2(__fmul_rn(__fadd_rn(h.x, o.x), 0.5f), __fmul_rn(__fadd_rn(h.y, o.y), 0.5f));
+        }
+        pair_accumulate(dx, dy, dz, r2, vh, vel[j], hh, hj, pp, th_lo, th_hi, scale, F);
     }
 }
 
@@ -379,6 +387,8 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
     const uint32_t ti = min(__float_as_uint(ph.w) >> 28, nt - 1u);
     const float min2 = min_dist_sqr_f();
     const float PRUNE = 1.0001f;
+    const float2 *cp = w.spatial ? (const float2 *)a.cellpair + w.cellpair_base : nullptr;
+    const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
     F[0] = F[1] = F[2] = 0.f;
     int n = 0;
     for (int ddx = -1; ddx <= 1; ddx++) {
@@ -407,7 +417,7 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
                     if (r2 < 1.0f && r2 >= min2) {
                         if (n == cap) {
                             list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo,
-                                          th_hi, scale, F);
+                                          th_hi, scale, F, cp, hc, a.cellg, w.cell_base);
                             n = 0;
                         }
                         s_j[n * TILE_BEADS + threadIdx.x] = j;
@@ -418,7 +428,8 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
             }
         }
     }
-    list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo, th_hi, scale, F);
+    list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo, th_hi, scale, F, cp, hc,
+                  a.cellg, w.cell_base);
 }
 
 template <int FINAL>

@@ -197,10 +197,13 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
                                               const WorldDev &w, const int c[3],
                                               const double xh[3], const Vec4d &vh, uint32_t hh,
                                               uint32_t ti, const Vec2d *__restrict__ pair,
+                                              const Vec2d *__restrict__ cp, uint32_t hc,
+                                              const uint32_t *__restrict__ cellg,
                                               uint32_t th_lo, uint32_t th_hi,
                                               double scale_inv_sqrt_dt, double F[3])
 {
     const uint32_t nt = w.n_types;
+    const uint32_t n2 = nt * nt;
     for (int k = 0; k < n; k++) {
         const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
         const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
@@ -214,7 +217,13 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
         const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
         const double dr = sqrt(dr2);
         const uint32_t hj = hash_of(pj);
-        const Vec2d pp = pair[ti * nt + min(hj >> 28, nt - 1u)];
+        const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
+        Vec2d pp = pair[pk];
+        if (cp) {  // spatial strengths: mean of the two beads' cell values (half_merge.hpp:570-583)
+            const Vec2d h = cp[(size_t)hc * n2 + pk], o = cp[(size_t)(cellg[j] - w.cell_base) * n2 + pk];
+            pp.x = (h.x + o.x) * 0.5;
+            pp.y = (h.y + o.y) * 0.5;
+        }
         const double kappa = 0.0, r0 = 0.5;
         const double inv_dr = 1.0 / dr;
         const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
@@ -260,6 +269,8 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
     const double min2 = (double)min_dist_sqr_f();
     const double PRUNE = 1.0 + 1e-9;
     const double o[3] = {xh[0] - (double)c[0], xh[1] - (double)c[1], xh[2] - (double)c[2]};
+    const Vec2d *cp = w.spatial ? (const Vec2d *)a.cellpair + w.cellpair_base : nullptr;
+    const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
     F[0] = F[1] = F[2] = 0.0;
     int n = 0;
     int dir[3];
@@ -283,8 +294,8 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
                     const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
                     if (dr2 >= 1 || dr2 < min2) continue;
                     if (n == cap) {
-                        list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, th_lo,
-                                      th_hi, scale_inv_sqrt_dt, F);
+                        list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, cp, hc,
+                                      a.cellg, th_lo, th_hi, scale_inv_sqrt_dt, F);
                         n = 0;
                     }
                     s_j[n * TILE_BEADS + threadIdx.x] = j;
@@ -294,8 +305,8 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
             }
         }
     }
-    list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, th_lo, th_hi,
-                  scale_inv_sqrt_dt, F);
+    list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, cp, hc, a.cellg, th_lo,
+                  th_hi, scale_inv_sqrt_dt, F);
 }
 
 template <int FINAL>
@@ -725,6 +736,8 @@ extern "C" int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, 
     if (w->stationary)
         for (uint32_t k = 0; k < w->n_bead_types; k++)
             if (w->stationary[k]) return fail(PDPD_E_UNSUPPORTED, "Engine does not support stationary bead types.");
+    if (w->cell_conservative || w->cell_dissipative)
+        return fail(PDPD_E_UNSUPPORTED, "The allocation-free entry point does not support per-cell strengths.");
     if (!(w->dt > 0 && w->dt < 1)) return fail(PDPD_E_INVALID, "pdpd_step_noalloc: dt must be in (0, 1)");
     uint64_t cells = 1;
     for (int k = 0; k < 3; k++) {

@@ -22,10 +22,12 @@ struct WorldDev {
     uint32_t param_base;  // first entry of this world's n_types^2 pair parameters
     uint32_t err;         // device-side error flags (ERR_*)
     uint32_t stationary;  // bit k: bead type k is stationary (not moved; v, f cleared each step)
+    uint32_t spatial;     // 1: per-cell strengths at cellpair[cellpair_base + local cell * n_types^2]
     double dt;
     double scale_inv_sqrt_dt;  // sqrt(24 kT / dt), kT = 1 (dpd_maths_core.hpp:24)
     uint64_t seed;
     int64_t t;
+    uint64_t cellpair_base;
 };
 
 // A run of consecutive sorted bead slots of one world: the unit of work of the step
@@ -99,6 +101,7 @@ struct KArgs {
     const BondTerm *bond_terms;
     const void *bond_params;   // float4 / Vec4d: (kappa, r0 | cos theta0, sin theta0, 0)
     const void *pair;          // float2 / Vec2d: (a_ij, sqrt(gamma_ij))
+    const void *cellpair;      // float2 / Vec2d per (cell, type pair) of spatial worlds
     const uint32_t *bonded_ids;  // ids of the beads that have bond terms (FP32 bond kernel)
     uint32_t n_bonded;
     float4 *fbond;               // FP32: bond force of each bonded bead, by sorted slot

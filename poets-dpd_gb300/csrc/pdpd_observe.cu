@@ -87,8 +87,15 @@ __global__ void __launch_bounds__(128) k_observe(KArgs a, uint32_t world, uint32
                         if (r2 >= 1.0 || r2 <= 0.0) continue;
                         const double r = sqrt(r2);
                         const uint32_t tj = min(hj >> 28, nt - 1u);
-                        const double aij = FP64 ? pair[2 * (w.param_base + ti * nt + tj)]
-                                                : (double)pairf[2 * (w.param_base + ti * nt + tj)];
+                        double aij = FP64 ? pair[2 * (w.param_base + ti * nt + tj)]
+                                          : (double)pairf[2 * (w.param_base + ti * nt + tj)];
+                        if (w.spatial) {  // mean of the two cells' values
+                            const size_t n2 = (size_t)nt * nt, pk = (size_t)ti * nt + tj;
+                            const size_t h = (size_t)w.cellpair_base + (size_t)(a.cellg[s] - w.cell_base) * n2 + pk;
+                            const size_t o = (size_t)w.cellpair_base + (size_t)(nc - w.cell_base) * n2 + pk;
+                            aij = FP64 ? (((const double *)a.cellpair)[2 * h] + ((const double *)a.cellpair)[2 * o]) * 0.5
+                                       : (double)((((const float *)a.cellpair)[2 * h] + ((const float *)a.cellpair)[2 * o]) * 0.5f);
+                        }
                         vir += aij * (1.0 - r) * r;
                         if (rdf) {
                             const uint32_t lo = min(ti, tj), hi2 = max(ti, tj);

@@ -22,6 +22,7 @@
 #include <functional>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "dpd/core/dpd_engine.hpp"
@@ -39,6 +40,7 @@ public:
         std::vector<double> bond_kappa, bond_r0;
         std::vector<uint32_t> angle_beads;
         std::vector<double> angle_kappa, angle_theta0;
+        std::vector<double> cell_conservative, cell_dissipative;  // spatial strengths only
         pdpd_world w{};
     };
 
@@ -61,9 +63,41 @@ public:
         const unsigned nt = s.bead_types.size();
         out.conservative.resize(nt * nt);
         out.dissipative.resize(nt * nt);
-        for (unsigned i = 0; i < nt * nt; i++) {
-            out.conservative[i] = (double)s.interactions.at(i).conservative;
-            out.dissipative[i] = (double)s.interactions.at(i).dissipative;
+        bool spatial = false;
+        for (unsigned i = 0; i < nt * nt; i++)
+            spatial |= !s.interactions.at(i).conservative.is_constant() ||
+                        !s.interactions.at(i).dissipative.is_constant();
+        out.cell_conservative.clear();
+        out.cell_dissipative.clear();
+        if (spatial) {
+            // Per-cell values, evaluated as the half-merge engine does at Attach
+            // (naive_dpd_engine_half_merge.hpp:221-236); the matrices hold cell 0's values.
+            const int L[3] = {(int)s.box[0], (int)s.box[1], (int)s.box[2]};
+            std::unordered_map<std::string, double> b;
+            for (int x = 0; x < L[0]; x++)
+                for (int y = 0; y < L[1]; y++)
+                    for (int z = 0; z < L[2]; z++) {
+                        b["x"] = x;
+                        b["y"] = y;
+                        b["z"] = z;
+                        b["ux"] = (x + 0.5) / s.box[0];
+                        b["uy"] = (y + 0.5) / s.box[1];
+                        b["uz"] = (z + 0.5) / s.box[2];
+                        for (unsigned i = 0; i < nt * nt; i++) {
+                            Parameter pc = s.interactions.at(i).conservative, pd = s.interactions.at(i).dissipative;
+                            out.cell_conservative.push_back(pc.evaluate(b));
+                            out.cell_dissipative.push_back(pd.evaluate(b));
+                        }
+                    }
+            for (unsigned i = 0; i < nt * nt; i++) {
+                out.conservative[i] = out.cell_conservative.empty() ? 0.0 : out.cell_conservative[i];
+                out.dissipative[i] = out.cell_dissipative.empty() ? 0.0 : out.cell_dissipative[i];
+            }
+        } else {
+            for (unsigned i = 0; i < nt * nt; i++) {
+                out.conservative[i] = (double)s.interactions.at(i).conservative;
+                out.dissipative[i] = (double)s.interactions.at(i).dissipative;
+            }
         }
         out.stationary.resize(nt);
         for (unsigned i = 0; i < nt; i++) out.stationary[i] = s.bead_types[i].stationary ? 1 : 0;
@@ -120,6 +154,8 @@ public:
         w.angle_beads = out.angle_beads.data();
         w.angle_kappa = out.angle_kappa.data();
         w.angle_theta0 = out.angle_theta0.data();
+        w.cell_conservative = spatial ? out.cell_conservative.data() : nullptr;
+        w.cell_dissipative = spatial ? out.cell_dissipative.data() : nullptr;
     }
 
     std::string CanSupport(const WorldState *s) const override
@@ -258,6 +294,7 @@ protected:
     bool CanSupportHookeanBonds() const override { return true; }
     bool CanSupportAngleBonds() const override { return true; }
     bool CanSupportStationaryBeadTypes() const override { return true; }
+    bool CanSupportSpatialDPDParameters() const override { return true; }
 
 private:
     int m_precision;

@@ -53,6 +53,7 @@ class PdpdWorld(C.Structure):
         ("bead_stride_bytes", C.c_size_t), ("n_bonds", C.c_uint32), ("bond_beads", C.c_void_p),
         ("bond_kappa", C.c_void_p), ("bond_r0", C.c_void_p), ("n_angles", C.c_uint32),
         ("angle_beads", C.c_void_p), ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p),
+        ("cell_conservative", C.c_void_p), ("cell_dissipative", C.c_void_p),
     ]
 
 
@@ -174,6 +175,11 @@ class _Flat:
                                                             _p(self.bk), _p(self.br))
         s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (self.ab.shape[0], _p(self.ab),
                                                                     _p(self.ak), _p(self.at))
+        cc, cd = getattr(world, "cell_conservative", None), getattr(world, "cell_dissipative", None)
+        self.cell_a = None if cc is None else np.ascontiguousarray(cc, np.float64)
+        self.cell_g = None if cd is None else np.ascontiguousarray(cd, np.float64)
+        s.cell_conservative = None if self.cell_a is None else self.cell_a.ctypes.data
+        s.cell_dissipative = None if self.cell_g is None else self.cell_g.ctypes.data
         self.struct = s
 
 

@@ -79,6 +79,10 @@ class World:
     x: np.ndarray                   # (n, 3) float64
     v: np.ndarray
     f: np.ndarray
+    # spatially varying strengths: per cell (x-major, z fastest) (nt, nt) a_ij and gamma_ij,
+    # or None (the matrices above everywhere)
+    cell_conservative: np.ndarray = None
+    cell_dissipative: np.ndarray = None
 
     @property
     def n_beads(self) -> int:
@@ -102,7 +106,9 @@ class World:
             poly_beads=self.poly_beads.copy(), polymer_id=self.polymer_id.copy(),
             polymer_offset=self.polymer_offset.copy(), bead_type=self.bead_type.copy(),
             polymer_type_of_bead=self.polymer_type_of_bead.copy(),
-            is_monomer=self.is_monomer.copy(), x=self.x.copy(), v=self.v.copy(), f=self.f.copy())
+            is_monomer=self.is_monomer.copy(), x=self.x.copy(), v=self.v.copy(), f=self.f.copy(),
+            cell_conservative=None if self.cell_conservative is None else self.cell_conservative.copy(),
+            cell_dissipative=None if self.cell_dissipative is None else self.cell_dissipative.copy())
 
     def flat_bonds(self):
         """Expand the polymer templates into flat bond and angle lists.

@@ -20,10 +20,12 @@ def world_fixture_names():
                   and not os.path.basename(p).startswith(("merge_", "v2_")))
 
 
-def merge_fixture_names():
-    """Fixtures made by the reference's half-merge engine (worlds with stationary bead types,
-    which the half-step engine does not support): same terms, another summation order."""
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "merge_*.npz")))
+def merge_fixture_names(kind=""):
+    """Fixtures made by the reference's half-merge engine (worlds with stationary bead types or
+    spatially varying strengths, which the half-step engine does not support): same terms,
+    another summation order.  kind: "stationary", "spatial" or "" (all)."""
+    return sorted(os.path.basename(p)[:-4]
+                  for p in glob.glob(os.path.join(GOLDEN, f"merge_{kind}*.npz")))
 
 
 def state_rel_err(a, b):
@@ -36,6 +38,9 @@ def state_rel_err(a, b):
 def load_world_fixture(name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     world = W.read_pdw1(d["world"].tobytes())
+    if "cell_a" in d.files:  # spatially varying strengths, as the reference evaluated them
+        world.cell_conservative = d["cell_a"].copy()
+        world.cell_dissipative = d["cell_g"].copy()
     return world, {k: d[k] for k in ("checkpoints", "t", "x", "v", "f")}
 
 

@@ -7,6 +7,9 @@
 //   adapter_check factories
 //   adapter_check cansupport <engine> <world.pdw1>
 //   adapter_check flatten <world.pdw1> <out.bin>
+//   adapter_check spatial <world.pdw1> <exprs.txt> <out.bin>
+//       strengths replaced by Parameter expressions (n^2 conservative, then n^2 dissipative
+//       lines); prints CanSupport, writes the flattened per-cell tables
 //   adapter_check v2file <world.pdw1> <section.bin> <out.v2>
 //       gb300_v2binary.hpp's file writer around a given BinaryData section
 #include "dpd/core/dpd_state_validator.hpp"
@@ -73,6 +76,30 @@ int main(int argc, char **argv)
                 x.push_back(p[2]);
             }
             put(f, x);
+            fclose(f);
+            return 0;
+        }
+        if (cmd == "spatial" && argc > 4) {
+            WorldState s = pdw1::read_pdw1(argv[2]);
+            std::ifstream in(argv[3]);
+            std::vector<std::string> lines;
+            std::string line;
+            while (std::getline(in, line))
+                if (!line.empty()) lines.push_back(line);
+            const size_t n2 = s.interactions.size();
+            if (lines.size() != 2 * n2) return 2;
+            for (size_t k = 0; k < n2; k++) {
+                s.interactions[k].conservative = Parameter(lines[k]);
+                s.interactions[k].dissipative = Parameter(lines[n2 + k]);
+            }
+            auto e = DPDEngineFactory::create("gb300_dpd_engine_fp64");
+            printf("[%s]\n", e->CanSupport(&s).c_str());
+            GB300DPDEngine::Flat flat;
+            GB300DPDEngine::Flatten(s, flat);
+            FILE *f = fopen(argv[4], "wb");
+            if (!f) return 2;
+            put(f, flat.cell_conservative);
+            put(f, flat.cell_dissipative);
             fclose(f);
             return 0;
         }

@@ -215,6 +215,48 @@ def v2binary_fixture(name, world, note):
     print(f"{name}: {n} beads, {len(v2)} bytes")
 
 
+def spatial_fixture(name, world, cons, diss, checkpoints, note, engine="naive_dpd_engine_half_merge"):
+    """A world with spatially varying interaction strengths (Parameter expressions, n^2
+    conservative and n^2 dissipative strings): the per-cell values the reference evaluates
+    (ref_harness tables) and the reference engine's checkpoints (ref_harness stepx)."""
+    nt = world.n_types
+    tmp_in = os.path.join(HERE, "_sx.pdw1")
+    tmp_ex = os.path.join(HERE, "_sx.txt")
+    tmp_tab = os.path.join(HERE, "_sx.tab")
+    tmp_out = os.path.join(HERE, "_sx.bin")
+    W.write_pdw1(world, tmp_in)
+    with open(tmp_ex, "w") as fh:
+        fh.write("\n".join(list(cons) + list(diss)) + "\n")
+    subprocess.run([HARNESS, "tables", tmp_in, tmp_ex, tmp_tab], check=True)
+    tab = np.fromfile(tmp_tab, np.float64).reshape(-1, 2, nt, nt)
+    subprocess.run([HARNESS, "stepx", engine, tmp_in, tmp_ex, tmp_out, str(len(checkpoints))]
+                   + [str(c) for c in checkpoints], check=True, stderr=subprocess.DEVNULL)
+    data = open(tmp_out, "rb").read()
+    for f in (tmp_in, tmp_ex, tmp_tab, tmp_out):
+        os.remove(f)
+    p = 0
+    ts, xs, vs, fs = [], [], [], []
+    for _ in checkpoints:
+        t = int(np.frombuffer(data, np.int64, 1, p)[0])
+        n = int(np.frombuffer(data, np.uint32, 1, p + 8)[0])
+        p += 12
+        rec = np.frombuffer(data, np.float64, 9 * n, p).reshape(n, 9)
+        p += 72 * n
+        ts.append(t)
+        xs.append(rec[:, 0:3])
+        vs.append(rec[:, 3:6])
+        fs.append(rec[:, 6:9])
+    buf = io.BytesIO()
+    W.write_pdw1(world, buf)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        world=np.frombuffer(buf.getvalue(), np.uint8),
+                        checkpoints=np.array(checkpoints), t=np.array(ts), x=np.stack(xs),
+                        v=np.stack(vs), f=np.stack(fs), cell_a=tab[:, 0], cell_g=tab[:, 1],
+                        exprs=np.array(list(cons) + list(diss)), engine=np.array(engine),
+                        note=np.array(note))
+    print(f"{name}: {world.n_beads} beads, {tab.shape[0]} cells, checkpoints {checkpoints}")
+
+
 def hash_fixture():
     rng = np.random.default_rng(2024)
     n = 4096
@@ -359,6 +401,16 @@ def main():
     save_world_fixture("merge_stationary_anchor", stationary_anchor_world(), [1, 5, 20],
                        "chains with stationary heads bonded to mobile beads, in 8^3 water "
                        "(half-merge engine)", merge)
+    # Spatially varying interaction strengths (half-merge engine, the one that supports them)
+    spatial_fixture("merge_spatial_water", W.make_water(8, seed=6, gen_seed=61),
+                    ["25+50*ux"], ["3+3*uy"], [1, 5, 20],
+                    "8^3 water, a = 25 + 50 ux, gamma = 3 + 3 uy (half-merge engine)")
+    pw = W.make_polymer_box(8, chain_fraction=0.1, seed=7)
+    c3 = ["25", "35", "40+40*uz", "35", "25", "75", "40+40*uz", "75", "25-(x-3.5)*(x-3.5)/4"]
+    d3 = ["3+3*ux", "4.5", "4.5", "4.5", "4.5", "4.5+y/8", "4.5", "4.5+y/8", "4.5"]
+    spatial_fixture("merge_spatial_polymer", pw, c3, d3, [1, 5, 20],
+                    "8^3 W/H/T polymer box with a_WT, a_TT, gamma_WW and gamma_HT varying in space "
+                    "(half-merge engine)")
     # v2binary snapshots (the reference's writer and reader)
     v2binary_fixture("v2_polymer8", W.make_polymer_box(8, chain_fraction=0.1, seed=2),
                      "8^3 polymer box, 10% H-T5 chains, initial state")

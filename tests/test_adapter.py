@@ -110,3 +110,22 @@ def test_v2binary_file_writer_matches_reference(exe, tmp_path, name):
     ps.write_bytes(section)
     run(exe, "v2file", str(pw), str(ps), str(po))
     assert po.read_bytes() == v2
+
+
+@pytest.mark.parametrize("name", ["merge_spatial_water", "merge_spatial_polymer"])
+def test_spatial_parameters_flatten_to_the_reference_cell_values(exe, tmp_path, name):
+    """Spatially varying strengths pass CanSupport and flatten into per-cell tables equal to
+    the values the reference itself evaluates per cell (ref_harness tables)."""
+    d = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    world = W.read_pdw1(d["world"].tobytes())
+    pw, pe, po = tmp_path / "w.pdw1", tmp_path / "e.txt", tmp_path / "o.bin"
+    W.write_pdw1(world, str(pw))
+    pe.write_text("\n".join(str(x) for x in d["exprs"]) + "\n")
+    out = run(exe, "spatial", str(pw), str(pe), str(po))
+    assert "[]" in out
+    data = po.read_bytes()
+    (n,) = struct.unpack_from("<Q", data, 0)
+    ca = np.frombuffer(data, "<f8", n, 8)
+    (m,) = struct.unpack_from("<Q", data, 8 + 8 * n)
+    cg = np.frombuffer(data, "<f8", m, 16 + 8 * n)
+    assert np.array_equal(ca, d["cell_a"].reshape(-1)) and np.array_equal(cg, d["cell_g"].reshape(-1))

@@ -23,7 +23,7 @@ from _helpers import force_rel_err, load_world_fixture, merge_fixture_names, sta
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", merge_fixture_names())
+@pytest.mark.parametrize("name", merge_fixture_names("stationary"))
 def test_fp64_stationary_bit_exact_vs_oracle_and_close_to_half_merge(name):
     world, ref = load_world_fixture(name)
     st = np.asarray(world.stationary, bool)[world.bead_type]
@@ -46,7 +46,7 @@ def test_fp64_stationary_bit_exact_vs_oracle_and_close_to_half_merge(name):
         assert state_rel_err(w.f, ref["f"][k]) < 1e-12
 
 
-@pytest.mark.parametrize("name", merge_fixture_names())
+@pytest.mark.parametrize("name", merge_fixture_names("stationary"))
 @pytest.mark.parametrize("force_kernel", [6, 0, 1])
 def test_fp32_stationary(name, force_kernel):
     world, ref = load_world_fixture(name)

@@ -89,7 +89,7 @@ def test_oracle_replays_reference_testbase_suite():
     assert n_seg == 900
 
 
-@pytest.mark.parametrize("name", merge_fixture_names())
+@pytest.mark.parametrize("name", merge_fixture_names("stationary"))
 def test_oracle_stationary_types_vs_reference_half_merge(name):
     """Stationary bead types against the reference's half-merge engine (the reference engine
     family member that supports them): stationary beads stay exactly where they are with v and
@@ -109,3 +109,26 @@ def test_oracle_stationary_types_vs_reference_half_merge(name):
         assert np.max(np.abs(ow.x - ref["x"][k])) < 1e-12
         assert state_rel_err(ow.v, ref["v"][k]) < 1e-12
         assert state_rel_err(ow.f, ref["f"][k]) < 1e-12
+
+
+@pytest.mark.parametrize("name", merge_fixture_names("spatial"))
+def test_oracle_spatial_strengths_vs_reference_half_merge(name):
+    """Spatially varying interaction strengths (Parameter expressions over the cell position),
+    evaluated per cell by the reference, against the reference's half-merge engine: the pair
+    strength is the mean of the two beads' cell values; agreement to summation-order
+    roundoff."""
+    world, ref = load_world_fixture(name)
+    assert world.cell_conservative is not None
+    ow = O.OracleWorld(world)
+    plain = O.OracleWorld(world.copy())
+    plain.cell_a = plain.cell_g = None  # the constant matrices: must differ (the test bites)
+    prev = 0
+    for k, c in enumerate(ref["checkpoints"]):
+        ow.run(int(c) - prev, nthreads=4)
+        prev = int(c)
+        assert ow.t == ref["t"][k]
+        assert np.max(np.abs(ow.x - ref["x"][k])) < 1e-12
+        assert state_rel_err(ow.v, ref["v"][k]) < 1e-12
+        assert state_rel_err(ow.f, ref["f"][k]) < 1e-12
+    plain.run(int(ref["checkpoints"][0]))
+    assert state_rel_err(plain.f, ref["f"][0]) > 1e-6
