@@ -346,14 +346,16 @@ struct pdpd_engine {
         // Staged-bead capacity: 1.5x the expected halo population of the densest world (at
         // most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
         a.brick_hc_max = (uint32_t)(cfg_brick[0] + 2) * (cfg_brick[1] + 2) * (cfg_brick[2] + 2);
-        // staged-bead capacity: the mean halo population + 8 standard deviations (Poisson) and
-        // a floor of 1.25x the mean; a fuller brick takes the (bit-identical) global path
+        // staged-bead capacity: the mean halo population + 6 standard deviations (Poisson) and
+        // a floor of 1.2x the mean; a fuller brick takes the (bit-identical) global path
         const double mean = max_density * a.brick_hc_max;
-        double want = std::max(mean + 8.0 * std::sqrt(mean), 1.25 * mean) + 32;
+        double want = std::max(mean + 6.0 * std::sqrt(mean), 1.2 * mean) + 32;
         a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
         int grid = 0;
         uint32_t bytes = 0;
-        int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, &grid, &bytes);
+        a.brick_npair = 1;
+        for (const WorldHost &wh : worlds) a.brick_npair = std::max(a.brick_npair, wh.dev.n_types * wh.dev.n_types);
+        int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, a.brick_npair, &grid, &bytes);
         if (rc)
             return fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
                         cudaGetErrorString((cudaError_t)rc));
@@ -369,8 +371,8 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
-        static const int cand[][4] = {{6, 2, 4, 4}, {6, 2, 2, 8}, {6, 4, 4, 4}, {6, 2, 4, 8},
-                                      {0, 2, 4, 4}, {0, 4, 4, 4}, {3, 2, 4, 4}, {1, 4, 4, 4}};
+        static const int cand[][4] = {{6, 4, 4, 4}, {7, 4, 4, 4}, {6, 2, 4, 4}, {7, 2, 4, 4},
+                                      {6, 2, 4, 8}, {0, 4, 4, 4}, {6, 2, 2, 8}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
         if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;

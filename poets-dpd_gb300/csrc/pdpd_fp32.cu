@@ -585,12 +585,12 @@ int launch_begin32(const KArgs &a, cudaStream_t s)
 
 // Set up the brick kernel for a brick shape: opt in to the shared memory it needs and
 // return its persistent grid (resident blocks x SMs) and dynamic shared-memory bytes.
-int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *grid,
+int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
                 uint32_t *smem_bytes)
 {
     int nb = 0;
     if (variant == 5) {
-        const CellLayout C = cell_layout(hc_max, maxb);
+        const CellLayout C = cell_layout(hc_max, maxb, npair);
         cudaError_t e = cudaFuncSetAttribute(k_force32_cells<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_force32_cells<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
@@ -602,7 +602,7 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *
         *smem_bytes = C.bytes;
         return 0;
     }
-    const BrickLayout L = brick_layout(hc_max, maxb, brick_variant_has_list(variant),
+    const BrickLayout L = brick_layout(hc_max, maxb, npair, brick_variant_has_list(variant),
                                        brick_variant_balanced(variant));
     const int bytes = (int)L.bytes;
     void (*k0)(KArgs, BrickLayout) = nullptr;
@@ -640,7 +640,7 @@ int launch_force32(const KArgs &a, int final_step, cudaStream_t s)
 static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
 {
     if (a.force_kernel == 5 && a.n_bricks > 0) {
-        const CellLayout C = cell_layout(a.brick_hc_max, a.brick_maxb);
+        const CellLayout C = cell_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair);
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
         if (final_step)
             k_force32_cells<1><<<grid, BRICK_THREADS, C.bytes, s>>>(a, C);
@@ -650,7 +650,7 @@ static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
     }
     if (a.force_kernel != 1 && a.n_bricks > 0) {
         const int v = a.force_kernel;
-        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, brick_variant_has_list(v),
+        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair, brick_variant_has_list(v),
                                            brick_variant_balanced(v));
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
         void (*k)(KArgs, BrickLayout);

@@ -20,12 +20,11 @@
 
 constexpr int BRICK_THREADS = 128;
 constexpr int BRICK_WARPS = BRICK_THREADS / 32;
-constexpr int BLIST_MAX = 32;
+constexpr int BLIST_MAX = 24;
 constexpr int BRICK_MAX_ROWS = 64;
 
 struct BrickHeader {
     WorldCache wc;
-    float2 pair[MAX_PAIR];
     uint32_t wsum[BRICK_WARPS];
     uint32_t home_rows[BRICK_MAX_ROWS + 1];
 };
@@ -34,7 +33,7 @@ struct BrickHeader {
 // list[BLIST_MAX][BRICK_THREADS].
 struct BrickLayout {
     uint32_t hc_max, maxb;
-    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_list, off_bal, bytes;
+    uint32_t off_pair, off_hstart, off_hslot, off_pos, off_vel, off_list, off_bal, bytes;
 };
 
 // Balanced list evaluation (variant 7): per pass of BRICK_THREADS home beads, the list
@@ -47,13 +46,17 @@ struct BrickBalance {
     float f[3][BRICK_THREADS];      // each owner's force (partial sums of flushed entries in)
 };
 
-__host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, int with_list,
-                                                    int with_balance = 0)
+// npair: the largest n_types^2 of the attached worlds (the staged pair table).
+__host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, uint32_t npair,
+                                                    int with_list, int with_balance = 0)
 {
     BrickLayout L;
     L.hc_max = hc_max;
     L.maxb = maxb;
     uint32_t off = (uint32_t)((sizeof(BrickHeader) + 15) & ~size_t(15));
+    L.off_pair = off;
+    off += 8 * npair;
+    off = (off + 15) & ~15u;
     L.off_hstart = off;
     off += 4 * (hc_max + 1);
     L.off_hslot = off;
@@ -331,14 +334,14 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
             const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
             float dx, dy, dz;
             const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-            if (r2 < 1.0f && r2 >= min2) {
-                if (n == cap) {
-                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
-                    n = 0;
-                }
-                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
-                n++;
+            // the entry is stored whatever the test says (position n is free) and kept by
+            // advancing n: no branch per candidate
+            const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
+            list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+            n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
+            if (n == cap) {
+                brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                n = 0;
             }
         }
     }
@@ -368,6 +371,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
+    float2 *spair = reinterpret_cast<float2 *>(smem_raw + lay.off_pair);
     uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
     uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
     float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
     const int cap = (a.list_capacity > 0 && a.list_capacity < BLIST_MAX) ? a.list_capacity : BLIST_MAX;
     for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi += gridDim.x) {
         const Brick br = a.bricks[bi];
-        load_world(a, br.world, H.wc, H.pair);
+        load_world(a, br.world, H.wc, spair);
         __syncthreads();
         const WorldDev &w = H.wc.w;
         const uint32_t nt = w.n_types;
@@ -424,7 +428,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     pi = spos[si];
                     vi = svel[si];
                     n = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, lx + 1, ly + 1, z + 1,
-                                           pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+                                           pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 }
                 if (tid < BLIST_MAX + 2) B.hist[tid] = 0u;
                 B.n[tid] = (uint16_t)n;
@@ -455,7 +459,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     if (no > 0) {
                         const uint32_t so = B.si[o];
                         float G[3] = {B.f[0][o], B.f[1][o], B.f[2][o]};
-                        brick_list_eval_col(spos, svel, list, (int)o, no, spos[so], svel[so], H.pair, nt,
+                        brick_list_eval_col(spos, svel, list, (int)o, no, spos[so], svel[so], spair, nt,
                                             th_lo, th_hi, scale, G);
                         B.f[0][o] = G[0];
                         B.f[1][o] = G[1];
@@ -484,7 +488,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             const uint32_t k = t - H.home_rows[r];
             const uint32_t s = hslot[hc0] + k;
             if (!staged) {  // halo larger than the shared-memory budget: gather from global memory
-                brick_fallback_bead<FINAL>(a, w, H.pair, th_lo, th_hi, scale, s, err);
+                brick_fallback_bead<FINAL>(a, w, spair, th_lo, th_hi, scale, s, err);
                 continue;
             }
             float F[3] = {0.f, 0.f, 0.f};
@@ -498,15 +502,15 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             int n = 0;
             if (FLAT >= 2) {  // variant 6 (and 7 when not staged, never reached)
                 const int nl = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi,
-                                                  vi, H.pair, nt, th_lo, th_hi, scale, F);
-                brick_list_eval(spos, svel, list, nl, pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+                                                  vi, spair, nt, th_lo, th_hi, scale, F);
+                brick_list_eval(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                 integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
                 continue;
             }
             if (FLAT) {
                 brick_gather_flat<LIST>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi, vi,
-                                        H.pair, nt, th_lo, th_hi, scale, F);
+                                        spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                 integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
                 continue;
@@ -533,7 +537,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                             if (r2 < 1.0f && r2 >= min2) {
                                 if (LIST) {
                                     if (n == cap) {
-                                        brick_list_eval(spos, svel, list, n, pi, vi, H.pair, nt, th_lo,
+                                        brick_list_eval(spos, svel, list, n, pi, vi, spair, nt, th_lo,
                                                         th_hi, scale, F);
                                         n = 0;
                                     }
@@ -542,7 +546,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                                 } else {
                                     const uint32_t hj = __float_as_uint(pj.w);
                                     pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
-                                                    H.pair[ti * nt + min(hj >> 28, nt - 1u)], th_lo,
+                                                    spair[ti * nt + min(hj >> 28, nt - 1u)], th_lo,
                                                     th_hi, scale, F);
                                 }
                             }
@@ -550,7 +554,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     }
                 }
             }
-            if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, H.pair, nt, th_lo, th_hi, scale, F);
+            if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, spair, nt, th_lo, th_hi, scale, F);
             const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
             integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
         }
@@ -584,15 +588,18 @@ struct CellWarp {
 
 struct CellLayout {
     uint32_t hc_max, maxb;
-    uint32_t off_hstart, off_hslot, off_pos, off_vel, off_f, off_warp, bytes;
+    uint32_t off_pair, off_hstart, off_hslot, off_pos, off_vel, off_f, off_warp, bytes;
 };
 
-__host__ __device__ inline CellLayout cell_layout(uint32_t hc_max, uint32_t maxb)
+__host__ __device__ inline CellLayout cell_layout(uint32_t hc_max, uint32_t maxb, uint32_t npair)
 {
     CellLayout L;
     L.hc_max = hc_max;
     L.maxb = maxb;
     uint32_t off = (uint32_t)((sizeof(BrickHeader) + 15) & ~size_t(15));
+    L.off_pair = off;
+    off += 8 * npair;
+    off = (off + 15) & ~15u;
     L.off_hstart = off;
     off += 4 * (hc_max + 1);
     L.off_hslot = off;
@@ -660,6 +667,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
+    float2 *spair = reinterpret_cast<float2 *>(smem_raw + lay.off_pair);
     uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
     uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
     float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
@@ -674,7 +682,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
     const float min2 = min_dist_sqr_f();
     for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi += gridDim.x) {
         const Brick br = a.bricks[bi];
-        load_world(a, br.world, H.wc, H.pair);
+        load_world(a, br.world, H.wc, spair);
         __syncthreads();
         const WorldDev &w = H.wc.w;
         const uint32_t nt = w.n_types;
@@ -736,7 +744,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
                                     if (r2 < 1.0f && r2 >= min2) {
                                         const uint32_t hj = __float_as_uint(pj.w);
                                         pair_accumulate(dx, dy, dz, r2, vi, svel[j], hi, hj,
-                                                        H.pair[ti * nt + min(hj >> 28, nt - 1u)],
+                                                        spair[ti * nt + min(hj >> 28, nt - 1u)],
                                                         th_lo, th_hi, scale, F);
                                     }
                                 }
@@ -795,7 +803,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
                         qn += __popc(mask);
                         __syncwarp();
                         if (qn >= 32) {
-                            cell_eval_queue(cw, lane, 32, spos, svel, h0, H.pair, nt, th_lo, th_hi, scale);
+                            cell_eval_queue(cw, lane, 32, spos, svel, h0, spair, nt, th_lo, th_hi, scale);
                             const uint32_t moved = lane + 32 < qn ? cw.queue[lane + 32] : 0u;
                             __syncwarp();
                             if (lane + 32 < qn) cw.queue[lane] = moved;
@@ -805,7 +813,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
                     }
                     __syncwarp();
                 }
-                if (qn > 0) cell_eval_queue(cw, lane, qn, spos, svel, h0, H.pair, nt, th_lo, th_hi, scale);
+                if (qn > 0) cell_eval_queue(cw, lane, qn, spos, svel, h0, spair, nt, th_lo, th_hi, scale);
                 for (uint32_t i = lane; i < nh; i += 32) {
                     sfx[h0 + i] = cw.fh[0][i];
                     sfy[h0 + i] = cw.fh[1][i];
@@ -831,7 +839,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
                 int c[3];
                 decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
                 float F[3] = {0.f, 0.f, 0.f};
-                pair_forces32_seq(a, w, H.pair, th_lo, th_hi, scale, c, ph, vh, F);
+                pair_forces32_seq(a, w, spair, th_lo, th_hi, scale, c, ph, vh, F);
                 integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
                 continue;
             }

@@ -54,7 +54,7 @@ struct Brick {
 };
 
 // Default brick shape (cells), the autotuner's usual pick on GB300; bx * by <= 64.
-constexpr int BRICK_X = 2, BRICK_Y = 4, BRICK_Z = 4;
+constexpr int BRICK_X = 4, BRICK_Y = 4, BRICK_Z = 4;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
@@ -117,6 +117,7 @@ struct KArgs {
     int brick_grid;      // persistent grid size of the brick kernel
     uint32_t brick_hc_max;  // halo cells of the nominal brick shape
     uint32_t brick_maxb;    // staged-bead capacity of one brick
+    uint32_t brick_npair;   // staged pair-table entries: the largest n_types^2 of the worlds
 };
 
 // Kernel launchers.  Each returns the number of kernels it launched.
@@ -144,7 +145,7 @@ int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uin
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
 
 size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
-int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, int *grid,
+int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
                 uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
 
