@@ -13,6 +13,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -39,6 +40,25 @@ namespace {
 double now_s()
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// fn(begin, end) over [0, n) on up to 16 host threads (chunks of at least min_chunk items):
+// the per-bead host packing and unpacking of large worlds.
+template <class F> void parallel_for(size_t n, size_t min_chunk, F fn)
+{
+    size_t nt = std::min<size_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    nt = std::min(nt, std::max<size_t>(1, n / std::max<size_t>(1, min_chunk)));
+    if (nt <= 1) {
+        fn((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t per = (n + nt - 1) / nt;
+    for (size_t k = 0; k < nt; k++) {
+        const size_t b = std::min(n, k * per), e = std::min(n, b + per);
+        if (b < e) th.emplace_back([=] { fn(b, e); });
+    }
+    for (auto &t : th) t.join();
 }
 
 // Device buffer that keeps its allocation while a request fits (bytes = capacity), so that a
@@ -816,18 +836,20 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             for (uint32_t k = 0; k < w.n_beads; k++) hh[bb + k] = w.hash[k];
             continue;
         }
-        for (uint32_t k = 0; k < w.n_beads; k++) {
-            const double *x = vec_at(w.x, w.bead_stride_bytes, k);
-            const double *v = vec_at(w.v, w.bead_stride_bytes, k);
-            const double *f = vec_at(w.f, w.bead_stride_bytes, k);
-            double *o = hs + 9 * (size_t)(bb + k);
-            for (int d = 0; d < 3; d++) {
-                o[d] = x[d];
-                o[3 + d] = v[d];
-                o[6 + d] = f[d];
+        parallel_for(w.n_beads, 1 << 16, [&, bb](size_t k0, size_t k1) {
+            for (size_t k = k0; k < k1; k++) {
+                const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
+                const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
+                const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
+                double *o = hs + 9 * (size_t)(bb + k);
+                for (int d = 0; d < 3; d++) {
+                    o[d] = x[d];
+                    o[3 + d] = v[d];
+                    o[6 + d] = f[d];
+                }
+                hh[bb + k] = w.hash[k];
             }
-            hh[bb + k] = w.hash[k];
-        }
+        });
     }
     cudaStream_t s = e->stream;
     auto H2D = [&](DevBuf &b, const void *src, size_t n) {
@@ -997,12 +1019,14 @@ static int download(pdpd_engine *e, int buf, cudaStream_t s)
 static void scatter(const double *src, uint32_t n, double *x, double *v, double *f, size_t stride)
 {
     size_t sb = stride ? stride : 3 * sizeof(double);
-    for (uint32_t i = 0; i < n; i++) {
-        const double *r = src + 9 * (size_t)i;
-        if (x) memcpy((char *)x + sb * i, r, 3 * sizeof(double));
-        if (v) memcpy((char *)v + sb * i, r + 3, 3 * sizeof(double));
-        if (f) memcpy((char *)f + sb * i, r + 6, 3 * sizeof(double));
-    }
+    parallel_for(n, 1 << 16, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; i++) {
+            const double *r = src + 9 * i;
+            if (x) memcpy((char *)x + sb * i, r, 3 * sizeof(double));
+            if (v) memcpy((char *)v + sb * i, r + 3, 3 * sizeof(double));
+            if (f) memcpy((char *)f + sb * i, r + 6, 3 * sizeof(double));
+        }
+    });
 }
 
 int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
@@ -1437,10 +1461,16 @@ int pdpd_v2binary_encode(pdpd_engine *e, uint32_t world, uint8_t *out, size_t ca
     e->launches += launch_v2_encode(e->args, e->fp64(), world, wd.n_beads, L->d_buf.as<uint8_t>(),
                                     L->d_off.as<uint32_t>(), e->d_v2err.as<uint32_t>(), e->stream);
     if (ce == cudaSuccess) ce = cudaGetLastError();
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(out, L->d_buf.p, L->bytes, cudaMemcpyDeviceToHost, e->stream);
-    if (ce == cudaSuccess) ce = cudaMemcpyAsync(&herr, e->d_v2err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+    // through pinned staging (a copy to pageable memory would be staged by the driver)
+    if (e->h_staging[1].alloc(L->bytes + 16) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    uint32_t *herr_p = (uint32_t *)((uint8_t *)e->h_staging[1].p + ((L->bytes + 3) & ~size_t(3)));
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(e->h_staging[1].p, L->d_buf.p, L->bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(herr_p, e->d_v2err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
     if (ce != cudaSuccess) return e->cuda_fail(ce, "v2binary encode");
+    herr = *herr_p;
+    const uint8_t *src = (const uint8_t *)e->h_staging[1].p;
+    parallel_for(L->bytes, 1 << 22, [&](size_t b, size_t en) { memcpy(out + b, src + b, en - b); });
     if (herr & 2u) return e->fail(PDPD_E_INVALID, "Bead is out of bounds.");
     if (herr & 1u)
         return e->fail(PDPD_E_INVALID, "A velocity or force is not finite or has magnitude 65536 or more "

@@ -373,19 +373,21 @@ class GB300DPDEngine:
                                                 _p(ps), _p(pb), C.byref(size)), "v2binary_prepare")
         return int(size.value)
 
-    def v2binary_encode(self, world_index=0) -> bytes:
-        """The BinaryData section of the world's current state, encoded on the GPU."""
+    def v2binary_encode(self, world_index=0) -> np.ndarray:
+        """The BinaryData section of the world's current state, encoded on the GPU (uint8
+        array; ``.tobytes()`` for bytes)."""
         size = C.c_size_t(0)
         self._check(lib().pdpd_v2binary_encode(self._h, world_index, None, 0, C.byref(size)),
                     "v2binary_encode")
         out = np.empty(max(1, size.value), np.uint8)
         self._check(lib().pdpd_v2binary_encode(self._h, world_index, out.ctypes.data, out.size,
                                                C.byref(size)), "v2binary_encode")
-        return out[:size.value].tobytes()
+        return out[:size.value]
 
-    def v2binary_decode(self, section: bytes, world_index=0):
-        """Set the world's x, v, f from a BinaryData section (decoded on the GPU)."""
-        buf = np.frombuffer(section, np.uint8)
+    def v2binary_decode(self, section, world_index=0):
+        """Set the world's x, v, f from a BinaryData section (bytes or uint8 array), decoded
+        on the GPU."""
+        buf = np.ascontiguousarray(np.frombuffer(section, np.uint8))
         self._check(lib().pdpd_v2binary_decode(self._h, world_index, buf.ctypes.data if buf.size else None,
                                                buf.size), "v2binary_decode")
         if self._worlds:

@@ -38,14 +38,12 @@ MAX_POLYMER_OFFSET = 127
 
 def bead_hash(bead_type, is_monomer, polymer_id, polymer_offset):
     """Vectorised ``BeadHash::construct`` (dpd_state.hpp:52-60)."""
-    bead_type = np.asarray(bead_type, dtype=np.uint64)
-    is_monomer = np.asarray(is_monomer, dtype=np.uint64)
-    polymer_id = np.asarray(polymer_id, dtype=np.uint64)
-    polymer_offset = np.asarray(polymer_offset, dtype=np.uint64)
-    h = (polymer_offset << np.uint64(POLYMER_OFFSET_SHIFT)) | polymer_id
-    h |= is_monomer << np.uint64(MONOMER_FLAG_SHIFT)
-    h |= bead_type << np.uint64(BEAD_TYPE_SHIFT)
-    return (h & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    # 32-bit arithmetic: bits shifted past bit 31 are dropped, as in the 32-bit hash
+    h = np.asarray(polymer_offset).astype(np.uint32) << np.uint32(POLYMER_OFFSET_SHIFT)
+    h |= np.asarray(polymer_id).astype(np.uint32)
+    h |= np.asarray(is_monomer).astype(np.uint32) << np.uint32(MONOMER_FLAG_SHIFT)
+    h |= np.asarray(bead_type).astype(np.uint32) << np.uint32(BEAD_TYPE_SHIFT)
+    return h
 
 
 @dataclass

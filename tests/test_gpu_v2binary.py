@@ -20,7 +20,7 @@ def test_fp64_encode_equals_reference_writer(name):
     eng = E.GB300DPDEngine("fp64")
     eng.Attach(world.copy())
     assert eng.v2binary_prepare() == len(section)
-    assert eng.v2binary_encode() == section
+    assert eng.v2binary_encode().tobytes() == section
 
 
 @pytest.mark.parametrize("name", v2_fixture_names())
@@ -36,7 +36,7 @@ def test_decode_equals_reference_reader(name):
     eng.v2binary_prepare()
     eng.v2binary_decode(section)
     assert np.array_equal(w.x, x) and np.array_equal(w.v, v) and np.array_equal(w.f, f)
-    assert eng.v2binary_encode() == section  # the decoded state re-encodes to the same bytes
+    assert eng.v2binary_encode().tobytes() == section  # the decoded state re-encodes to the same bytes
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
@@ -47,7 +47,7 @@ def test_encode_after_a_run_equals_oracle_codec(prec):
     eng.Attach(w)
     eng.v2binary_prepare()
     eng.Run(25)  # w now holds the engine's x, v, f
-    assert eng.v2binary_encode() == V.encode_section(w)
+    assert eng.v2binary_encode().tobytes() == V.encode_section(w)
 
 
 def test_non_sequential_polymer_ids_and_batches():
@@ -59,8 +59,8 @@ def test_non_sequential_polymer_ids_and_batches():
     pids = (np.arange(len(a.poly_type), dtype=np.uint32) * 3 + 7)
     eng.v2binary_prepare(1, polymer_ids=pids)
     eng.v2binary_prepare(0)
-    assert eng.v2binary_encode(1) == V.encode_section(a, polymer_ids=pids)
-    assert eng.v2binary_encode(0) == V.encode_section(b)
+    assert eng.v2binary_encode(1).tobytes() == V.encode_section(a, polymer_ids=pids)
+    assert eng.v2binary_encode(0).tobytes() == V.encode_section(b)
 
 
 def test_round_trip_large_box():
@@ -73,10 +73,10 @@ def test_round_trip_large_box():
     n = eng.v2binary_prepare()
     eng.Run(20)
     x0, v0, f0 = w.x.copy(), w.v.copy(), w.f.copy()
-    sec = eng.v2binary_encode()
+    sec = eng.v2binary_encode().tobytes()
     assert len(sec) == n
     eng.v2binary_decode(sec)
-    assert eng.v2binary_encode() == sec
+    assert eng.v2binary_encode().tobytes() == sec
     d = np.abs(w.x - x0)
     d = np.minimum(d, np.asarray(w.box, float) - d)
     assert d.max() <= 0.5 / 65536 + 1e-12
@@ -100,7 +100,7 @@ def test_errors():
     eng2 = E.GB300DPDEngine("fp64")
     eng2.Attach(good)
     eng2.v2binary_prepare()
-    sec = bytearray(eng2.v2binary_encode())
+    sec = bytearray(eng2.v2binary_encode().tobytes())
     sec[0] ^= 1  # first polymer header: another polymer type
     with pytest.raises(RuntimeError, match="structure"):
         eng2.v2binary_decode(bytes(sec))
