@@ -62,15 +62,18 @@ template <class F> void parallel_for(size_t n, size_t min_chunk, F fn)
 }
 
 // Device buffer that keeps its allocation while a request fits (bytes = capacity), so that a
-// re-attach of a batch of similar size allocates nothing.
+// re-attach of a batch of similar size allocates nothing.  A buffer that has to grow takes
+// half as much again as asked (a growing batch re-allocates a few times, not at every re-pack).
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
     cudaError_t alloc(size_t n)
     {
         if (p && n <= bytes) return cudaSuccess;
+        const bool grow = p != nullptr;
         release();
         if (n == 0) n = 16;
+        if (grow) n += n / 2;
         cudaError_t e = cudaMalloc(&p, n);
         if (e != cudaSuccess) {
             p = nullptr;
@@ -94,6 +97,7 @@ struct HostPinned {
     cudaError_t alloc(size_t n)
     {
         if (n <= bytes) return cudaSuccess;
+        if (p) n += n / 2;  // pinning is slow: grow by half again
         release();
         cudaError_t e = cudaMallocHost(&p, n);
         if (e != cudaSuccess) {
@@ -470,7 +474,10 @@ struct pdpd_engine {
 // ------------------------------------------------------------------------------------------
 // validation
 
-static int check_world(const pdpd_world *w, char *reason, size_t n, bool need_beads = true)
+// fresh: the world's beads come from its descriptor (bead arrays required, every element
+// checked); false for a world re-packed from the device, whose descriptor was checked when it
+// was first attached.
+static int check_world(const pdpd_world *w, char *reason, size_t n, bool fresh = true)
 {
     auto say = [&](int code, const char *msg) {
         if (reason && n) snprintf(reason, n, "%s", msg);
@@ -497,21 +504,22 @@ static int check_world(const pdpd_world *w, char *reason, size_t n, bool need_be
     if (w->cell_conservative) {
         const uint64_t nv = cells * (uint64_t)w->n_bead_types * w->n_bead_types;
         if (nv >= (1ull << 32)) return say(PDPD_E_UNSUPPORTED, "Per-cell strength tables larger than 2^32 entries.");
-        for (uint64_t k = 0; k < nv; k++)
+        for (uint64_t k = 0; fresh && k < nv; k++)
             if (!std::isfinite(w->cell_conservative[k]) || !(w->cell_dissipative[k] >= 0) ||
                 !std::isfinite(w->cell_dissipative[k]))
                 return say(PDPD_E_INVALID, "Per-cell interaction strengths must be finite and gamma >= 0.");
     }
-    if (w->n_beads && (!w->hash || (need_beads && (!w->x || !w->v || !w->f))))
+    if (w->n_beads && (!w->hash || (fresh && (!w->x || !w->v || !w->f))))
         return say(PDPD_E_INVALID, "Missing bead arrays.");
-    for (uint32_t i = 0; i < w->n_beads; i++)
-        if ((w->hash[i] >> 28) >= w->n_bead_types) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
     if (w->n_bonds && (!w->bond_beads || !w->bond_kappa || !w->bond_r0))
         return say(PDPD_E_INVALID, "Missing bond arrays.");
-    for (uint32_t k = 0; k < 2 * w->n_bonds; k++)
-        if (w->bond_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Bond refers to a bead that does not exist.");
     if (w->n_angles && (!w->angle_beads || !w->angle_kappa || !w->angle_theta0))
         return say(PDPD_E_INVALID, "Missing angle-bond arrays.");
+    if (!fresh) return PDPD_OK;
+    for (uint32_t i = 0; i < w->n_beads; i++)
+        if ((w->hash[i] >> 28) >= w->n_bead_types) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
+    for (uint32_t k = 0; k < 2 * w->n_bonds; k++)
+        if (w->bond_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Bond refers to a bead that does not exist.");
     for (uint32_t k = 0; k < 3 * w->n_angles; k++)
         if (w->angle_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Angle bond refers to a bead that does not exist.");
     return PDPD_OK;
@@ -732,16 +740,39 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
 
     // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
     // the flat list order.
-    std::vector<uint32_t> row(nb + 1, 0);
-    for (uint32_t i = 0; i < n_worlds; i++) {
+    // (no bond terms at all, e.g. pure water: the rows are all zero and are set on the device)
+    std::vector<uint32_t> row(n_terms ? nb + 1 : 0, 0);
+    for (uint32_t i = 0; n_terms && i < n_worlds; i++) {
         const pdpd_world &w = ws[i];
         uint32_t bb = wdev[i].bead_base;
         for (uint32_t k = 0; k < 2 * w.n_bonds; k++) row[bb + w.bond_beads[k] + 1]++;
         for (uint32_t k = 0; k < 3 * w.n_angles; k++) row[bb + w.angle_beads[k] + 1]++;
     }
-    for (uint64_t i = 0; i < nb; i++) row[i + 1] += row[i];
+    if (n_terms) {  // inclusive prefix of row[1..nb] in parallel chunks: chunk sums, then offsets
+        const size_t n = nb, chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
+        const size_t per = (n + chunks - 1) / chunks;
+        std::vector<uint32_t> part(chunks + 1, 0);
+        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
+            for (size_t c = c0; c < c1; c++) {
+                uint32_t acc = 0;
+                for (size_t i = c * per; i < std::min(n, (c + 1) * per); i++) acc += row[i + 1];
+                part[c + 1] = acc;
+            }
+        });
+        for (size_t c = 0; c < chunks; c++) part[c + 1] += part[c];
+        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
+            for (size_t c = c0; c < c1; c++) {
+                uint32_t acc = part[c];
+                for (size_t i = c * per; i < std::min(n, (c + 1) * per); i++) row[i + 1] = acc += row[i + 1];
+            }
+        });
+    }
     std::vector<BondTerm> terms(n_terms);
-    std::vector<uint32_t> fill(row.begin(), row.end() - 1);
+    std::vector<uint32_t> fill(n_terms ? nb : 0);
+    if (n_terms)
+        parallel_for(nb, 1 << 18, [&](size_t i0, size_t i1) {
+            memcpy(fill.data() + i0, row.data() + i0, sizeof(uint32_t) * (i1 - i0));
+        });
     std::vector<double> bp64;
     std::vector<float> bp32;
     uint32_t pidx = 0;
@@ -810,9 +841,18 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_hash, sizeof(uint32_t) * nb);
     // Polymer beads (monomer bit of the hash clear), for the FP32 bond kernel.
     std::vector<uint32_t> bonded;
-    for (uint32_t i = 0; i < n_worlds; i++)
-        for (uint32_t k = 0; k < ws[i].n_beads; k++)
-            if (!(ws[i].hash[k] & (1u << 27))) bonded.push_back(wdev[i].bead_base + k);
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        const uint32_t n = ws[i].n_beads, bb = wdev[i].bead_base;
+        const size_t chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
+        const size_t per = (n + chunks - 1) / chunks;
+        std::vector<std::vector<uint32_t>> part(chunks);
+        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
+            for (size_t c = c0; c < c1; c++)
+                for (size_t k = c * per; k < std::min<size_t>(n, (c + 1) * per); k++)
+                    if (!(ws[i].hash[k] & (1u << 27))) part[c].push_back(bb + (uint32_t)k);
+        });
+        for (const auto &p : part) bonded.insert(bonded.end(), p.begin(), p.end());
+    }
     A(e->d_bonded, sizeof(uint32_t) * std::max<size_t>(1, bonded.size()));
     A(e->d_fbond, f64 ? 16 : sizeof(float4) * std::max<uint64_t>(1, nb));
     A(e->d_staging[0], sizeof(double) * 9 * nb);
@@ -833,7 +873,9 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         const pdpd_world &w = ws[i];
         uint32_t bb = wdev[i].bead_base;
         if (keep_old && keep_old[i] >= 0) {  // bead state comes from the old arena (below)
-            for (uint32_t k = 0; k < w.n_beads; k++) hh[bb + k] = w.hash[k];
+            parallel_for(w.n_beads, 1 << 18, [&, bb](size_t k0, size_t k1) {
+                memcpy(hh + bb + k0, w.hash + k0, sizeof(uint32_t) * (k1 - k0));
+            });
             continue;
         }
         parallel_for(w.n_beads, 1 << 16, [&, bb](size_t k0, size_t k1) {
@@ -857,7 +899,10 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     };
     H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
     H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
-    H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
+    if (n_terms)
+        H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
+    else if (ce == cudaSuccess)
+        ce = cudaMemsetAsync(e->d_bond_row.p, 0, sizeof(uint32_t) * (nb + 1), s);
     H2D(e->d_bond_terms, terms.data(), sizeof(BondTerm) * n_terms);
     if (f64) {
         H2D(e->d_bond_params, bp64.data(), sizeof(double) * bp64.size());
