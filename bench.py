@@ -281,16 +281,42 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
 
 
 def dist_setup(n_gpus):
+    """One process per GPU under torchrun: (rank, world_size, local rank).  Replicas only: the
+    ranks exchange nothing but the barrier and the max-over-ranks time (NCCL on GPUs, gloo
+    where there is no GPU, e.g. the CPU tests of this path)."""
     rank, world_size = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
     if world_size > 1:
         import torch
         import torch.distributed as dist
 
         local = int(os.environ.get("LOCAL_RANK", rank))
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if not dist.is_initialized():
+            if torch.cuda.is_available():
+                torch.cuda.set_device(local)
+                dist.init_process_group("nccl")
+            else:
+                dist.init_process_group("gloo")
         return rank, world_size, local
     return 0, 1, 0
+
+
+def max_over_ranks(x: float, world_size: int) -> float:
+    """The largest of the ranks' values (the job's time is its slowest replica's)."""
+    if world_size <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, ms: float, world_size: int) -> float:
+    """Whole-job throughput: every rank processed units_per_rank in at most ms."""
+    return world_size * units_per_rank / (ms / 1e3)
 
 
 def run_reference_arm(args):
@@ -387,13 +413,8 @@ def run_engine_arm(args):
         torch.cuda.synchronize()
         time.sleep(0.2)
     launches = eng.kernel_launches() - launches0
-    ms = ev0.elapsed_time(ev1)
-    if world_size > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        ms = float(t.item())
-    value = world_size * n * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world_size)
+    value = aggregate_rate(n * args.steps, ms, world_size)
 
     # --- dominant kernel: per-phase CUDA-event times over the same number of steps
     phases = eng.profile_run(args.steps)
