@@ -197,7 +197,7 @@ def batched_grid_metrics(steps=200, plain_steps=10, n_states=512, device=0):
 
 
 def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed=5, device=0,
-                    seq_fp32=8, seq_fp64=4):
+                    seq_fp32=16, seq_fp64=4):
     """Serving stream: Poisson arrivals at `rate` jobs/s for `window_s` seconds (seeded).  Each
     job is pure DPD water (density 3, a = 25, gamma = 4.5, dt = 0.02) in a cube of side
     log-uniform on [8, 64] (rounded), n_steps uniform on 100..2000, a host callback every
@@ -274,7 +274,9 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
             "latency_max_s": st["latency_max_s"], "max_active_jobs": st["max_active"],
             "repacks": st["repacks"] - st0["repacks"],
-            "repack_s": st["repack_s"] - st0["repack_s"], "gpu_launches": launches,
+            "repack_s": st["repack_s"] - st0["repack_s"],
+            "wasted_bead_steps": st["wasted_bead_steps"] - st0["wasted_bead_steps"],
+            "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,
             "served_vs_sequential_fp32": served / seq32, "served_vs_sequential_fp64": served / seq64}

@@ -287,6 +287,8 @@ typedef struct pdpd_server_stats {
     double wall_s;         /* first submit to last completion */
     double latency_p50_s, latency_p99_s, latency_max_s;  /* submit -> final callback done */
     double repack_s;       /* host wall time spent in re-packs */
+    uint64_t wasted_bead_steps;  /* steps of ended jobs' worlds kept in the batch until the
+                                    next re-pack (not counted in bead_steps) */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.

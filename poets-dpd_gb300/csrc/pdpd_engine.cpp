@@ -1612,6 +1612,7 @@ struct ServerJob {
     bool stopped = false;    // no further callbacks: the callback asked to stop, or it failed
     bool ended = false;      // final state delivered or owed; the world leaves the batch at the
                              // next point where every running job is at an interval boundary
+    bool leave_now = false;  // ended, and stepping it on to that point costs more than a re-pack
 };
 
 // A callback owed for one job: its rows start at `row` in host snapshot buffer `buf`.
@@ -1657,6 +1658,8 @@ struct pdpd_server {
     std::vector<Delivery> owed;
     int owed_buf = 0;
     bool changed = false;
+    double rate_est = 2e9;        // bead-steps per second of recent epochs
+    double repack_est_s = 0.005;  // recent re-pack time
     HostPinned snap[2];
     cudaEvent_t ev_unsorted = nullptr, ev_copied[2] = {nullptr, nullptr};
     std::thread worker;
@@ -1703,6 +1706,7 @@ int pdpd_server::repack()
     std::lock_guard<std::mutex> lk(mu);
     st.repacks++;
     st.repack_s += t_repack;
+    repack_est_s = 0.7 * repack_est_s + 0.3 * t_repack;
     return PDPD_OK;
 }
 
@@ -1780,15 +1784,15 @@ void pdpd_server::run()
             bool in_phase = true;
             for (auto &j : active)
                 if (!j->ended) in_phase &= j->done % interval == 0;
+            for (size_t i = 0; i < active.size();)
+                if (active[i]->ended && (in_phase || active[i]->leave_now)) {
+                    retiring.push_back(std::move(active[i]));
+                    active.erase(active.begin() + i);
+                    changed = true;
+                } else {
+                    i++;
+                }
             if (in_phase) {
-                for (size_t i = 0; i < active.size();)
-                    if (active[i]->ended) {
-                        retiring.push_back(std::move(active[i]));
-                        active.erase(active.begin() + i);
-                        changed = true;
-                    } else {
-                        i++;
-                    }
                 size_t used = 0;
                 for (auto &j : active) used += j->bytes;
                 while (!pending.empty() && (active.empty() || used + pending.front()->bytes <= budget)) {
@@ -1816,6 +1820,7 @@ void pdpd_server::run()
         for (auto &j : active)
             if (!j->ended) epoch = std::min({epoch, interval - j->done % interval, j->n_steps - j->done});
         if (epoch == UINT32_MAX) epoch = 0;  // only ended jobs: they leave at the next iteration
+        const double t_epoch0 = now_s();
         if (epoch > 0) {
             rc = pdpd_run_async(eng, epoch);
             std::vector<size_t> at_boundary;
@@ -1872,13 +1877,30 @@ void pdpd_server::run()
                 pdpd_attach(eng, nullptr);
                 changed = false;
             }
+            uint64_t stepped = 0, live_phase = 0;
             {
                 std::lock_guard<std::mutex> lk(mu);
-                for (auto &j : active)
+                for (auto &j : active) {
+                    stepped += (uint64_t)j->desc.n_beads * epoch;
                     if (!j->ended) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
+                    else st.wasted_bead_steps += (uint64_t)j->desc.n_beads * epoch;
+                }
             }
-            for (auto &j : active)
+            const double dt_epoch = now_s() - t_epoch0;
+            if (stepped && dt_epoch > 0) rate_est = 0.7 * rate_est + 0.3 * (double)stepped / dt_epoch;
+            for (auto &j : active) {
                 if (j->done == j->n_steps) j->ended = true;  // final state is owed
+                if (!j->ended) live_phase = j->done % interval;
+            }
+            // Ended worlds step on until the live jobs reach their next interval boundary; when
+            // that costs more than an early re-pack, they leave at once.
+            uint64_t zombie = 0;
+            const uint64_t rem = live_phase ? interval - live_phase : 0;
+            for (auto &j : active)
+                if (j->ended) zombie += (uint64_t)j->desc.n_beads * rem;
+            if (zombie && (double)zombie / rate_est > repack_est_s)
+                for (auto &j : active)
+                    if (j->ended) j->leave_now = true;
             owed.swap(next);
             owed_buf = b;
             b ^= 1;
