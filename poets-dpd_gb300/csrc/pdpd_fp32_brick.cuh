@@ -329,6 +329,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
         const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : hstart[rowc + 2];
         const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
         const uint32_t dbase = (uint32_t)(rr * 3) << 11;
+#pragma unroll 2
         for (uint32_t j = j0; j < j1; j++) {
             const float4 pj = spos[j];
             const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
