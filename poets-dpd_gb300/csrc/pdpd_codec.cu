@@ -90,10 +90,11 @@ template <int FP64>
 __global__ void k_v2_encode(KArgs a, uint32_t world, uint32_t n, uint8_t *__restrict__ buf,
                             const uint32_t *__restrict__ off, uint32_t *err)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
     const WorldDev &w = a.worlds[world];
-    const uint32_t s = a.slot_of_id[w.bead_base + i];
+    const uint32_t s = w.bead_base + k;        // walk the world's slots (coalesced reads)
+    const uint32_t i = a.ids[s] - w.bead_base;  // the bead in slot s: its record
     double x[3], v[3], f[3];
     if (FP64) {
         const Vec4d p = ((const Vec4d *)a.posA)[s], vv = ((const Vec4d *)a.velA)[s],

@@ -91,7 +91,7 @@ struct KArgs {
     void *posA, *velA, *frc;
     uint32_t *ids;       // bead id of each sorted slot
     uint32_t *cellg;     // global cell of each sorted slot
-    uint32_t *slot_of_id;
+    uint32_t *slot_of_id;   // sorted slot of each polymer bead, by id (monomers: not kept)
     // advanced, not yet sorted state (B), indexed by the A slot it came from
     void *posB, *velB, *frcB;
     uint2 *keyrank;      // (new global cell, arrival rank in that cell)

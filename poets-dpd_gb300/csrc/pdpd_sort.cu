@@ -120,6 +120,18 @@ __global__ void k_place(uint32_t n, const uint2 *__restrict__ keyrank,
     tmp[dst] = make_uint4(s, ids[s], kr.x, 0u);
 }
 
+// The bead hash carried in the w component of a position payload.
+__device__ __forceinline__ uint32_t payload_hash(const float4 &p)
+{
+    return __float_as_uint(p.w);
+}
+__device__ __forceinline__ uint32_t payload_hash(const Vec4d &p)
+{
+    return (uint32_t)__double_as_longlong(p.w);
+}
+
+// slot_of_id is kept for polymer beads only (monomer bit of the hash clear): the bond kernels
+// look up bond partners through it; the codec walks slots and reads ids instead.
 template <class P>
 __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_t *__restrict__ start,
                         const P *__restrict__ pos_in, const P *__restrict__ vel_in,
@@ -135,12 +147,13 @@ __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_
     uint32_t rank = 0;
     for (uint32_t k = b; k < end; k++) rank += tmp[k].y < e.y ? 1u : 0u;
     uint32_t dst = b + rank;
-    pos_out[dst] = pos_in[e.x];
+    const P p = pos_in[e.x];
+    pos_out[dst] = p;
     vel_out[dst] = vel_in[e.x];
     if (frc_in) frc_out[dst] = frc_in[e.x];
     ids_out[dst] = e.y;
     cellg_out[dst] = e.z;
-    slot_of_id[e.y] = dst;
+    if (!(payload_hash(p) & (1u << 27))) slot_of_id[e.y] = dst;
 }
 
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s)
