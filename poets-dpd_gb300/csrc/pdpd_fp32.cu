@@ -224,12 +224,11 @@ __device__ __forceinline__ void pair_accumulate(float dx, float dy, float dz, fl
                                   __fmaf_rn(ey, __fsub_rn(vi.y, vj.y), __fmul_rn(ex, __fsub_rn(vi.x, vj.x))));
     const float sg = __fmul_rn(pp.y, wr);
     const float u = hash_u(th_lo, th_hi, hi, hj);
-    const float con = __fmul_rn(pp.x, wr);
-    const float diss = __fmul_rn(__fmul_rn(sg, sg), rdotv);
-    const float scaled = __fmaf_rn(__fmul_rn(sg, scale), u, __fsub_rn(con, diss));
-    F[0] = __fadd_rn(F[0], __fmul_rn(ex, scaled));
-    F[1] = __fadd_rn(F[1], __fmul_rn(ey, scaled));
-    F[2] = __fadd_rn(F[2], __fmul_rn(ez, scaled));
+    const float con_m_diss = __fmaf_rn(-__fmul_rn(sg, sg), rdotv, __fmul_rn(pp.x, wr));
+    const float scaled = __fmaf_rn(__fmul_rn(sg, scale), u, con_m_diss);
+    F[0] = __fmaf_rn(ex, scaled, F[0]);
+    F[1] = __fmaf_rn(ey, scaled, F[1]);
+    F[2] = __fmaf_rn(ez, scaled, F[2]);
 }
 
 // Bonds, update_mom and either the final write or the next update_pos with the cell count,
