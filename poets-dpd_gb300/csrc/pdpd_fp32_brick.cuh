@@ -20,7 +20,7 @@
 
 constexpr int BRICK_THREADS = 128;
 constexpr int BRICK_WARPS = BRICK_THREADS / 32;
-constexpr int BLIST_MAX = 24;
+constexpr int BLIST_MAX = 32;
 constexpr int BRICK_MAX_ROWS = 64;
 
 struct BrickHeader {
@@ -301,8 +301,9 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
 // a row's 3 cells (dz = -1, 0, +1) are one contiguous range of staged beads, trimmed at its
 // ends by the same conservative test as the per-cell loop.  The warp pays the longest row of
 // its lanes 9 times instead of the longest cell 27 times.  The in-range candidates go to this
-// thread's list in the direction order (a full list is evaluated into F first); returns the
-// number of entries left in the list.
+// thread's list in the direction order; room for a whole row is made before the row (the list
+// is evaluated into F first when it could overflow), so the candidate loop has no capacity
+// check and no branch.  Returns the number of entries left in the list.
 __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spos,
                                                   const float4 *__restrict__ svel,
                                                   uint16_t *__restrict__ list, int cap,
@@ -329,20 +330,34 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
         const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : hstart[rowc + 2];
         const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
         const uint32_t dbase = (uint32_t)(rr * 3) << 11;
+        if (n + (int)(j1 - j0) > cap) {  // room for the whole row, or evaluate the list first
+            brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+            n = 0;
+        }
+        if ((int)(j1 - j0) <= cap) {
 #pragma unroll 2
-        for (uint32_t j = j0; j < j1; j++) {
-            const float4 pj = spos[j];
-            const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
-            float dx, dy, dz;
-            const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-            // the entry is stored whatever the test says (position n is free) and kept by
-            // advancing n: no branch per candidate
-            const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-            list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
-            n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
-            if (n == cap) {
-                brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
-                n = 0;
+            for (uint32_t j = j0; j < j1; j++) {
+                const float4 pj = spos[j];
+                const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
+                float dx, dy, dz;
+                const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
+                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
+            }
+        } else {
+            for (uint32_t j = j0; j < j1; j++) {
+                const float4 pj = spos[j];
+                const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
+                float dx, dy, dz;
+                const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
+                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
+                if (n == cap) {
+                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    n = 0;
+                }
             }
         }
     }
