@@ -54,7 +54,7 @@ struct Brick {
 };
 
 // Default brick shape (cells), the autotuner's usual pick on GB300; bx * by <= 64.
-constexpr int BRICK_X = 4, BRICK_Y = 4, BRICK_Z = 4;
+constexpr int BRICK_X = 3, BRICK_Y = 4, BRICK_Z = 6;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
