@@ -145,11 +145,12 @@ const ConfigEntry kConfig[] = {
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
-    {"force_kernel", "FP32 force kernel (default 6): 0 = shared-memory brick with neighbour lists, "
+    {"force_kernel", "FP32 force kernel (default 8): 0 = shared-memory brick with neighbour lists, "
                      "1 = thread per bead from global memory, 2 = shared-memory brick, "
                      "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence, "
                      "5 = warp per home cell, 6 = as 0 with the neighbour cells walked row by row, "
-                     "7 = as 6 with the lists evaluated balanced across lanes."},
+                     "7 = as 6 with the lists evaluated balanced across lanes, "
+                     "8 = as 6 with 512-thread blocks for larger bricks."},
     {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
@@ -174,7 +175,7 @@ struct pdpd_engine {
     int cfg_grid_blocks = 0;
     int cfg_graph_steps = 0;
     int cfg_use_graphs = 1;
-    int cfg_force_kernel = 6;
+    int cfg_force_kernel = 8;
     int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
     int cfg_autotune = 0;
     bool tuned = false;
@@ -395,8 +396,8 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
-        static const int cand[][4] = {{6, 3, 4, 6}, {6, 3, 3, 8}, {6, 4, 4, 6}, {7, 3, 3, 8},
-                                      {6, 4, 4, 4}, {6, 2, 4, 8}, {0, 3, 4, 6}, {1, 4, 4, 4}};
+        static const int cand[][4] = {{8, 4, 8, 8}, {8, 6, 8, 6}, {8, 4, 6, 10}, {6, 3, 4, 6},
+                                      {6, 3, 3, 8}, {7, 3, 3, 8}, {6, 4, 4, 6}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
         if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;
@@ -1222,7 +1223,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
     else if (k == "force_kernel") {
-        if (v > 7) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..7");
+        if (v > 8) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..8");
         e->cfg_force_kernel = (int)v;
     } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {
         int idx = k == "brick_x" ? 0 : (k == "brick_y" ? 1 : 2);

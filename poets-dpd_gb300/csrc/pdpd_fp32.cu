@@ -602,7 +602,7 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint3
         return 0;
     }
     const BrickLayout L = brick_layout(hc_max, maxb, npair, brick_variant_has_list(variant),
-                                       brick_variant_balanced(variant));
+                                       brick_variant_balanced(variant), brick_variant_threads(variant));
     const int bytes = (int)L.bytes;
     void (*k0)(KArgs, BrickLayout) = nullptr;
     void (*k1)(KArgs, BrickLayout) = nullptr;
@@ -612,11 +612,16 @@ int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint3
     case 3: k0 = k_force32_brick<0, 1, 1>; k1 = k_force32_brick<1, 1, 1>; break;
     case 6: k0 = k_force32_brick<0, 1, 2>; k1 = k_force32_brick<1, 1, 2>; break;
     case 7: k0 = k_force32_brick<0, 1, 3>; k1 = k_force32_brick<1, 1, 3>; break;
+    case 8:
+        k0 = k_force32_brick<0, 1, 2, BRICK_THREADS_WIDE>;
+        k1 = k_force32_brick<1, 1, 2, BRICK_THREADS_WIDE>;
+        break;
     default: k0 = k_force32_brick<0, 0, 1>; k1 = k_force32_brick<1, 0, 1>; break;
     }
     cudaError_t e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k0, BRICK_THREADS, bytes);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k0, (int)brick_variant_threads(variant), bytes);
     if (e != cudaSuccess) return (int)e;
     if (nb < 1) return (int)cudaErrorInvalidConfiguration;
     *grid = nb * sm_count;
@@ -650,7 +655,7 @@ static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
     if (a.force_kernel != 1 && a.n_bricks > 0) {
         const int v = a.force_kernel;
         const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair, brick_variant_has_list(v),
-                                           brick_variant_balanced(v));
+                                           brick_variant_balanced(v), brick_variant_threads(v));
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
         void (*k)(KArgs, BrickLayout);
         switch (v) {
@@ -659,9 +664,12 @@ static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
         case 3: k = final_step ? k_force32_brick<1, 1, 1> : k_force32_brick<0, 1, 1>; break;
         case 6: k = final_step ? k_force32_brick<1, 1, 2> : k_force32_brick<0, 1, 2>; break;
         case 7: k = final_step ? k_force32_brick<1, 1, 3> : k_force32_brick<0, 1, 3>; break;
+        case 8:
+            k = final_step ? k_force32_brick<1, 1, 2, BRICK_THREADS_WIDE> : k_force32_brick<0, 1, 2, BRICK_THREADS_WIDE>;
+            break;
         default: k = final_step ? k_force32_brick<1, 0, 1> : k_force32_brick<0, 0, 1>; break;
         }
-        k<<<grid, BRICK_THREADS, L.bytes, s>>>(a, L);
+        k<<<grid, brick_variant_threads(v), L.bytes, s>>>(a, L);
         return 1;
     }
     if (final_step)

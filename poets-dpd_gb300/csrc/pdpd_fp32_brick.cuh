@@ -18,19 +18,21 @@
 // kernel and the overflow fallback produce bit-identical forces: the same explicitly
 // rounded pair routine, the same order.
 
-constexpr int BRICK_THREADS = 128;
+constexpr int BRICK_THREADS = 128;       // threads per block of variants 0, 2-7
 constexpr int BRICK_WARPS = BRICK_THREADS / 32;
+constexpr int BRICK_THREADS_WIDE = 512;  // threads per block of variant 8 (larger bricks)
+constexpr int BRICK_MAX_WARPS = BRICK_THREADS_WIDE / 32;
 constexpr int BLIST_MAX = 32;
 constexpr int BRICK_MAX_ROWS = 64;
 
 struct BrickHeader {
     WorldCache wc;
-    uint32_t wsum[BRICK_WARPS];
+    uint32_t wsum[BRICK_MAX_WARPS];
     uint32_t home_rows[BRICK_MAX_ROWS + 1];
 };
 
 // Shared-memory layout of one block: header, hstart[HC+1], hslot[HC], pos[maxb], vel[maxb],
-// list[BLIST_MAX][BRICK_THREADS].
+// list[BLIST_MAX][threads].
 struct BrickLayout {
     uint32_t hc_max, maxb;
     uint32_t off_pair, off_hstart, off_hslot, off_pos, off_vel, off_list, off_bal, bytes;
@@ -48,7 +50,8 @@ struct BrickBalance {
 
 // npair: the largest n_types^2 of the attached worlds (the staged pair table).
 __host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t maxb, uint32_t npair,
-                                                    int with_list, int with_balance = 0)
+                                                    int with_list, int with_balance = 0,
+                                                    uint32_t threads = BRICK_THREADS)
 {
     BrickLayout L;
     L.hc_max = hc_max;
@@ -67,7 +70,7 @@ __host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t ma
     L.off_vel = off;
     off += 16 * maxb;
     L.off_list = off;
-    if (with_list) off += 2 * BLIST_MAX * BRICK_THREADS;
+    if (with_list) off += 2 * BLIST_MAX * threads;
     off = (off + 15) & ~15u;
     L.off_bal = off;
     if (with_balance) off += (uint32_t)sizeof(BrickBalance);
@@ -79,7 +82,11 @@ __host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t ma
 // the one that evaluates them balanced across lanes.
 inline int brick_variant_has_list(int variant)
 {
-    return (variant == 0 || variant == 3 || variant == 6 || variant == 7) ? 1 : 0;
+    return (variant == 0 || variant == 3 || variant == 6 || variant == 7 || variant == 8) ? 1 : 0;
+}
+inline uint32_t brick_variant_threads(int variant)
+{
+    return variant == 8 ? BRICK_THREADS_WIDE : BRICK_THREADS;
 }
 inline int brick_variant_balanced(int variant)
 {
@@ -87,6 +94,7 @@ inline int brick_variant_balanced(int variant)
 }
 
 // Evaluate list entries [0, n) of this thread in order, adding to F.
+template <int T = BRICK_THREADS>
 __device__ __forceinline__ void brick_list_eval_col(const float4 *__restrict__ spos,
                                                     const float4 *__restrict__ svel,
                                                     const uint16_t *__restrict__ list, int col, int n,
@@ -97,7 +105,7 @@ __device__ __forceinline__ void brick_list_eval_col(const float4 *__restrict__ s
     const uint32_t hi = __float_as_uint(pi.w);
     const uint32_t ti = min(hi >> 28, nt - 1u);
     for (int k = 0; k < n; k++) {
-        const uint32_t e = list[k * BRICK_THREADS + col];
+        const uint32_t e = list[k * T + col];
         const uint32_t j = e & 2047u, d = e >> 11;  // d = (dx+1)*9 + (dy+1)*3 + (dz+1)
         const float4 pj = spos[j];
         const float ax = __fsub_rn(pi.x, (float)((int)(d / 9u) - 1));
@@ -112,6 +120,7 @@ __device__ __forceinline__ void brick_list_eval_col(const float4 *__restrict__ s
 }
 
 // This thread's own list (column threadIdx.x).
+template <int T = BRICK_THREADS>
 __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
                                                 const float4 *__restrict__ svel,
                                                 const uint16_t *__restrict__ list, int n,
@@ -119,7 +128,7 @@ __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
                                                 const float2 *pair, uint32_t nt, uint32_t th_lo,
                                                 uint32_t th_hi, float scale, float F[3])
 {
-    brick_list_eval_col(spos, svel, list, threadIdx.x, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+    brick_list_eval_col<T>(spos, svel, list, threadIdx.x, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
 // Pair forces of one staged home bead, with the 27 neighbour cells walked as one flat
@@ -129,7 +138,7 @@ __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
 // The sequence -- rows in order, cells in order, beads in order -- is the reference's
 // direction order, and pruned cells (nearest face >= 1 away) hold no in-range bead, so the
 // accumulated force is bit-identical to the nested-loop variants.
-template <int LIST>
+template <int LIST, int T = BRICK_THREADS>
 __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spos,
                                                   const float4 *__restrict__ svel,
                                                   uint16_t *__restrict__ list, int cap,
@@ -174,11 +183,11 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
         if (r2 < 1.0f && r2 >= min2) {
             if (LIST) {
                 if (n == cap) {
-                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
                     n = 0;
                 }
                 const int ddz = j < c1 ? -1 : (j < c2 ? 0 : 1);
-                list[n * BRICK_THREADS + threadIdx.x] =
+                list[n * T + threadIdx.x] =
                     (uint16_t)(j | (uint32_t)(((rdx + 1) * 9 + (rdy + 1) * 3 + (ddz + 1)) << 11));
                 n++;
             } else {
@@ -189,7 +198,7 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
         }
         j++;
     }
-    if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+    if (LIST) brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
 // Halo setup and staging of one brick, block-wide (ends with __syncthreads):
@@ -198,6 +207,7 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
 //   H.home_rows[r] = first home index of home (x, y) row r, and, if the halo fits in maxb,
 //   spos / svel = the halo's beads.  Halo coordinates lie in [-1, L] (bricks are cut at the
 //   box faces), so each wraps with one conditional add or subtract.
+template <int T = BRICK_THREADS>
 __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const WorldDev &w, const Brick &br,
                                                      BrickHeader &H, uint32_t *hstart, uint32_t *hslot,
                                                      float4 *spos, float4 *svel, uint32_t maxb,
@@ -209,7 +219,7 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
     const int L0 = w.L[0], L1 = w.L[1], L2 = w.L[2];
 
     // counts of a contiguous range of halo cells per thread, then a block exclusive scan
-    const int per = (HC + BRICK_THREADS - 1) / BRICK_THREADS;
+    const int per = (HC + T - 1) / T;
     const int hc_begin = min(HC, tid * per), hc_end = min(HC, hc_begin + per);
     uint32_t tsum = 0;
     if (hc_begin < hc_end) {
@@ -248,7 +258,7 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
     if (lane == 31) H.wsum[warp] = inc;
     __syncthreads();
     uint32_t run = inc - tsum, tot = 0;
-    for (int k = 0; k < BRICK_WARPS; k++) {
+    for (int k = 0; k < T / 32; k++) {
         if (k < warp) run += H.wsum[k];
         tot += H.wsum[k];
     }
@@ -273,7 +283,7 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
     // wrap is one contiguous run of slots
     if (tot <= maxb) {
         const bool zrun = br.z0 >= 1 && br.z0 + br.bz + 1 <= L2;
-        for (int row = warp; row < HX * HY; row += BRICK_WARPS) {
+        for (int row = warp; row < HX * HY; row += T / 32) {
             const int hc0 = row * HZ;
             const uint32_t base = hstart[hc0];
             const uint32_t len = hstart[hc0 + HZ] - base;
@@ -304,6 +314,7 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
 // thread's list in the direction order; room for a whole row is made before the row (the list
 // is evaluated into F first when it could overflow), so the candidate loop has no capacity
 // check and no branch.  Returns the number of entries left in the list.
+template <int T = BRICK_THREADS>
 __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spos,
                                                   const float4 *__restrict__ svel,
                                                   uint16_t *__restrict__ list, int cap,
@@ -331,7 +342,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
         const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
         const uint32_t dbase = (uint32_t)(rr * 3) << 11;
         if (n + (int)(j1 - j0) > cap) {  // room for the whole row, or evaluate the list first
-            brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+            brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
             n = 0;
         }
         if ((int)(j1 - j0) <= cap) {
@@ -342,7 +353,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
                 const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                list[n * T + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
                 n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
             }
         } else {
@@ -352,10 +363,10 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
                 const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-                list[n * BRICK_THREADS + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                list[n * T + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
                 n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
                 if (n == cap) {
-                    brick_list_eval(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
                     n = 0;
                 }
             }
@@ -382,8 +393,8 @@ __device__ __forceinline__ void brick_fallback_bead(const KArgs &a, const WorldD
     integrate32<FINAL>(a, w, s, c, ph, vh, F, err);
 }
 
-template <int FINAL, int LIST, int FLAT>
-__global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickLayout lay)
+template <int FINAL, int LIST, int FLAT, int T = BRICK_THREADS>
+__global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
@@ -412,19 +423,19 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
 
         // ---- 1-2. halo cells (hstart, hslot, home rows) and staging
         uint32_t total = 0, n_home = 0;
-        brick_halo_and_stage(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
+        brick_halo_and_stage<T>(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
         const bool staged = total <= lay.maxb;
 
         // ---- 3. one thread per home bead: pair forces, bonds, integration
         uint32_t err = 0;
-        if (FLAT == 3 && staged) {
+        if (FLAT == 3 && T == BRICK_THREADS && staged) {
             // Variant 7, per pass of BRICK_THREADS home beads: (a) each thread walks the rows of
             // its bead into its list; (b) the lists are counting-sorted by length and lane l
             // evaluates list perm[l], so a warp's lanes run lists of about the same length; (c)
             // each thread integrates its own bead.  Every list is still summed by one thread
             // in its own order: the forces are those of the other variants, bit for bit.
             BrickBalance &B = *reinterpret_cast<BrickBalance *>(smem_raw + lay.off_bal);
-            for (uint32_t t0 = 0; t0 < n_home; t0 += BRICK_THREADS) {
+            for (uint32_t t0 = 0; t0 < n_home; t0 += T) {
                 const uint32_t t = t0 + tid;
                 const bool act = t < n_home;
                 float F[3] = {0.f, 0.f, 0.f};
@@ -443,7 +454,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     while (hstart[hc0 + z + 1] <= si) z++;
                     pi = spos[si];
                     vi = svel[si];
-                    n = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, lx + 1, ly + 1, z + 1,
+                    n = brick_rows_collect<T>(spos, svel, list, cap, hstart, HY, HZ, lx + 1, ly + 1, z + 1,
                                            pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 }
                 if (tid < BLIST_MAX + 2) B.hist[tid] = 0u;
@@ -490,12 +501,12 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                     integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
                 }
-                if (t0 + BRICK_THREADS < n_home) __syncthreads();  // the lists are reused
+                if (t0 + T < n_home) __syncthreads();  // the lists are reused
             }
             if (err) atomicOr(&a.worlds[br.world].err, err);
             continue;
         }
-        for (uint32_t t = tid; t < n_home; t += BRICK_THREADS) {
+        for (uint32_t t = tid; t < n_home; t += T) {
             int r = 0;
             while (H.home_rows[r + 1] <= t) r++;
             const int lx = r / br.by, ly = r - lx * br.by;
@@ -517,15 +528,15 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
             const uint32_t ti = min(hi >> 28, nt - 1u);
             int n = 0;
             if (FLAT >= 2) {  // variant 6 (and 7 when not staged, never reached)
-                const int nl = brick_rows_collect(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi,
+                const int nl = brick_rows_collect<T>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi,
                                                   vi, spair, nt, th_lo, th_hi, scale, F);
-                brick_list_eval(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
+                brick_list_eval<T>(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                 integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
                 continue;
             }
             if (FLAT) {
-                brick_gather_flat<LIST>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi, vi,
+                brick_gather_flat<LIST, T>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi, vi,
                                         spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                 integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
@@ -553,11 +564,11 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                             if (r2 < 1.0f && r2 >= min2) {
                                 if (LIST) {
                                     if (n == cap) {
-                                        brick_list_eval(spos, svel, list, n, pi, vi, spair, nt, th_lo,
+                                        brick_list_eval<T>(spos, svel, list, n, pi, vi, spair, nt, th_lo,
                                                         th_hi, scale, F);
                                         n = 0;
                                     }
-                                    list[n * BRICK_THREADS + tid] = (uint16_t)(j | dpk);
+                                    list[n * T + tid] = (uint16_t)(j | dpk);
                                     n++;
                                 } else {
                                     const uint32_t hj = __float_as_uint(pj.w);
@@ -570,7 +581,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_brick(KArgs a, BrickL
                     }
                 }
             }
-            if (LIST) brick_list_eval(spos, svel, list, n, pi, vi, spair, nt, th_lo, th_hi, scale, F);
+            if (LIST) brick_list_eval<T>(spos, svel, list, n, pi, vi, spair, nt, th_lo, th_hi, scale, F);
             const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
             integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
         }

@@ -54,7 +54,7 @@ struct Brick {
 };
 
 // Default brick shape (cells), the autotuner's usual pick on GB300; bx * by <= 64.
-constexpr int BRICK_X = 3, BRICK_Y = 4, BRICK_Z = 6;
+constexpr int BRICK_X = 4, BRICK_Y = 8, BRICK_Z = 8;
 
 enum ErrFlags : uint32_t {
     ERR_BOND_SNAPPED = 1u,  // Hookean bond longer than the maximum bond length
@@ -110,10 +110,11 @@ struct KArgs {
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
-    int force_kernel;    // FP32: 6 (default) = brick kernel, neighbour lists, row walk;
+    int force_kernel;    // FP32: 6 = brick kernel, neighbour lists, row walk (8: the same with
+                         // 512-thread blocks, the default);
                          // 0 = as 6 with a cell walk, 2 = brick kernel without lists,
                          // 3 / 4 = flat walk, 5 = warp per cell, 7 = as 6, balanced lists,
-                         // 1 = thread per bead (global)
+                         // 8 = as 6 with 512-thread blocks, 1 = thread per bead (global)
     int brick_grid;      // persistent grid size of the brick kernel
     uint32_t brick_hc_max;  // halo cells of the nominal brick shape
     uint32_t brick_maxb;    // staged-bead capacity of one brick

@@ -105,7 +105,7 @@ def test_fp64_bit_exact_large_box_one_step():
 
 # ---------------------------------------------------------------------------- FP32
 
-@pytest.mark.parametrize("force_kernel", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("force_kernel", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 @pytest.mark.parametrize("name", [n for n in world_fixture_names() if n != "empty_world"])
 def test_fp32_vs_reference(name, force_kernel):
     world, ref = load_world_fixture(name)
@@ -120,7 +120,7 @@ def test_fp32_vs_reference(name, force_kernel):
     assert np.max(np.abs(dx)) < 1e-6
 
 
-@pytest.mark.parametrize("force_kernel", [0, 1, 5, 6, 7])
+@pytest.mark.parametrize("force_kernel", [0, 1, 5, 6, 7, 8])
 def test_fp32_polymer_box_one_and_ten_steps(force_kernel):
     world = W.make_polymer_box(32, chain_fraction=0.1, seed=2)
     ow = O.OracleWorld(world)
@@ -225,7 +225,9 @@ LAUNCH_CONFIGS = {
              {"force_kernel": 6}, {"force_kernel": 6, "list_capacity": 2},
              {"force_kernel": 6, "brick_x": 3, "brick_y": 5, "brick_z": 7},
              {"force_kernel": 7}, {"force_kernel": 7, "list_capacity": 2},
-             {"force_kernel": 7, "brick_x": 4, "brick_y": 4, "brick_z": 8}),
+             {"force_kernel": 7, "brick_x": 4, "brick_y": 4, "brick_z": 8},
+             {"force_kernel": 8}, {"force_kernel": 8, "brick_x": 4, "brick_y": 8, "brick_z": 8},
+             {"force_kernel": 8, "list_capacity": 3, "brick_x": 3, "brick_y": 5, "brick_z": 7}),
     # The warp-per-cell kernel sums each bead's pairs in a different (but data-determined)
     # order: deterministic and independent of the launch configuration.
     "fp32_cells": ({"force_kernel": 5}, {"force_kernel": 5, "use_graphs": 0},
@@ -269,7 +271,7 @@ def clustered_world():
     return w
 
 
-@pytest.mark.parametrize("force_kernel", [0, 2, 3, 4, 6, 7])
+@pytest.mark.parametrize("force_kernel", [0, 2, 3, 4, 6, 7, 8])
 def test_fp32_brick_overflow_fallback(force_kernel):
     world = clustered_world()
     ref = world.copy()
