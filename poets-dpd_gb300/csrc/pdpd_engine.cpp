@@ -145,13 +145,15 @@ const ConfigEntry kConfig[] = {
     {"grid_blocks", "Persistent grid size of the tile kernels (0 = 16 blocks per SM)."},
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
-    {"force_kernel", "FP32 force kernel (default 8): 0 = shared-memory brick with neighbour lists, "
+    {"force_kernel", "FP32 force kernel (default by size: 8 from about 1,300 cells per SM, else 6): "
+                     "0 = shared-memory brick with neighbour lists, "
                      "1 = thread per bead from global memory, 2 = shared-memory brick, "
                      "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence, "
                      "5 = warp per home cell, 6 = as 0 with the neighbour cells walked row by row, "
                      "7 = as 6 with the lists evaluated balanced across lanes, "
                      "8 = as 6 with 512-thread blocks for larger bricks."},
-    {"brick_x", "Brick extent in cells along x (FP32 brick kernel)."},
+    {"brick_x", "Brick extent in cells along x (FP32 brick kernel; default by size: 4x8x8, "
+                "3x4x6 from about 400 cells per SM, 2x4x4 below)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
     {"autotune", "FP32: time the force-kernel variants and brick shapes on the first steps of "
@@ -178,6 +180,9 @@ struct pdpd_engine {
     int cfg_force_kernel = 8;
     int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
     int cfg_autotune = 0;
+    bool kernel_user = false;  // force_kernel set through the config
+    bool brick_user = false;   // a brick_* entry set through the config
+    bool tuning = false;       // the autotuner is trying candidates
     bool tuned = false;
     std::string tune_log;
     double max_density = 0;
@@ -336,12 +341,31 @@ struct pdpd_engine {
         return PDPD_OK;
     }
 
+    // Default kernel variant and brick shape for the attached batch, where the config does not
+    // name them.  The persistent brick kernels want several bricks per SM: the 512-thread row
+    // walk on 4x8x8 bricks is fastest from about 1,300 cells per SM (a 58^3 box on 152 SMs),
+    // the 128-thread row walk on 3x4x6 bricks from about 400, and on 2x4x4 bricks below that.
+    // All of them give the same trajectory.
+    void default_shape()
+    {
+        uint64_t cells = 0;
+        for (const WorldHost &wh : worlds)
+            cells += (uint64_t)wh.dev.L[0] * (uint64_t)wh.dev.L[1] * (uint64_t)wh.dev.L[2];
+        const uint64_t per_sm = cells / (uint64_t)std::max(1, sm_count);
+        if (!kernel_user) cfg_force_kernel = per_sm >= 1300 ? 8 : 6;
+        if (brick_user) return;
+        static const int big[3] = {4, 8, 8}, mid[3] = {3, 4, 6}, small[3] = {2, 4, 4};
+        const int *b = cfg_force_kernel == 8 || per_sm >= 1300 ? big : (per_sm >= 400 ? mid : small);
+        for (int d = 0; d < 3; d++) cfg_brick[d] = b[d];
+    }
+
     // Build the brick work queue of the FP32 force kernel for the current brick shape: every
     // world cut into bx x by x bz bricks (edge bricks cut at the box faces), uploaded, and
     // the kernel's shared-memory budget and persistent grid set up.
     int configure_bricks()
     {
         KArgs &a = args;
+        if (!tuning && !tuned) default_shape();
         // worlds with per-cell strengths run on the thread-per-bead kernel
         a.force_kernel = any_spatial() ? 1 : cfg_force_kernel;
         a.bricks = nullptr;
@@ -409,6 +433,7 @@ struct pdpd_engine {
         int best_i = -1;
         uint32_t used = 0;
         tune_log.clear();
+        tuning = true;
         for (int i = 0; i < n_cand; i++) {
             cfg_force_kernel = cand[i][0];
             cfg_brick[0] = cand[i][1];
@@ -442,8 +467,9 @@ struct pdpd_engine {
         cfg_brick[0] = pick[1];
         cfg_brick[1] = pick[2];
         cfg_brick[2] = pick[3];
-        configure_bricks();
         tuned = true;
+        tuning = false;
+        configure_bricks();
         return used;
     }
 
@@ -1225,6 +1251,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "force_kernel") {
         if (v > 8) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..8");
         e->cfg_force_kernel = (int)v;
+        e->kernel_user = true;
     } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {
         int idx = k == "brick_x" ? 0 : (k == "brick_y" ? 1 : 2);
         int nb[3] = {e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2]};
@@ -1232,6 +1259,7 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
         if (v < 1 || v > 32 || nb[0] * nb[1] > 64 || (nb[0] + 2) * (nb[1] + 2) * (nb[2] + 2) > 2048)
             return e->fail(PDPD_E_INVALID, "brick shape %dx%dx%d out of range", nb[0], nb[1], nb[2]);
         e->cfg_brick[idx] = (int)v;
+        e->brick_user = true;
     } else if (k == "autotune") {
         e->cfg_autotune = v ? 1 : 0;
         e->tuned = false;
