@@ -171,9 +171,10 @@ __device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, co
 constexpr int LIST_MAX = 32;
 
 // make_relative_cell_pos (naive_dpd_engine_half_step.hpp:181-196) for one direction:
-// neighbour cell and the periodic shift of its beads.
+// neighbour cell and the periodic shift of its beads (+L, -L or +0.0: the values the
+// reference's (is_right - is_left) * L takes, chosen without arithmetic).
 __device__ __forceinline__ uint32_t neighbour64(const WorldDev &w, const int c[3], const int dir[3],
-                                                double delta[3])
+                                                const double Ld[3], double delta[3])
 {
     int op[3];
 #pragma unroll
@@ -182,19 +183,22 @@ __device__ __forceinline__ uint32_t neighbour64(const WorldDev &w, const int c[3
         const int is_left = raw < 0;
         const int is_right = raw == w.L[i];
         op[i] = raw + (is_left - is_right) * w.L[i];
-        delta[i] = (double)(is_right - is_left) * (double)w.L[i];
+        delta[i] = is_right ? Ld[i] : (is_left ? -Ld[i] : 0.0);
     }
     return w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] +
            (uint32_t)op[2];
 }
 
-// Phase 2: calc_force (dpd_maths_core_half_step.hpp:69-157) with kappa = 0, r0 = 0.5 for the
-// listed neighbours, in list order, each term in the reference's operation order.
+// Phase 2: the reference's pair filter and calc_force (dpd_maths_core_half_step.hpp:69-157,
+// kappa = 0, r0 = 0.5) for the listed candidates, in list order, each operation in the
+// reference's order.  The list holds every neighbour that can be in range (the walk's
+// prefilter is conservative); the exact FP64 test here keeps dr2 < 1 and dr2 >= 1e-18
+// (naive_dpd_engine_half_step.hpp:404-411), so the terms added are the reference's.
 __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
                                               const Vec4d *__restrict__ vel,
                                               const uint32_t *__restrict__ s_j,
                                               const uint8_t *__restrict__ s_dir, int n,
-                                              const WorldDev &w, const int c[3],
+                                              const WorldDev &w, const int c[3], const double Ld[3],
                                               const double xh[3], const Vec4d &vh, uint32_t hh,
                                               uint32_t ti, const Vec2d *__restrict__ pair,
                                               const Vec2d *__restrict__ cp, uint32_t hc,
@@ -204,17 +208,19 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
 {
     const uint32_t nt = w.n_types;
     const uint32_t n2 = nt * nt;
+    const double min2 = (double)min_dist_sqr_f();
     for (int k = 0; k < n; k++) {
         const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
         const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
         const int dir[3] = {(int)(d & 3u) - 1, (int)((d >> 2) & 3u) - 1, (int)((d >> 4) & 3u) - 1};
         double delta[3];
-        neighbour64(w, c, dir, delta);
+        neighbour64(w, c, dir, Ld, delta);
         const Vec4d pj = pos[j];
-        const Vec4d vj = vel[j];
         const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
         const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
         const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+        if (dr2 >= 1 || dr2 < min2) continue;
+        const Vec4d vj = vel[j];
         const double dr = sqrt(dr2);
         const uint32_t hj = hash_of(pj);
         const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
@@ -245,56 +251,65 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
     }
 }
 
-__device__ __forceinline__ double slab_gap64(double o, int d)
+__device__ __forceinline__ float slab_gap32(float o, int d)
 {
-    return d == 0 ? 0.0 : (d < 0 ? o : 1.0 - o);
+    return d == 0 ? 0.0f : (d < 0 ? o : 1.0f - o);
 }
 
 // Pair forces on one bead: for each of the 27 directions in (-1..1)^3 order, for each bead
 // of that cell in id order, the reference's update_cell_forces filter
-// (naive_dpd_engine_half_step.hpp:358-424); in-range neighbours go to the list, which is
-// evaluated in the same order.  A cell is skipped when its nearest face is further than
-// 1 + 1e-9 from the bead: no bead in it can pass dr2 < 1, so the list is unchanged.
+// (naive_dpd_engine_half_step.hpp:358-424), then the forces in that order.
+//
+// The walk itself does no FP64 arithmetic (the GPU's FP64 pipe is the kernel's bound): it
+// tests the beads' FP32 cell offsets (posf, x - floor(x) rounded to FP32, error <= 2^-25)
+// against a squared distance of 1.0001, and list_forces64 applies the exact FP64 test.  The
+// FP32 separation of two offsets differs from the exact one by < 3e-7 per axis, so its
+// square differs by < 4e-6 for pairs in range: no neighbour with dr2 < 1 is dropped, and the
+// list's in-range entries, in order, are the reference's.  Rows and cells whose nearest face
+// is >= 1.0001 away (FP32 gaps of the same offsets) hold no neighbour in range.
 __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
                                               const Vec2d *s_pair, uint32_t *s_j, uint8_t *s_dir,
                                               int cap, uint32_t th_lo, uint32_t th_hi,
                                               double scale_inv_sqrt_dt, const int c[3],
-                                              const double xh[3], const Vec4d &vh, uint32_t hh,
-                                              double F[3])
+                                              const double xh[3], const float4 oh, const Vec4d &vh,
+                                              uint32_t hh, double F[3])
 {
     const Vec4d *__restrict__ pos = (const Vec4d *)a.posA;
     const Vec4d *__restrict__ vel = (const Vec4d *)a.velA;
+    const float4 *__restrict__ posf = a.posf;
     const uint32_t *__restrict__ start = a.start;
     const uint32_t ti = min(hh >> 28, w.n_types - 1u);
-    const double min2 = (double)min_dist_sqr_f();
-    const double PRUNE = 1.0 + 1e-9;
-    const double o[3] = {xh[0] - (double)c[0], xh[1] - (double)c[1], xh[2] - (double)c[2]};
+    const float PRUNE = 1.0001f;
+    const double Ld[3] = {(double)w.L[0], (double)w.L[1], (double)w.L[2]};
     const Vec2d *cp = w.spatial ? (const Vec2d *)a.cellpair + w.cellpair_base : nullptr;
     const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
     F[0] = F[1] = F[2] = 0.0;
     int n = 0;
     int dir[3];
     for (dir[0] = -1; dir[0] <= 1; dir[0]++) {
-        const double gx = slab_gap64(o[0], dir[0]);
+        const float gx = slab_gap32(oh.x, dir[0]);
+        const float ax = oh.x - (float)dir[0];
         for (dir[1] = -1; dir[1] <= 1; dir[1]++) {
-            const double gy = slab_gap64(o[1], dir[1]);
-            const double gxy = gx * gx + gy * gy;
+            const float gy = slab_gap32(oh.y, dir[1]);
+            const float gxy = gx * gx + gy * gy;
             if (gxy >= PRUNE) continue;
+            const float ay = oh.y - (float)dir[1];
             for (dir[2] = -1; dir[2] <= 1; dir[2]++) {
-                const double gz = slab_gap64(o[2], dir[2]);
+                const float gz = slab_gap32(oh.z, dir[2]);
                 if (gxy + gz * gz >= PRUNE) continue;
-                double delta[3];
-                const uint32_t nc = neighbour64(w, c, dir, delta);
+                const float az = oh.z - (float)dir[2];
+                int op[3];
+#pragma unroll
+                for (int i = 0; i < 3; i++) op[i] = wrap_index(c[i] + dir[i], w.L[i]);
+                const uint32_t nc = w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] + (uint32_t)op[2];
                 const uint32_t j1 = start[nc + 1];
                 const uint8_t dpk = (uint8_t)((dir[0] + 1) | ((dir[1] + 1) << 2) | ((dir[2] + 1) << 4));
                 for (uint32_t j = start[nc]; j < j1; j++) {
-                    const Vec4d pj = pos[j];
-                    const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
-                    const double dx0 = xh[0] - obx, dx1 = xh[1] - oby, dx2 = xh[2] - obz;
-                    const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
-                    if (dr2 >= 1 || dr2 < min2) continue;
+                    const float4 q = posf[j];
+                    const float ex = ax - q.x, ey = ay - q.y, ez = az - q.z;
+                    if (ex * ex + ey * ey + ez * ez >= PRUNE) continue;
                     if (n == cap) {
-                        list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, cp, hc,
+                        list_forces64(pos, vel, s_j, s_dir, n, w, c, Ld, xh, vh, hh, ti, s_pair, cp, hc,
                                       a.cellg, th_lo, th_hi, scale_inv_sqrt_dt, F);
                         n = 0;
                     }
@@ -305,7 +320,7 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
             }
         }
     }
-    list_forces64(pos, vel, s_j, s_dir, n, w, c, xh, vh, hh, ti, s_pair, cp, hc, a.cellg, th_lo,
+    list_forces64(pos, vel, s_j, s_dir, n, w, c, Ld, xh, vh, hh, ti, s_pair, cp, hc, a.cellg, th_lo,
                   th_hi, scale_inv_sqrt_dt, F);
 }
 
@@ -336,7 +351,8 @@ __global__ void __launch_bounds__(TILE_BEADS) k_force64(KArgs a)
         decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
         double x[3] = {ph.x, ph.y, ph.z};
         double F[3];
-        pair_forces64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, vh, hh, F);
+        pair_forces64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, a.posf[s], vh,
+                      hh, F);
         if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
         // update_mom: v += f * half(dt); a stationary type's v and f are cleared instead
         // (naive_dpd_engine_half_merge.hpp:387-394), so the next update_pos leaves it in place

@@ -105,6 +105,8 @@ struct KArgs {
     const uint32_t *bonded_ids;  // ids of the beads that have bond terms (FP32 bond kernel)
     uint32_t n_bonded;
     float4 *fbond;               // FP32: bond force of each bonded bead, by sorted slot
+    float4 *posf;                // FP64: (x - floor(x), hash) in FP32, by sorted slot: the
+                                 // neighbour walk's distance prefilter
     // id-ordered staging for upload / download: 9 doubles per bead (x, v, f)
     double *staging;
     int block_threads;

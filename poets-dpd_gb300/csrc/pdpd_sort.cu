@@ -130,6 +130,18 @@ __device__ __forceinline__ uint32_t payload_hash(const Vec4d &p)
     return (uint32_t)__double_as_longlong(p.w);
 }
 
+// FP64 positions as FP32 offsets inside their cell (x - floor(x) is exact in FP64, the cell
+// being floor(x)), for the force kernel's distance prefilter; the hash rides along.
+__device__ __forceinline__ float4 offset_shadow(const float4 &p)
+{
+    return p;
+}
+__device__ __forceinline__ float4 offset_shadow(const Vec4d &p)
+{
+    return make_float4((float)(p.x - floor(p.x)), (float)(p.y - floor(p.y)), (float)(p.z - floor(p.z)),
+                       __uint_as_float(payload_hash(p)));
+}
+
 // slot_of_id is kept for polymer beads only (monomer bit of the hash clear): the bond kernels
 // look up bond partners through it; the codec walks slots and reads ids instead.
 template <class P>
@@ -138,7 +150,7 @@ __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_
                         const P *__restrict__ frc_in, P *__restrict__ pos_out,
                         P *__restrict__ vel_out, P *__restrict__ frc_out,
                         uint32_t *__restrict__ ids_out, uint32_t *__restrict__ cellg_out,
-                        uint32_t *__restrict__ slot_of_id)
+                        uint32_t *__restrict__ slot_of_id, float4 *__restrict__ shadow_out)
 {
     uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
@@ -154,6 +166,7 @@ __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_
     ids_out[dst] = e.y;
     cellg_out[dst] = e.z;
     if (!(payload_hash(p) & (1u << 27))) slot_of_id[e.y] = dst;
+    if (shadow_out) shadow_out[dst] = offset_shadow(p);
 }
 
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s)
@@ -171,13 +184,13 @@ int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t
                                        (const Vec4d *)a.velB,
                                        with_force ? (const Vec4d *)a.frcB : nullptr,
                                        (Vec4d *)a.posA, (Vec4d *)a.velA, (Vec4d *)a.frc, a.ids,
-                                       a.cellg, a.slot_of_id);
+                                       a.cellg, a.slot_of_id, a.posf);
     } else {
         k_canon<float4><<<g, T, 0, s>>>(a.n_beads, a.tmp, a.start, (const float4 *)a.posB,
                                         (const float4 *)a.velB,
                                         with_force ? (const float4 *)a.frcB : nullptr,
                                         (float4 *)a.posA, (float4 *)a.velA, (float4 *)a.frc,
-                                        a.ids, a.cellg, a.slot_of_id);
+                                        a.ids, a.cellg, a.slot_of_id, nullptr);
     }
     return 4;
 }
