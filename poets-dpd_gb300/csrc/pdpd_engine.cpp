@@ -196,7 +196,7 @@ struct pdpd_engine {
     DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
-    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
@@ -250,7 +250,7 @@ struct pdpd_engine {
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
-                          &d_v2err, &d_cellpair, &d_posf};
+                          &d_v2err, &d_cellpair, &d_posf, &d_bterm};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -866,7 +866,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
     A(e->d_cellpair, std::max<size_t>(16, f64 ? sizeof(double) * cp64.size() : sizeof(float) * cp32.size()));
     A(e->d_hash, sizeof(uint32_t) * nb);
-    // Polymer beads (monomer bit of the hash clear), for the FP32 bond kernel.
+    // Polymer beads (monomer bit of the hash clear), for the bond kernels.
     std::vector<uint32_t> bonded;
     for (uint32_t i = 0; i < n_worlds; i++) {
         const uint32_t n = ws[i].n_beads, bb = wdev[i].bead_base;
@@ -883,6 +883,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_bonded, sizeof(uint32_t) * std::max<size_t>(1, bonded.size()));
     A(e->d_fbond, f64 ? 16 : sizeof(float4) * std::max<uint64_t>(1, nb));
     A(e->d_posf, f64 ? sizeof(float4) * std::max<uint64_t>(1, nb) : 16);
+    A(e->d_bterm, f64 ? sizeof(double) * 4 * std::max<uint64_t>(1, n_terms) : 16);
     A(e->d_staging[0], sizeof(double) * 9 * nb);
     if (ce != cudaSuccess) {
         cudaGetLastError();
@@ -997,9 +998,10 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     a.pair = e->d_pair.p;
     a.cellpair = e->d_cellpair.p;
     a.bonded_ids = e->d_bonded.as<uint32_t>();
-    a.n_bonded = f64 ? 0u : (uint32_t)bonded.size();
+    a.n_bonded = (uint32_t)bonded.size();
     a.fbond = e->d_fbond.as<float4>();
     a.posf = f64 ? e->d_posf.as<float4>() : nullptr;
+    a.bterm = f64 ? e->d_bterm.p : nullptr;
     a.staging = e->d_staging[0].as<double>();
     a.block_threads = 128;
     int gb = e->cfg_grid_blocks > 0 ? e->cfg_grid_blocks : 16 * e->sm_count;

@@ -99,13 +99,16 @@ __device__ __forceinline__ void load_x(const Vec4d *__restrict__ pos, uint32_t s
     x[2] = p.z;
 }
 
-// Bond forces on one bead, in the order of its CSR row (Hookean bonds, then angle bonds),
-// each term evaluated exactly as update_hookean_bond / update_angle_bond
+// Bond terms of one bead, one per row of its CSR (Hookean bonds, then angle bonds), each
+// evaluated exactly as update_hookean_bond / update_angle_bond
 // (naive_dpd_engine_half_step.hpp:426-483) and calc_angle_force
-// (dpd_maths_core_half_step.hpp:177-229).
-__device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, const double xs[3],
-                              double F[3], uint32_t &err)
+// (dpd_maths_core_half_step.hpp:177-229), and stored with the sign it is added with: the
+// force kernel adds the rows in order after the pair forces (F - t == F + (-t) in IEEE
+// arithmetic), which is the reference's order of additions to the bead's force.
+__device__ void bond_terms64(const KArgs &a, const WorldDev &w, uint32_t id, const double xs[3],
+                             uint32_t &err)
 {
+    Vec4d *out = (Vec4d *)a.bterm;
     const Vec4d *pos = (const Vec4d *)a.posA;
     const Vec4d *prm_tab = (const Vec4d *)a.bond_params;
     const uint32_t r0 = a.bond_row[id], r1 = a.bond_row[id + 1];
@@ -125,11 +128,13 @@ __device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, co
             const double dr0 = prm.y - dr;
             const double hookean_force = prm.x * dr0;
             const double s = hookean_force / dr;
+            double t[3];
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 const double fd = dx[d] * s;
-                F[d] = role == 0 ? F[d] - fd : F[d] + fd;
+                t[d] = role == 0 ? -fd : fd;
             }
+            out[r] = Vec4d{t[0], t[1], t[2], 0.0};
         } else {
             load_x(pos, a.slot_of_id[bt.b], xb);
             const double *xh = role == 0 ? xs : xa;
@@ -162,8 +167,10 @@ __device__ void bond_forces64(const KArgs &a, const WorldDev &w, uint32_t id, co
                     mf[d] = -(hf[d] + tf[d]);
                 }
             }
+            double t[3];
 #pragma unroll
-            for (int d = 0; d < 3; d++) F[d] = F[d] + (role == 0 ? hf[d] : (role == 1 ? mf[d] : tf[d]));
+            for (int d = 0; d < 3; d++) t[d] = role == 0 ? hf[d] : (role == 1 ? mf[d] : tf[d]);
+            out[r] = Vec4d{t[0], t[1], t[2], 0.0};
         }
     }
 }
@@ -197,7 +204,7 @@ __device__ __forceinline__ uint32_t neighbour64(const WorldDev &w, const int c[3
 __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
                                               const Vec4d *__restrict__ vel,
                                               const uint32_t *__restrict__ s_j,
-                                              const uint8_t *__restrict__ s_dir, int n,
+                                              const uint8_t *__restrict__ s_dir, int col, int n,
                                               const WorldDev &w, const int c[3], const double Ld[3],
                                               const double xh[3], const Vec4d &vh, uint32_t hh,
                                               uint32_t ti, const Vec2d *__restrict__ pair,
@@ -210,8 +217,8 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
     const uint32_t n2 = nt * nt;
     const double min2 = (double)min_dist_sqr_f();
     for (int k = 0; k < n; k++) {
-        const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
-        const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
+        const uint32_t j = s_j[k * TILE_BEADS + col];
+        const uint32_t d = s_dir[k * TILE_BEADS + col];
         const int dir[3] = {(int)(d & 3u) - 1, (int)((d >> 2) & 3u) - 1, (int)((d >> 4) & 3u) - 1};
         double delta[3];
         neighbour64(w, c, dir, Ld, delta);
@@ -251,14 +258,49 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
     }
 }
 
+// The home bead's data the list evaluation needs.
+struct Home64 {
+    double x[3];
+    Vec4d v;
+    uint32_t hash, ti, hc;
+    int c[3];
+};
+
+__device__ __forceinline__ Home64 home64(const KArgs &a, const WorldDev &w, uint32_t s)
+{
+    Home64 h;
+    const Vec4d p = ((const Vec4d *)a.posA)[s];
+    h.x[0] = p.x;
+    h.x[1] = p.y;
+    h.x[2] = p.z;
+    h.v = ((const Vec4d *)a.velA)[s];
+    h.hash = hash_of(p);
+    h.ti = min(h.hash >> 28, w.n_types - 1u);
+    h.hc = a.cellg[s] - w.cell_base;
+    decode_cell(h.hc, w.L, h.c[0], h.c[1], h.c[2]);
+    return h;
+}
+
+__device__ __forceinline__ void eval_list64(const KArgs &a, const WorldDev &w, const Vec2d *s_pair,
+                                            const uint32_t *s_j, const uint8_t *s_dir, int col, int n,
+                                            const Home64 &h, uint32_t th_lo, uint32_t th_hi, double F[3])
+{
+    const double Ld[3] = {(double)w.L[0], (double)w.L[1], (double)w.L[2]};
+    const Vec2d *cp = w.spatial ? (const Vec2d *)a.cellpair + w.cellpair_base : nullptr;
+    list_forces64((const Vec4d *)a.posA, (const Vec4d *)a.velA, s_j, s_dir, col, n, w, h.c, Ld, h.x, h.v,
+                  h.hash, h.ti, s_pair, cp, h.hc, a.cellg, th_lo, th_hi, w.scale_inv_sqrt_dt, F);
+}
+
 __device__ __forceinline__ float slab_gap32(float o, int d)
 {
     return d == 0 ? 0.0f : (d < 0 ? o : 1.0f - o);
 }
 
-// Pair forces on one bead: for each of the 27 directions in (-1..1)^3 order, for each bead
-// of that cell in id order, the reference's update_cell_forces filter
-// (naive_dpd_engine_half_step.hpp:358-424), then the forces in that order.
+// The neighbour walk of one bead: for each of the 27 directions in (-1..1)^3 order, for each
+// bead of that cell in id order (the reference's update_cell_forces order,
+// naive_dpd_engine_half_step.hpp:358-424), candidates are appended to the bead's list
+// (column threadIdx.x); a full list is evaluated into F on the spot.  Returns the entries
+// left in the list.
 //
 // The walk itself does no FP64 arithmetic (the GPU's FP64 pipe is the kernel's bound): it
 // tests the beads' FP32 cell offsets (posf, x - floor(x) rounded to FP32, error <= 2^-25)
@@ -267,23 +309,13 @@ __device__ __forceinline__ float slab_gap32(float o, int d)
 // square differs by < 4e-6 for pairs in range: no neighbour with dr2 < 1 is dropped, and the
 // list's in-range entries, in order, are the reference's.  Rows and cells whose nearest face
 // is >= 1.0001 away (FP32 gaps of the same offsets) hold no neighbour in range.
-__device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
-                                              const Vec2d *s_pair, uint32_t *s_j, uint8_t *s_dir,
-                                              int cap, uint32_t th_lo, uint32_t th_hi,
-                                              double scale_inv_sqrt_dt, const int c[3],
-                                              const double xh[3], const float4 oh, const Vec4d &vh,
-                                              uint32_t hh, double F[3])
+__device__ __forceinline__ int walk64(const KArgs &a, const WorldDev &w, const Vec2d *s_pair,
+                                      uint32_t *s_j, uint8_t *s_dir, int cap, uint32_t th_lo,
+                                      uint32_t th_hi, const Home64 &h, const float4 oh, double F[3])
 {
-    const Vec4d *__restrict__ pos = (const Vec4d *)a.posA;
-    const Vec4d *__restrict__ vel = (const Vec4d *)a.velA;
     const float4 *__restrict__ posf = a.posf;
     const uint32_t *__restrict__ start = a.start;
-    const uint32_t ti = min(hh >> 28, w.n_types - 1u);
     const float PRUNE = 1.0001f;
-    const double Ld[3] = {(double)w.L[0], (double)w.L[1], (double)w.L[2]};
-    const Vec2d *cp = w.spatial ? (const Vec2d *)a.cellpair + w.cellpair_base : nullptr;
-    const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
-    F[0] = F[1] = F[2] = 0.0;
     int n = 0;
     int dir[3];
     for (dir[0] = -1; dir[0] <= 1; dir[0]++) {
@@ -300,7 +332,7 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
                 const float az = oh.z - (float)dir[2];
                 int op[3];
 #pragma unroll
-                for (int i = 0; i < 3; i++) op[i] = wrap_index(c[i] + dir[i], w.L[i]);
+                for (int i = 0; i < 3; i++) op[i] = wrap_index(h.c[i] + dir[i], w.L[i]);
                 const uint32_t nc = w.cell_base + ((uint32_t)op[0] * (uint32_t)w.L[1] + (uint32_t)op[1]) * (uint32_t)w.L[2] + (uint32_t)op[2];
                 const uint32_t j1 = start[nc + 1];
                 const uint8_t dpk = (uint8_t)((dir[0] + 1) | ((dir[1] + 1) << 2) | ((dir[2] + 1) << 4));
@@ -309,8 +341,7 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
                     const float ex = ax - q.x, ey = ay - q.y, ez = az - q.z;
                     if (ex * ex + ey * ey + ez * ez >= PRUNE) continue;
                     if (n == cap) {
-                        list_forces64(pos, vel, s_j, s_dir, n, w, c, Ld, xh, vh, hh, ti, s_pair, cp, hc,
-                                      a.cellg, th_lo, th_hi, scale_inv_sqrt_dt, F);
+                        eval_list64(a, w, s_pair, s_j, s_dir, threadIdx.x, n, h, th_lo, th_hi, F);
                         n = 0;
                     }
                     s_j[n * TILE_BEADS + threadIdx.x] = j;
@@ -320,10 +351,46 @@ __device__ __forceinline__ void pair_forces64(const KArgs &a, const WorldDev &w,
             }
         }
     }
-    list_forces64(pos, vel, s_j, s_dir, n, w, c, Ld, xh, vh, hh, ti, s_pair, cp, hc, a.cellg, th_lo,
-                  th_hi, scale_inv_sqrt_dt, F);
+    return n;
 }
 
+// Lists of a tile, re-dealt to threads by length (see k_force64).
+struct Balance64 {
+    uint32_t hist[LIST_MAX + 2];
+    uint8_t n[TILE_BEADS];
+    uint8_t perm[TILE_BEADS];
+    double f[3][TILE_BEADS];
+};
+
+// Bond terms of every polymer bead, one thread per bead (a compact list of the few bonded
+// beads), stored by CSR row for the force kernel: the lanes of a warp all do bond work,
+// instead of one or two lanes of a pair-force warp.
+__global__ void __launch_bounds__(128) k_bonds64(KArgs a)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n_bonded) return;
+    const uint32_t id = a.bonded_ids[k];
+    uint32_t lo = 0, hi = a.n_worlds;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (a.worlds[mid].bead_base <= id) lo = mid; else hi = mid;
+    }
+    const WorldDev &w = a.worlds[lo];
+    const Vec4d p = ((const Vec4d *)a.posA)[a.slot_of_id[id]];
+    const double x[3] = {p.x, p.y, p.z};
+    uint32_t err = 0;
+    bond_terms64(a, w, id, x, err);
+    if (err) atomicOr(&a.worlds[lo].err, err);
+}
+
+// Force pass of a tile of TILE_BEADS sorted beads, one thread per bead:
+//   1. each thread walks its bead's neighbours into its list;
+//   2. the lists are counting-sorted by length and thread t evaluates list perm[t], so the
+//      lanes of a warp evaluate lists of about the same length (the FP64 pipe executes an
+//      instruction for the whole warp whatever its active lanes); every list is still
+//      summed by one thread in its own order, so the result is the same;
+//   3. each thread adds its bead's bond terms (k_bonds64) in CSR order, then update_mom and
+//      either the final write or the next update_pos with its cell count.
 template <int FINAL>
 __global__ void __launch_bounds__(TILE_BEADS) k_force64(KArgs a)
 {
@@ -331,52 +398,105 @@ __global__ void __launch_bounds__(TILE_BEADS) k_force64(KArgs a)
     __shared__ uint32_t s_j[LIST_MAX * TILE_BEADS];
     __shared__ uint8_t s_dir[LIST_MAX * TILE_BEADS];
     __shared__ WorldCache wc;
-    if (threadIdx.x == 0) wc.world = 0xffffffffu;
+    __shared__ Balance64 B;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) wc.world = 0xffffffffu;
     __syncthreads();
     const int cap = (a.list_capacity > 0 && a.list_capacity < LIST_MAX) ? a.list_capacity : LIST_MAX;
     for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const Tile tl = a.tiles[tile];
         load_world(a, tl.world, wc, s_pair);
         const WorldDev &w = wc.w;
-        const uint32_t s = tl.slot_begin + threadIdx.x;
-        if (s >= tl.slot_end) continue;
-        const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+        const uint32_t s = tl.slot_begin + tid;
+        const bool act = s < tl.slot_end;
         const uint64_t th = t_hash((uint32_t)w.t, w.seed);
         const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
-        uint32_t err = 0;
-        const Vec4d ph = ((const Vec4d *)a.posA)[s];
-        const Vec4d vh = ((const Vec4d *)a.velA)[s];
-        const uint32_t hh = hash_of(ph);
-        int c[3];
-        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-        double x[3] = {ph.x, ph.y, ph.z};
-        double F[3];
-        pair_forces64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, w.scale_inv_sqrt_dt, c, x, a.posf[s], vh,
-                      hh, F);
-        if (!(hh & (1u << 27))) bond_forces64(a, w, a.ids[s], x, F, err);
-        // update_mom: v += f * half(dt); a stationary type's v and f are cleared instead
-        // (naive_dpd_engine_half_merge.hpp:387-394), so the next update_pos leaves it in place
-        double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
-        if ((w.stationary >> (hh >> 28)) & 1u) {
-            v[0] = v[1] = v[2] = 0.0;
-            F[0] = F[1] = F[2] = 0.0;
+        double F[3] = {0.0, 0.0, 0.0};
+        int n = 0;
+        if (act) {
+            const Home64 h = home64(a, w, s);
+            n = walk64(a, w, s_pair, s_j, s_dir, cap, th_lo, th_hi, h, a.posf[s], F);
         }
-        if (FINAL) {
-            Vec4d vo = {v[0], v[1], v[2], 0.0};
-            Vec4d fo = {F[0], F[1], F[2], 0.0};
-            ((Vec4d *)a.velB)[s] = vo;
-            ((Vec4d *)a.frc)[s] = fo;
-            if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
-        } else {
-            const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
-            const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
-            Vec4d po = {x[0], x[1], x[2], ph.w};
-            Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
-            ((Vec4d *)a.posB)[s] = po;
-            ((Vec4d *)a.velB)[s] = vo;
-            a.keyrank[s] = make_uint2(key, rank);
+        if (tid < LIST_MAX + 2) B.hist[tid] = 0u;
+        B.n[tid] = (uint8_t)n;
+        B.f[0][tid] = F[0];
+        B.f[1][tid] = F[1];
+        B.f[2][tid] = F[2];
+        __syncthreads();
+        const uint32_t rank = atomicAdd(&B.hist[n], 1u);  // n <= LIST_MAX
+        __syncthreads();
+        if (warp == 0) {  // exclusive prefix of the LIST_MAX + 1 bins
+            const uint32_t v = B.hist[lane];
+            uint32_t inc = v;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+                if (lane >= off) inc += y;
+            }
+            B.hist[lane] = inc - v;
+            if (lane == 31) B.hist[32] = inc;
         }
-        if (err) atomicOr(&a.worlds[tl.world].err, err);
+        __syncthreads();
+        B.perm[B.hist[n] + rank] = (uint8_t)tid;
+        __syncthreads();
+        {
+            const int o = B.perm[tid];
+            const int no = B.n[o];
+            if (no > 0) {
+                const Home64 h = home64(a, w, tl.slot_begin + (uint32_t)o);
+                double G[3] = {B.f[0][o], B.f[1][o], B.f[2][o]};
+                eval_list64(a, w, s_pair, s_j, s_dir, o, no, h, th_lo, th_hi, G);
+                B.f[0][o] = G[0];
+                B.f[1][o] = G[1];
+                B.f[2][o] = G[2];
+            }
+        }
+        __syncthreads();
+        if (act) {
+            F[0] = B.f[0][tid];
+            F[1] = B.f[1][tid];
+            F[2] = B.f[2][tid];
+            const double dt = w.dt, hdt = dt * 0.5, hdt2 = (dt * dt) * 0.5;
+            uint32_t err = 0;
+            const Vec4d ph = ((const Vec4d *)a.posA)[s];
+            const Vec4d vh = ((const Vec4d *)a.velA)[s];
+            const uint32_t hh = hash_of(ph);
+            double x[3] = {ph.x, ph.y, ph.z};
+            if (!(hh & (1u << 27))) {  // polymer bead: its bond terms, in CSR order
+                const uint32_t id = a.ids[s];
+                const Vec4d *bt = (const Vec4d *)a.bterm;
+                for (uint32_t r = a.bond_row[id]; r < a.bond_row[id + 1]; r++) {
+                    const Vec4d t = bt[r];
+                    F[0] = F[0] + t.x;
+                    F[1] = F[1] + t.y;
+                    F[2] = F[2] + t.z;
+                }
+            }
+            // update_mom: v += f * half(dt); a stationary type's v and f are cleared instead
+            // (naive_dpd_engine_half_merge.hpp:387-394), so the next update_pos leaves it in place
+            double v[3] = {vh.x + F[0] * hdt, vh.y + F[1] * hdt, vh.z + F[2] * hdt};
+            if ((w.stationary >> (hh >> 28)) & 1u) {
+                v[0] = v[1] = v[2] = 0.0;
+                F[0] = F[1] = F[2] = 0.0;
+            }
+            if (FINAL) {
+                Vec4d vo = {v[0], v[1], v[2], 0.0};
+                Vec4d fo = {F[0], F[1], F[2], 0.0};
+                ((Vec4d *)a.velB)[s] = vo;
+                ((Vec4d *)a.frc)[s] = fo;
+                if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) err |= ERR_NONFINITE;
+            } else {
+                const uint32_t key = advance_position64(w, dt, hdt2, x, v, F, err);
+                const uint32_t rank2 = atomicAdd(&a.cnt[key], 1u);
+                Vec4d po = {x[0], x[1], x[2], ph.w};
+                Vec4d vo = {v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.0};
+                ((Vec4d *)a.posB)[s] = po;
+                ((Vec4d *)a.velB)[s] = vo;
+                a.keyrank[s] = make_uint2(key, rank2);
+            }
+            if (err) atomicOr(&a.worlds[tl.world].err, err);
+        }
+        __syncthreads();  // the lists and B are reused by the next tile
     }
 }
 
@@ -490,11 +610,16 @@ int launch_begin64(const KArgs &a, cudaStream_t s)
 
 int launch_force64(const KArgs &a, int final_step, cudaStream_t s)
 {
+    int n = 0;
+    if (a.n_bonded > 0) {
+        k_bonds64<<<(a.n_bonded + 127) / 128, 128, 0, s>>>(a);
+        n++;
+    }
     if (final_step)
         k_force64<1><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     else
         k_force64<0><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
-    return 1;
+    return n + 1;
 }
 
 int launch_finish64(const KArgs &a, cudaStream_t s)

@@ -102,11 +102,12 @@ struct KArgs {
     const void *bond_params;   // float4 / Vec4d: (kappa, r0 | cos theta0, sin theta0, 0)
     const void *pair;          // float2 / Vec2d: (a_ij, sqrt(gamma_ij))
     const void *cellpair;      // float2 / Vec2d per (cell, type pair) of spatial worlds
-    const uint32_t *bonded_ids;  // ids of the beads that have bond terms (FP32 bond kernel)
+    const uint32_t *bonded_ids;  // ids of the beads that have bond terms (bond kernels)
     uint32_t n_bonded;
     float4 *fbond;               // FP32: bond force of each bonded bead, by sorted slot
     float4 *posf;                // FP64: (x - floor(x), hash) in FP32, by sorted slot: the
                                  // neighbour walk's distance prefilter
+    void *bterm;                 // FP64: each bond term's force (Vec4d), by CSR row
     // id-ordered staging for upload / download: 9 doubles per bead (x, v, f)
     double *staging;
     int block_threads;
