@@ -70,6 +70,13 @@ __device__ __forceinline__ uint32_t advance_position(const WorldDev &w, float dt
            (uint32_t)nc[2];
 }
 
+// Arrival rank in the new cell with the z-half mark the sort orders by (bit 31: offset
+// z >= 0.5, compared exactly in FP32).
+__device__ __forceinline__ uint32_t zhalf_rank(uint32_t rank, float oz)
+{
+    return rank | (oz >= 0.5f ? 0x80000000u : 0u);
+}
+
 // Position of bead `slot` relative to a bead at (cell c, offset o), using the
 // minimum-image integer cell difference.
 __device__ __forceinline__ void rel_pos(const WorldDev &w, const float4 *__restrict__ pos,
@@ -264,7 +271,7 @@ __device__ __forceinline__ void integrate32(const KArgs &a, const WorldDev &w, u
         ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
         ((float4 *)a.velB)[s] = make_float4(__fmaf_rn(F[0], hdt, v[0]), __fmaf_rn(F[1], hdt, v[1]),
                                             __fmaf_rn(F[2], hdt, v[2]), 0.f);
-        a.keyrank[s] = make_uint2(key, rank);
+        a.keyrank[s] = make_uint2(key, zhalf_rank(rank, o[2]));
     }
 }
 
@@ -487,7 +494,7 @@ __global__ void __launch_bounds__(TILE_BEADS) k_begin32(KArgs a)
         ((float4 *)a.posB)[s] = make_float4(o[0], o[1], o[2], ph.w);
         ((float4 *)a.velB)[s] = st ? make_float4(vh.x, vh.y, vh.z, 0.f)
                                    : make_float4(v[0] + F[0] * hdt, v[1] + F[1] * hdt, v[2] + F[2] * hdt, 0.f);
-        a.keyrank[s] = make_uint2(key, rank);
+        a.keyrank[s] = make_uint2(key, zhalf_rank(rank, o[2]));
         if (err) atomicOr(&a.worlds[tl.world].err, err);
     }
 }
@@ -528,7 +535,7 @@ __global__ void k_bin32(KArgs a, const uint32_t *__restrict__ hash_in)
     ((float4 *)a.velB)[g] = make_float4((float)st[3], (float)st[4], (float)st[5], 0.f);
     ((float4 *)a.frcB)[g] = make_float4((float)st[6], (float)st[7], (float)st[8], 0.f);
     a.ids[g] = g;
-    a.keyrank[g] = make_uint2(key, rank);
+    a.keyrank[g] = make_uint2(key, zhalf_rank(rank, o[2]));
 }
 
 __global__ void k_finish32(KArgs a)

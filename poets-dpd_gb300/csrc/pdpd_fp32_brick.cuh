@@ -35,7 +35,7 @@ struct BrickHeader {
 // list[BLIST_MAX][threads].
 struct BrickLayout {
     uint32_t hc_max, maxb;
-    uint32_t off_pair, off_hstart, off_hslot, off_pos, off_vel, off_list, off_bal, bytes;
+    uint32_t off_pair, off_hstart, off_hslot, off_hlo, off_pos, off_vel, off_list, off_bal, bytes;
 };
 
 // Balanced list evaluation (variant 7): per pass of BRICK_THREADS home beads, the list
@@ -64,6 +64,8 @@ __host__ __device__ inline BrickLayout brick_layout(uint32_t hc_max, uint32_t ma
     off += 4 * (hc_max + 1);
     L.off_hslot = off;
     off += 4 * hc_max;
+    L.off_hlo = off;
+    off += 2 * hc_max;
     off = (off + 15) & ~15u;
     L.off_pos = off;
     off += 16 * maxb;
@@ -210,8 +212,8 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
 template <int T = BRICK_THREADS>
 __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const WorldDev &w, const Brick &br,
                                                      BrickHeader &H, uint32_t *hstart, uint32_t *hslot,
-                                                     float4 *spos, float4 *svel, uint32_t maxb,
-                                                     uint32_t &total, uint32_t &n_home)
+                                                     uint16_t *hlo, float4 *spos, float4 *svel,
+                                                     uint32_t maxb, uint32_t &total, uint32_t &n_home)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int HX = br.bx + 2, HY = br.by + 2, HZ = br.bz + 2;
@@ -239,6 +241,7 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
             const uint32_t n = a.start[c + 1] - s0;
             hslot[hc] = s0;
             hstart[hc] = n;  // count for now
+            hlo[hc] = n ? (uint16_t)min((uint32_t)a.zlo[c], n) : (uint16_t)0;
             tsum += n;
             if (++hz == HZ) {
                 hz = 0;
@@ -318,7 +321,8 @@ template <int T = BRICK_THREADS>
 __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spos,
                                                   const float4 *__restrict__ svel,
                                                   uint16_t *__restrict__ list, int cap,
-                                                  const uint32_t *__restrict__ hstart, int HY, int HZ,
+                                                  const uint32_t *__restrict__ hstart,
+                                                  const uint16_t *__restrict__ hlo, int HY, int HZ,
                                                   int hx, int hy, int hz, const float4 pi,
                                                   const float4 vi, const float2 *pair, uint32_t nt,
                                                   uint32_t th_lo, uint32_t th_hi, float scale,
@@ -328,6 +332,9 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
     const float min2 = min_dist_sqr_f();
     const float azm = __fsub_rn(pi.z, -1.0f), azp = __fsub_rn(pi.z, 1.0f);
     const float gzm = pi.z, gzp = 1.0f - pi.z;
+    // gaps to the far halves of the end cells: the lower half of the cell below (z offsets
+    // < 0.5) and the upper half of the cell above (>= 0.5)
+    const float gzm2 = pi.z + 0.5f, gzp2 = 1.5f - pi.z;
     int n = 0;
 #pragma unroll 1
     for (int rr = 0; rr < 9; rr++) {
@@ -337,8 +344,9 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
         if (gxy >= PRUNE) continue;
         const int rowc = ((hx + ddx) * HY + (hy + ddy)) * HZ + hz;
         const uint32_t c1 = hstart[rowc], c2 = hstart[rowc + 1];
-        const uint32_t j0 = gxy + gzm * gzm >= PRUNE ? c1 : hstart[rowc - 1];
-        const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : hstart[rowc + 2];
+        const uint32_t c0 = hstart[rowc - 1], c3 = hstart[rowc + 2];
+        const uint32_t j0 = gxy + gzm * gzm >= PRUNE ? c1 : (gxy + gzm2 * gzm2 >= PRUNE ? c0 + hlo[rowc - 1] : c0);
+        const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : (gxy + gzp2 * gzp2 >= PRUNE ? c2 + hlo[rowc + 1] : c3);
         const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
         const uint32_t dbase = (uint32_t)(rr * 3) << 11;
         if (n + (int)(j1 - j0) > cap) {  // room for the whole row, or evaluate the list first
@@ -401,6 +409,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
     float2 *spair = reinterpret_cast<float2 *>(smem_raw + lay.off_pair);
     uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
     uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
+    uint16_t *hlo = reinterpret_cast<uint16_t *>(smem_raw + lay.off_hlo);
     float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
     float4 *svel = reinterpret_cast<float4 *>(smem_raw + lay.off_vel);
     uint16_t *list = reinterpret_cast<uint16_t *>(smem_raw + lay.off_list);
@@ -423,7 +432,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
 
         // ---- 1-2. halo cells (hstart, hslot, home rows) and staging
         uint32_t total = 0, n_home = 0;
-        brick_halo_and_stage<T>(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
+        brick_halo_and_stage<T>(a, w, br, H, hstart, hslot, hlo, spos, svel, lay.maxb, total, n_home);
         const bool staged = total <= lay.maxb;
 
         // ---- 3. one thread per home bead: pair forces, bonds, integration
@@ -454,7 +463,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
                     while (hstart[hc0 + z + 1] <= si) z++;
                     pi = spos[si];
                     vi = svel[si];
-                    n = brick_rows_collect<T>(spos, svel, list, cap, hstart, HY, HZ, lx + 1, ly + 1, z + 1,
+                    n = brick_rows_collect<T>(spos, svel, list, cap, hstart, hlo, HY, HZ, lx + 1, ly + 1, z + 1,
                                            pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 }
                 if (tid < BLIST_MAX + 2) B.hist[tid] = 0u;
@@ -528,7 +537,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
             const uint32_t ti = min(hi >> 28, nt - 1u);
             int n = 0;
             if (FLAT >= 2) {  // variant 6 (and 7 when not staged, never reached)
-                const int nl = brick_rows_collect<T>(spos, svel, list, cap, hstart, HY, HZ, hx, hy, hz, pi,
+                const int nl = brick_rows_collect<T>(spos, svel, list, cap, hstart, hlo, HY, HZ, hx, hy, hz, pi,
                                                   vi, spair, nt, th_lo, th_hi, scale, F);
                 brick_list_eval<T>(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
@@ -615,7 +624,7 @@ struct CellWarp {
 
 struct CellLayout {
     uint32_t hc_max, maxb;
-    uint32_t off_pair, off_hstart, off_hslot, off_pos, off_vel, off_f, off_warp, bytes;
+    uint32_t off_pair, off_hstart, off_hslot, off_hlo, off_pos, off_vel, off_f, off_warp, bytes;
 };
 
 __host__ __device__ inline CellLayout cell_layout(uint32_t hc_max, uint32_t maxb, uint32_t npair)
@@ -631,6 +640,8 @@ __host__ __device__ inline CellLayout cell_layout(uint32_t hc_max, uint32_t maxb
     off += 4 * (hc_max + 1);
     L.off_hslot = off;
     off += 4 * hc_max;
+    L.off_hlo = off;
+    off += 2 * hc_max;
     off = (off + 15) & ~15u;
     L.off_pos = off;
     off += 16 * maxb;
@@ -697,6 +708,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
     float2 *spair = reinterpret_cast<float2 *>(smem_raw + lay.off_pair);
     uint32_t *hstart = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hstart);
     uint32_t *hslot = reinterpret_cast<uint32_t *>(smem_raw + lay.off_hslot);
+    uint16_t *hlo = reinterpret_cast<uint16_t *>(smem_raw + lay.off_hlo);
     float4 *spos = reinterpret_cast<float4 *>(smem_raw + lay.off_pos);
     float4 *svel = reinterpret_cast<float4 *>(smem_raw + lay.off_vel);
     float *sfx = reinterpret_cast<float *>(smem_raw + lay.off_f);
@@ -720,7 +732,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force32_cells(KArgs a, CellLa
 
         // ---- 1-2. halo cells (hstart, hslot, home rows) and staging
         uint32_t total = 0, n_home = 0;
-        brick_halo_and_stage(a, w, br, H, hstart, hslot, spos, svel, lay.maxb, total, n_home);
+        brick_halo_and_stage(a, w, br, H, hstart, hslot, hlo, spos, svel, lay.maxb, total, n_home);
         const bool staged = total <= lay.maxb;
 
         // ---- pair forces: one warp per home cell

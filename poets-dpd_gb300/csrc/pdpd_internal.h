@@ -92,6 +92,8 @@ struct KArgs {
     uint32_t *ids;       // bead id of each sorted slot
     uint32_t *cellg;     // global cell of each sorted slot
     uint32_t *slot_of_id;   // sorted slot of each polymer bead, by id (monomers: not kept)
+    uint16_t *zlo;       // FP32: beads of each cell in its lower z half (offset z < 0.5), which
+                         // the sort places first; not written for empty cells
     // advanced, not yet sorted state (B), indexed by the A slot it came from
     void *posB, *velB, *frcB;
     uint2 *keyrank;      // (new global cell, arrival rank in that cell)

@@ -4,13 +4,16 @@
 // also gives the bead a provisional rank inside its new cell).  Here:
 //   1. k_scan_reduce + k_scan_final: exclusive prefix sum of the counts -> start[] (and
 //      the counts are cleared for the next step);
-//   2. k_place: each bead writes (old slot, id, cell) at start[cell] + provisional rank;
-//   3. k_canon: each placed bead re-ranks itself by bead id inside its cell and moves its
-//      payload to start[cell] + id-rank.
+//   2. k_place: each bead writes (old slot, id, cell, z half) at start[cell] + provisional rank;
+//   3. k_canon: each placed bead re-ranks itself by (z half, bead id) inside its cell and
+//      moves its payload to start[cell] + that rank.
 // The result is canonical: cells in index order, beads inside a cell in ascending bead id,
 // whatever order the atomics ran in.  That is the order in which the reference's cell lists
-// hold beads (naive_dpd_engine_half_step.hpp:276-293), so the force kernels can add pair
-// forces in the reference's order and the engine is deterministic run to run.
+// hold beads (naive_dpd_engine_half_step.hpp:276-293), so the FP64 force kernel adds pair
+// forces in the reference's order and the engine is deterministic run to run.  The FP32
+// engine marks beads whose cell offset z is >= 0.5 (bit 31 of the arrival rank): they follow
+// the lower-half beads of their cell, still in id order, and zlo[cell] counts the lower
+// half, so the FP32 neighbour walk can skip the far half of an end cell.
 #include "pdpd_device.cuh"
 
 namespace pdpd {
@@ -116,8 +119,8 @@ __global__ void k_place(uint32_t n, const uint2 *__restrict__ keyrank,
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     uint2 kr = keyrank[s];
-    uint32_t dst = start[kr.x] + kr.y;
-    tmp[dst] = make_uint4(s, ids[s], kr.x, 0u);
+    uint32_t dst = start[kr.x] + (kr.y & 0x7fffffffu);
+    tmp[dst] = make_uint4(s, ids[s], kr.x, kr.y >> 31);
 }
 
 // The bead hash carried in the w component of a position payload.
@@ -150,14 +153,20 @@ __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_
                         const P *__restrict__ frc_in, P *__restrict__ pos_out,
                         P *__restrict__ vel_out, P *__restrict__ frc_out,
                         uint32_t *__restrict__ ids_out, uint32_t *__restrict__ cellg_out,
-                        uint32_t *__restrict__ slot_of_id, float4 *__restrict__ shadow_out)
+                        uint32_t *__restrict__ slot_of_id, float4 *__restrict__ shadow_out,
+                        uint16_t *__restrict__ zlo)
 {
     uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
     uint4 e = tmp[d];
     uint32_t b = start[e.z], end = start[e.z + 1];
-    uint32_t rank = 0;
-    for (uint32_t k = b; k < end; k++) rank += tmp[k].y < e.y ? 1u : 0u;
+    uint32_t rank = 0, lo = 0;
+    for (uint32_t k = b; k < end; k++) {
+        const uint4 o = tmp[k];
+        rank += (o.w < e.w || (o.w == e.w && o.y < e.y)) ? 1u : 0u;
+        lo += o.w == 0u ? 1u : 0u;
+    }
+    if (zlo && rank == 0) zlo[e.z] = (uint16_t)min(lo, 0xffffu);
     uint32_t dst = b + rank;
     const P p = pos_in[e.x];
     pos_out[dst] = p;
@@ -184,13 +193,13 @@ int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t
                                        (const Vec4d *)a.velB,
                                        with_force ? (const Vec4d *)a.frcB : nullptr,
                                        (Vec4d *)a.posA, (Vec4d *)a.velA, (Vec4d *)a.frc, a.ids,
-                                       a.cellg, a.slot_of_id, a.posf);
+                                       a.cellg, a.slot_of_id, a.posf, nullptr);
     } else {
         k_canon<float4><<<g, T, 0, s>>>(a.n_beads, a.tmp, a.start, (const float4 *)a.posB,
                                         (const float4 *)a.velB,
                                         with_force ? (const float4 *)a.frcB : nullptr,
                                         (float4 *)a.posA, (float4 *)a.velA, (float4 *)a.frc,
-                                        a.ids, a.cellg, a.slot_of_id, nullptr);
+                                        a.ids, a.cellg, a.slot_of_id, nullptr, a.zlo);
     }
     return 4;
 }
