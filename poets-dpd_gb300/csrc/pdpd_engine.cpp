@@ -420,8 +420,8 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
-        static const int cand[][4] = {{8, 4, 8, 8}, {8, 6, 8, 6}, {8, 4, 6, 10}, {6, 3, 4, 6},
-                                      {6, 3, 3, 8}, {7, 3, 3, 8}, {6, 4, 4, 6}, {1, 4, 4, 4}};
+        static const int cand[][4] = {{8, 4, 8, 8}, {8, 6, 8, 6}, {8, 4, 6, 10}, {8, 4, 7, 10},
+                                      {6, 3, 4, 6}, {6, 3, 3, 8}, {6, 4, 4, 6}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
         if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;
