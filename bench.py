@@ -1,23 +1,35 @@
-"""Benchmark of the GB300 DPD engine: bead-steps/s on the 128^3 polymer-solvent box.
+"""Benchmark of the GB300 DPD engine: bead-steps/s of the FP32 batched engine on the
+512-state grid against the plain one-state-at-a-time FP64 engine, with the served stream's
+p50/p99 job latency and the 128^3 HBM-roofline run beside it.
 
-Workload (default): 128x128x128 periodic box at density 3 = 6,291,456 beads, types W/H/T,
-5% of the beads in H-T-T-T-T-T chains (Hookean k=128 r0=0.5, angle k=20 theta0=0),
-a_WW=a_HH=a_TT=25, a_WH=35, a_WT=a_HT=75, gamma=4.5, dt=0.01, FP32 engine.  Synthetic data:
-seeded uniform positions, Gaussian kT=1 velocities.  A "step" is one DPD timestep of the
-whole box.  The state (~300 MB of bead payload) is larger than L2, so no flush is needed.
+Workload (default, `batched512`): 512 independent polymer-solvent states, cube side uniform
+on 8..32 (17,880,960 beads in total), types W/H/T, 5% of the beads in H-T-T-T-T-T chains
+(Hookean k=128 r0=0.5, angle k=20 theta0=0), a_WW=a_HH=a_TT=25, a_WH=35, a_WT ~ U[25,100]
+and gamma ~ U[3,6] per state, dt=0.01, state seed = index + 1.  Synthetic data: seeded uniform
+positions, Gaussian kT=1 velocities.  A "step" is one DPD timestep of every state.  The
+grid's bead payload (~1 GB) is larger than L2, so no flush is needed.
 
-  value     bead-steps/s with the state resident on the GPU: K steps timed with CUDA events
-            on the engine's stream (graph replays), barrier + synchronize on both sides.
-  e2e       the same metric through the C ABI with host buffers: Attach (upload) + Run(K) +
-            read back x, v, f, timed on the host.
-  roofline  the force kernel (dominant): algorithmic bytes per launch (1,180 B per
-            bead-step x beads) / its average CUDA-event duration, against the measured HBM
-            copy bandwidth.
+  value     FP32 bead-steps/s of the whole grid resident on the GPU (one arena, one brick work
+            queue, each step one CUDA-graph replay, autotuned kernel): K steps timed with CUDA
+            events on the engine's stream, barrier + synchronize on both sides.
+  e2e       the same metric through the C ABI with host buffers: AttachBatch (upload of the
+            512 states) + Run(K) + read-back of x, v, f of every state, timed on the host.
+  plain_fp64  the plain FP64 engine run one state at a time (Attach excluded, as the
+            reference's bpsExec), and the batched / plain ratio.
+  roofline  the force pass (bond kernel + brick kernel, dominant): algorithmic bytes per launch
+            (1,180 B per bead-step x beads) / its average CUDA-event duration, against the
+            measured HBM copy bandwidth.
+  roofline_run  the 128^3 box (6,291,456 beads, same chain recipe, a_WT = 75, gamma = 4.5):
+            value, e2e, roofline and phases of the single large state.
+  serving   the served stream (Poisson arrivals, continuous batching): p50/p99 latency and
+            served bead-steps/s against sequential execution.
   cpu_baseline  the oracle (C restatement of the reference's FP64 half-step engine) on all
-            host cores, on a bounded sample of the same recipe.
+            host cores, on a bounded sample of the same workload.
 
+--workload polymer128 (or polymer32, water8) makes the single box the headline instead.
 --impl reference times the reference's CPU implementation of the path (the oracle port;
-the reference sources are not present where this runs) on the same recipe and metric.
+the reference sources are not present where this runs) on a bounded sample of the same
+workload and metric.
 """
 
 from __future__ import annotations
@@ -48,6 +60,9 @@ WORKLOADS = {
     "polymer32": (32, 0.10, 2, 0.01),
     "water8": (8, 0.0, 1, 0.02),
 }
+GRID = "batched512"          # the 512-state grid (pdpd_world.make_batched_grid)
+GRID_STATES = 512
+REF_SAMPLE_BEADS = 200_000   # the CPU sample of the grid: its first states up to this size
 
 
 def make_world(name, side=None):
@@ -141,38 +156,43 @@ def oracle_rate(world, max_seconds=12.0, max_steps=200, threads=None):
     return world.n_beads * steps / dt, threads, steps, dt
 
 
-def batched_grid_metrics(steps=200, plain_steps=10, n_states=512, device=0):
-    """512 independent polymer-solvent states, cube side uniform on 8..32, per-state
-    a_WT ~ U[25,100] and gamma ~ U[3,6], 5% chains, dt = 0.01, seeds = index + 1.
+def grid_sample(n_states=GRID_STATES, min_beads=REF_SAMPLE_BEADS):
+    """The grid's first states, as many as reach min_beads (the same states every run)."""
+    worlds = []
+    for w in W.make_batched_grid(n_states, count=16):
+        worlds.append(w)
+        if sum(x.n_beads for x in worlds) >= min_beads:
+            break
+    return worlds
 
-    FP32 batched: all states attached to one engine (one arena, one brick work queue over all
-    states, each step one CUDA-graph replay), autotuned, `steps` steps timed with CUDA events.
-    FP64 plain: the FP64 engine run one state at a time (Attach excluded from the time, as the
+
+def oracle_rate_multi(worlds, max_seconds=12.0, max_steps=200, threads=None):
+    """Oracle bead-steps/s on all host cores over several states: a step is one step of
+    every state in turn; runs steps until max_seconds or max_steps."""
+    import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    ows = [O.OracleWorld(w) for w in worlds]
+    for ow in ows:
+        ow.run(1, nthreads=threads)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < max_seconds:
+        for ow in ows:
+            ow.run(1, nthreads=threads)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return sum(w.n_beads for w in worlds) * steps / dt, threads, steps, dt
+
+
+def plain_fp64_metrics(worlds, plain_steps=10, device=0):
+    """The plain FP64 engine run one state at a time (Attach excluded from the time, as the
     reference's bpsExec), `plain_steps` steps per state, CUDA events around each Run."""
     import torch
 
     import pdpd_engine as E
 
-    worlds = W.make_batched_grid(n_states)
-    total = sum(w.n_beads for w in worlds)
     dev = torch.device("cuda", device)
-    eng = E.GB300DPDEngine("fp32", device=device)
-    eng.SetConfigEntry("autotune", 1)
-    eng.AttachBatch([w.copy() for w in worlds])
-    eng.run_async(40)  # the autotuner's trials are the first of these steps
-    eng.sync()
-    stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    eng.run_async(steps)
-    ev1.record(stream)
-    eng.sync()
-    torch.cuda.synchronize()
-    batched = total * steps / (ev0.elapsed_time(ev1) / 1e3)
-    tuned = {n: v for n, _, v in eng.GetConfigEntries()}
-    eng.close()
-
+    total = sum(w.n_beads for w in worlds)
     e64 = E.GB300DPDEngine("fp64", device=device)
     s64 = torch.cuda.ExternalStream(e64.stream(), device=dev)
     ms_total = 0.0
@@ -187,13 +207,11 @@ def batched_grid_metrics(steps=200, plain_steps=10, n_states=512, device=0):
         e64.sync()
         torch.cuda.synchronize()
         ms_total += a.elapsed_time(b)
-    plain = total * plain_steps / (ms_total / 1e3)
     e64.close()
-    return {"workload": f"{n_states} states, sides 8..32, {total} beads, 5% H-T5 chains",
-            "beads": total, "fp32_batched": batched, "fp64_plain_state_by_state": plain,
-            "ratio": batched / plain, "steps": steps, "plain_steps_per_state": plain_steps,
-            "autotuned": {k: tuned[k] for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
-                                                "autotune")}}
+    return {"value": total * plain_steps / (ms_total / 1e3), "unit": "bead-steps/s",
+            "steps_per_state": plain_steps,
+            "note": "FP64 engine (bit-exact with the reference), one state at a time, "
+                    "Attach excluded"}
 
 
 def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed=5, device=0,
@@ -322,82 +340,106 @@ def aggregate_rate(units_per_rank: float, ms: float, world_size: int) -> float:
 
 
 def run_reference_arm(args):
+    """The reference's CPU implementation of the path (the oracle port) on a bounded sample of
+    the workload, all host cores; rank 0 only (the other ranks exit without work)."""
     rank, world_size, _ = dist_setup(args.gpus)
     if rank != 0:
         return
-    side = args.ref_side
-    world = make_world(args.workload, side=side)
     import oracle as O
 
+    if args.workload == GRID:
+        worlds = grid_sample()
+        workload = grid_workload_name(GRID_STATES)
+        sample = (f"the grid's first {len(worlds)} states ({sum(w.n_beads for w in worlds)} "
+                  f"beads), one step of each per step")
+    else:
+        worlds = [make_world(args.workload, side=args.ref_side)]
+        L = WORKLOADS[args.workload][0]
+        workload = f"{args.workload}: {L}^3 polymer-solvent box recipe"
+        sample = f"{args.ref_side}^3 box of the same recipe ({worlds[0].n_beads} beads)"
     threads = os.cpu_count() or 1
-    ow = O.OracleWorld(world)
+    ows = [O.OracleWorld(w) for w in worlds]
     for _ in range(args.warmup):
-        ow.run(1, nthreads=threads)
+        for ow in ows:
+            ow.run(1, nthreads=threads)
     t0 = time.perf_counter()
-    ow.run(args.steps, nthreads=threads)
+    for _ in range(args.steps):
+        for ow in ows:
+            ow.run(1, nthreads=threads)
     dt = time.perf_counter() - t0
-    rate = world.n_beads * args.steps / dt
-    L = WORKLOADS[args.workload][0]
+    rate = sum(w.n_beads for w in worlds) * args.steps / dt
     line = {
-        "impl": "reference", "metric": "bead-steps/s", "value": rate, "unit": "bead-steps/s",
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "bead-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {L}^3 polymer-solvent box recipe",
-                   "sample": f"{side}^3 box of the same recipe ({world.n_beads} beads)",
-                   "parallelism": "replicas only"},
+        "config": {"workload": workload, "sample": sample, "parallelism": "replicas only"},
         "cpu_baseline": {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{side}^3 box, {world.n_beads} beads, {args.steps} steps"},
+                         "sample": f"{sample}, {args.steps} steps"},
         "e2e": {"value": rate, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_engine_arm(args):
+def grid_workload_name(n_states):
+    part = "" if n_states == GRID_STATES else f" (its first {n_states})"
+    return (f"{GRID}: {GRID_STATES} polymer-solvent states{part}, sides U{{8..32}}, density 3, "
+            f"5% H-T5 chains, a_WT ~ U[25,100], gamma ~ U[3,6], fp32 batched")
+
+
+def upload_bytes(worlds):
+    """Host-to-device bytes of an Attach: x, v, f (doubles) and the hash of every bead, the
+    bond CSR rows and terms."""
+    total = 0
+    for w in worlds:
+        n = w.n_beads
+        bb, _, _, ab, _, _ = w.flat_bonds()
+        total += n * (9 * 8 + 4) + (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
+    return total
+
+
+def force_roofline(phases, beads, precision, traffic_key=None):
+    """Roofline of the force pass from profile_run's per-phase CUDA-event times; traffic from
+    the ncu capture summarised in profiles/force_kernel_traffic.json (per bead-step)."""
+    force_ms = phases["force_ms"] / max(1, phases["force_launches"])
+    peak, peak_kind = measured_peaks()
+    achieved = ALGO_BYTES[precision] * beads / (force_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "force_kernel_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tj = json.load(fh)
+        key = f"{traffic_key or precision}_bytes_per_bead_step"
+        if key in tj:
+            traffic = tj[key] * beads
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "kernel": "force", "kernel_ms": force_ms,
+            "algo_bytes_per_bead_step": ALGO_BYTES[precision], "peak_source": peak_kind,
+            "compulsory_frac": COMPULSORY_BYTES * beads / (force_ms / 1e3) / 1e9 / peak}
+    ph = {"force": force_ms, "sort": phases["sort_ms"] / max(1, phases["sort_launches"])}
+    return roof, ph
+
+
+def tune(eng, attach, steps=64):
+    """Autotune once (its trials are ordinary steps: the trajectory does not depend on the
+    choice), then keep the chosen kernel and brick shape fixed."""
+    eng.SetConfigEntry("autotune", 1)
+    attach()
+    eng.run_async(steps)
+    eng.sync()
+    tuned = {k: v for k, _, v in eng.GetConfigEntries()}
+    eng.SetConfigEntry("autotune", 0)
+    return {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+
+
+def timed_run(eng, steps, warmup, dev, local, world_size, attach):
+    """Resident-state rate: attach, warm up, then `steps` graph replays between CUDA events on
+    the engine's stream (barrier + synchronize on both sides), clocks sampled meanwhile."""
     import torch
 
-    import pdpd_engine as E
-
-    rank, world_size, local = dist_setup(args.gpus)
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    world = make_world(args.workload, side=args.side)
-    n = world.n_beads
-    eng = E.GB300DPDEngine(args.precision, device=local)
-
-    # --- autotune once (its trials are ordinary steps: the trajectory does not depend on the
-    # choice), then fix the chosen kernel and brick shape for every measurement below
-    if args.precision == "fp32" and args.autotune:
-        eng.SetConfigEntry("autotune", 1)
-        eng.Attach(world.copy())
-        eng.run_async(64)
-        eng.sync()
-        tuned = {k: v for k, _, v in eng.GetConfigEntries()}
-        eng.SetConfigEntry("autotune", 0)
-    else:
-        tuned = {k: v for k, _, v in eng.GetConfigEntries()}
-
-    # --- e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
-    w_e2e = world.copy()
-    eng.Attach(w_e2e)
-    eng.Run(args.warmup)
-    torch.cuda.synchronize()
-    w_e2e = world.copy()
-    t0 = time.perf_counter()
-    eng.Attach(w_e2e)
-    eng.Run(args.steps)  # Run() reads x, v, f back into the host world
-    e2e_dt = time.perf_counter() - t0
-    h2d = n * (9 * 8 + 4)
-    bb, _, _, ab, _, _ = w_e2e.flat_bonds()
-    h2d += (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
-    d2h = n * 9 * 8
-    e2e_rate = n * args.steps / e2e_dt
-
-    # --- value: resident state, graph replays, CUDA events on the engine's stream
-    w = world.copy()
-    eng.Attach(w)
-    eng.run_async(args.warmup)
+    attach()
+    eng.run_async(warmup)
     eng.sync()
     stream = torch.cuda.ExternalStream(eng.stream(), device=dev)
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -409,21 +451,88 @@ def run_engine_arm(args):
     with ClockSampler(local) as clocks:
         time.sleep(0.3)
         ev0.record(stream)
-        eng.run_async(args.steps)
+        eng.run_async(steps)
         ev1.record(stream)
         eng.sync()
         torch.cuda.synchronize()
         time.sleep(0.2)
     launches = eng.kernel_launches() - launches0
     ms = max_over_ranks(ev0.elapsed_time(ev1), world_size)
-    value = aggregate_rate(n * args.steps, ms, world_size)
+    return ms, launches, clocks.summary()
 
-    # --- dominant kernel: per-phase CUDA-event times over the same number of steps
-    phases = eng.profile_run(args.steps)
 
-    # --- interval snapshots: the v2binary section encoded on the GPU vs the full read-back
-    snapshot = None
-    if world_size == 1 and args.precision in ("fp32", "fp64"):
+def measure_grid(args, dev, local, world_size):
+    """The headline: the 512-state grid on one FP32 engine."""
+    import pdpd_engine as E
+
+    n_states = args.grid_states
+    worlds = W.make_batched_grid(GRID_STATES, count=n_states)
+    total = sum(w.n_beads for w in worlds)
+    eng = E.GB300DPDEngine("fp32", device=local)
+    if args.autotune:
+        tuned = tune(eng, lambda: eng.AttachBatch([w.copy() for w in worlds]))
+    else:
+        tuned = {k: v for k, _, v in eng.GetConfigEntries()
+                 if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+    # e2e: AttachBatch (upload) + Run(K) + read-back of every state, host buffers
+    eng.AttachBatch([w.copy() for w in worlds])
+    eng.Run(args.warmup)
+    hw = [w.copy() for w in worlds]
+    t0 = time.perf_counter()
+    eng.AttachBatch(hw)
+    eng.Run(args.steps)  # Run() reads x, v, f of every state back into the host worlds
+    e2e_dt = time.perf_counter() - t0
+    e2e = {"value": total * args.steps / e2e_dt, "unit": "bead-steps/s",
+           "h2d_bytes_per_step": upload_bytes(worlds) / args.steps,
+           "d2h_bytes_per_step": total * 72 / args.steps,
+           "note": "AttachBatch (upload of all states) + Run(K) + read-back of x, v, f of every "
+                   "state; bytes are per step of K"}
+    ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
+                                     lambda: eng.AttachBatch([w.copy() for w in worlds]))
+    roof, ph = force_roofline(eng.profile_run(args.steps), total, "fp32", "fp32_grid")
+    eng.close()
+    plain = plain_fp64_metrics(worlds, device=local) if not args.no_plain else None
+    value = aggregate_rate(total * args.steps, ms, world_size)
+    if plain:
+        plain["batched_vs_plain"] = value / world_size / plain["value"]
+    return {"value": value, "ms": ms, "beads": total, "e2e": e2e, "launches": launches,
+            "clocks": clocks, "roofline": roof, "phases": ph, "tuned": tuned, "plain_fp64": plain,
+            "config": {"workload": grid_workload_name(n_states), "states": n_states,
+                       "beads": total, "precision": "fp32",
+                       "l2": "state > L2 (no flush)",
+                       "parallelism": "replicas only" if world_size > 1 else "single GPU"}}
+
+
+def measure_box(args, name, side, precision, dev, local, world_size, autotune, snapshot=True):
+    """One large state (the 128^3 HBM-roofline run by default)."""
+    import pdpd_engine as E
+
+    world = make_world(name, side=side)
+    n = world.n_beads
+    eng = E.GB300DPDEngine(precision, device=local)
+    if precision == "fp32" and autotune:
+        tuned = tune(eng, lambda: eng.Attach(world.copy()))
+    else:
+        tuned = {k: v for k, _, v in eng.GetConfigEntries()
+                 if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+    # e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
+    eng.Attach(world.copy())
+    eng.Run(args.warmup)
+    w_e2e = world.copy()
+    t0 = time.perf_counter()
+    eng.Attach(w_e2e)
+    eng.Run(args.steps)  # Run() reads x, v, f back into the host world
+    e2e_dt = time.perf_counter() - t0
+    e2e = {"value": n * args.steps / e2e_dt, "unit": "bead-steps/s",
+           "h2d_bytes_per_step": upload_bytes([world]) / args.steps,
+           "d2h_bytes_per_step": n * 72 / args.steps,
+           "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"}
+    ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
+                                     lambda: eng.Attach(world.copy()))
+    roof, ph = force_roofline(eng.profile_run(args.steps), n, precision)
+    snap = None
+    if snapshot and world_size == 1:
+        # interval snapshots: the v2binary section encoded on the GPU vs the full read-back
         sec_bytes = eng.v2binary_prepare()
         eng.v2binary_encode()
         eng.read_state(0)
@@ -436,26 +545,39 @@ def run_engine_arm(args):
         for _ in range(reps):
             eng.read_state(0)
         t_rs = (time.perf_counter() - t0) / reps
-        snapshot = {"v2binary_bytes_per_bead": sec_bytes / n, "v2binary_ms": 1e3 * t_v2,
-                    "read_state_bytes_per_bead": 72.0, "read_state_ms": 1e3 * t_rs,
-                    "note": "one snapshot of the whole box: GPU-encoded v2binary section vs x, v, f "
-                            "read back as doubles (wall clock, host buffers)"}
-    force_ms = phases["force_ms"] / max(1, phases["force_launches"])
-    peak, peak_kind = measured_peaks()
-    algo = ALGO_BYTES[args.precision] * n
-    achieved = algo / (force_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "force_kernel_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as fh:
-            tj = json.load(fh)
-        key = f"{args.precision}_bytes_per_bead_step"
-        if key in tj:
-            traffic = tj[key] * n
+        snap = {"v2binary_bytes_per_bead": sec_bytes / n, "v2binary_ms": 1e3 * t_v2,
+                "read_state_bytes_per_bead": 72.0, "read_state_ms": 1e3 * t_rs,
+                "note": f"one snapshot of the {side or WORKLOADS[name][0]}^3 box: GPU-encoded "
+                        f"v2binary section vs x, v, f read back as doubles (wall clock, host "
+                        f"buffers)"}
+    eng.close()
+    L = side or WORKLOADS[name][0]
+    return {"value": aggregate_rate(n * args.steps, ms, world_size), "ms": ms, "beads": n,
+            "e2e": e2e, "launches": launches, "clocks": clocks, "roofline": roof, "phases": ph,
+            "tuned": tuned, "snapshot": snap,
+            "config": {"workload": f"{name}: {L}^3 box, density 3, {n} beads, "
+                                   f"{WORKLOADS[name][1]:.0%} H-T5 chains, {precision}",
+                       "beads": n, "precision": precision, "l2": "state > L2 (no flush)",
+                       "parallelism": "replicas only" if world_size > 1 else "single GPU"}}
 
-    batched = None
-    if not args.no_batched and world_size == 1:
-        batched = batched_grid_metrics(device=local)
+
+def run_engine_arm(args):
+    import torch
+
+    rank, world_size, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    grid = args.workload == GRID
+    if grid:
+        main = measure_grid(args, dev, local, world_size)
+        side = None
+        if not args.no_roofline_run:
+            side = measure_box(args, "polymer128", args.side, "fp32", dev, local, world_size,
+                               args.autotune)
+    else:
+        main = measure_box(args, args.workload, args.side, args.precision, dev, local, world_size,
+                           args.autotune)
+        side = None
     serving = None
     if args.serving_window > 0 and world_size == 1:
         serving = serving_metrics(window_s=args.serving_window, device=local)
@@ -463,41 +585,43 @@ def run_engine_arm(args):
         return
     cpu = None
     if not args.no_cpu_baseline:
-        sample_side = args.ref_side
-        rate, threads, steps, dt = oracle_rate(make_world(args.workload, side=sample_side))
+        if grid:
+            sample = grid_sample()
+            rate, threads, steps, dt = oracle_rate_multi(sample)
+            desc = (f"the grid's first {len(sample)} states ({sum(w.n_beads for w in sample)} "
+                    f"beads), {steps} steps of each in {dt:.1f} s")
+        else:
+            rate, threads, steps, dt = oracle_rate(make_world(args.workload, side=args.ref_side))
+            desc = f"{args.ref_side}^3 box of the same recipe, {steps} steps in {dt:.1f} s"
         cpu = {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-               "sample": f"{sample_side}^3 box of the same recipe, {steps} steps in {dt:.1f} s"}
-    L = args.side or WORKLOADS[args.workload][0]
+               "sample": desc}
     line = {
-        "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world_size,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "metric": METRIC, "value": main["value"], "unit": "bead-steps/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {L}^3 box, density 3, {n} beads, "
-                               f"{WORKLOADS[args.workload][1]:.0%} H-T5 chains, {args.precision}",
-                   "beads": n, "precision": args.precision, "l2": "state > L2 (no flush)",
-                   "parallelism": "replicas only" if world_size > 1 else "single GPU"},
-        "e2e": {"value": e2e_rate, "unit": "bead-steps/s", "h2d_bytes_per_step": h2d / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps,
-                "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "force", "kernel_ms": force_ms,
-                     "algo_bytes_per_bead_step": ALGO_BYTES[args.precision],
-                     "peak_source": peak_kind,
-                     "compulsory_frac": COMPULSORY_BYTES * n / (force_ms / 1e3) / 1e9 / peak},
-        "phases_ms_per_step": {"force": force_ms,
-                               "sort": phases["sort_ms"] / max(1, phases["sort_launches"])},
-        "clocks": clocks.summary(),
-        "gpu_launches": launches,
+        "dtype": "f32" if (grid or args.precision == "fp32") else "f64", "data": "synthetic",
+        "config": main["config"],
+        "e2e": main["e2e"],
+        "roofline": main["roofline"],
+        "phases_ms_per_step": main["phases"],
+        "clocks": main["clocks"],
+        "gpu_launches": main["launches"],
         "cpu_baseline": cpu,
-        "batched_grid": batched,
+        "plain_fp64": main.get("plain_fp64"),
         "serving": serving,
-        "snapshot": snapshot,
-        "kernel_config": {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z",
-                                                    "autotune")},
+        "roofline_run": None if side is None else {
+            "workload": side["config"]["workload"], "value": side["value"],
+            "ms_per_step": side["ms"] / args.steps, "e2e": side["e2e"],
+            "roofline": side["roofline"], "phases_ms_per_step": side["phases"],
+            "clocks": side["clocks"], "gpu_launches": side["launches"],
+            "kernel_config": side["tuned"]},
+        "snapshot": (side or main).get("snapshot"),
+        "kernel_config": main["tuned"],
     }
     print(json.dumps(line), flush=True)
+
+
+METRIC = "bead-steps/s (FP32 batched vs plain FP64); served p50/p99 job latency"
 
 
 def main():
@@ -506,19 +630,24 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="polymer128", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--workload", default=GRID, choices=[GRID] + sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"],
+                    help="precision of a single-box workload (the grid is FP32)")
     ap.add_argument("--ref-side", type=int, default=32,
-                    help="box side of the bounded CPU sample (same recipe)")
+                    help="box side of the bounded CPU sample of a single-box workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batched", action="store_true",
-                    help="skip the 512-state batched grid (FP32 batched vs FP64 plain)")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 state-by-state run of the grid")
+    ap.add_argument("--no-roofline-run", action="store_true",
+                    help="skip the 128^3 single-box run beside the grid")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: autotune the FP32 force kernel first (default); 0: default kernel")
     ap.add_argument("--serving-window", type=float, default=4.0,
                     help="seconds of Poisson arrivals of the serving stream (0 skips it)")
+    ap.add_argument("--grid-states", type=int, default=GRID_STATES,
+                    help="run the grid's first N states only (profiling on a smaller grid)")
     ap.add_argument("--side", type=int, default=None,
-                    help="override the box side of the workload (profiling on smaller boxes)")
+                    help="override the box side of the single-box run (profiling on smaller boxes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -1090,7 +1090,26 @@ static int download(pdpd_engine *e, int buf, cudaStream_t s)
     if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
         return e->fail(PDPD_E_NOMEM, "staging allocation failed");
     a.staging = e->d_staging[buf].as<double>();
-    e->launches += e->fp64() ? launch_unsort64(a, s) : launch_unsort32(a, s);
+    e->launches += e->fp64() ? launch_unsort64(a, s, 0, e->n_beads) : launch_unsort32(a, s);
+    return PDPD_OK;
+}
+
+// Unsort one world only (its own work tiles) into device staging buffer `buf`: the rows
+// of its beads, so reading every world of a batch in turn costs one pass over the arena.
+static int download_world(pdpd_engine *e, int buf, uint32_t world, cudaStream_t s)
+{
+    KArgs a = e->args;
+    if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "staging allocation failed");
+    uint32_t first = 0;
+    for (uint32_t k = 0; k < world; k++) first += (e->worlds[k].dev.n_beads + TILE_BEADS - 1) / TILE_BEADS;
+    a.tiles = e->args.tiles + first;
+    a.n_tiles = (e->worlds[world].dev.n_beads + TILE_BEADS - 1) / TILE_BEADS;
+    if (a.n_tiles == 0) return PDPD_OK;
+    a.grid_blocks = (int)std::min<uint32_t>((uint32_t)std::max(1, e->args.grid_blocks), a.n_tiles);
+    a.staging = e->d_staging[buf].as<double>();
+    const WorldDev &wd = e->worlds[world].dev;
+    e->launches += e->fp64() ? launch_unsort64(a, s, wd.bead_base, wd.n_beads) : launch_unsort32(a, s);
     return PDPD_OK;
 }
 
@@ -1114,7 +1133,7 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
     if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
     cudaSetDevice(e->device);
-    int rc = download(e, 0, e->stream);
+    int rc = download_world(e, 0, world, e->stream);
     if (rc) return rc;
     const WorldDev &wd = e->worlds[world].dev;
     size_t nbytes = sizeof(double) * 9 * (size_t)wd.n_beads;

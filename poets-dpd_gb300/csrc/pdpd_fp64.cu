@@ -574,10 +574,11 @@ __global__ void k_finish64(KArgs a)
         for (uint32_t w = threadIdx.x; w < a.n_worlds; w += blockDim.x) a.worlds[w].t += 1;
 }
 
-__global__ void k_unsort64(KArgs a)
+__global__ void k_unsort64(KArgs a, uint32_t first, uint32_t count)
 {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n_beads) return;
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t s = first + k;
     const Vec4d p = ((const Vec4d *)a.posA)[s];
     const Vec4d v = ((const Vec4d *)a.velA)[s];
     const Vec4d f = ((const Vec4d *)a.frc)[s];
@@ -628,10 +629,10 @@ int launch_finish64(const KArgs &a, cudaStream_t s)
     return 1;
 }
 
-int launch_unsort64(const KArgs &a, cudaStream_t s)
+int launch_unsort64(const KArgs &a, cudaStream_t s, uint32_t first, uint32_t count)
 {
-    if (a.n_beads == 0) return 0;
-    k_unsort64<<<(a.n_beads + 255) / 256, 256, 0, s>>>(a);
+    if (count == 0) return 0;
+    k_unsort64<<<(count + 255) / 256, 256, 0, s>>>(a, first, count);
     return 1;
 }
 

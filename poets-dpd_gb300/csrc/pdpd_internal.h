@@ -143,7 +143,7 @@ int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
 int launch_begin64(const KArgs &a, cudaStream_t s);
 int launch_force64(const KArgs &a, int final_step, cudaStream_t s);
 int launch_finish64(const KArgs &a, cudaStream_t s);
-int launch_unsort64(const KArgs &a, cudaStream_t s);
+int launch_unsort64(const KArgs &a, cudaStream_t s, uint32_t first, uint32_t count);  // sorted slots [first, first + count)
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s);
 
 // Device RNG on arrays (device pointers), for known-answer tests.

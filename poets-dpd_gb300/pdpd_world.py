@@ -318,16 +318,17 @@ def make_polymer_box(L, chain_fraction=0.1, seed=2, a_wt=75.0, gamma=4.5, dt=0.0
 
 
 def make_batched_grid(n_states=512, side_lo=8, side_hi=32, chain_fraction=0.05, steps=200,
-                      gen_seed=4):
+                      gen_seed=4, count=None):
     """Batched grid of independent polymer-solvent states: cube side uniform on
     [side_lo, side_hi], per-state a_WT ~ U[25,100], gamma ~ U[3,6] (all pairs), state seed
-    = index+1, dt = 0.01."""
+    = index+1, dt = 0.01.  ``count`` builds only the first ``count`` states (the same ones the
+    full grid starts with)."""
     rng = np.random.default_rng(gen_seed)
     sides = rng.integers(side_lo, side_hi + 1, size=n_states)
     a_wt = rng.uniform(25.0, 100.0, size=n_states)
     gam = rng.uniform(3.0, 6.0, size=n_states)
     worlds = []
-    for i in range(n_states):
+    for i in range(n_states if count is None else min(count, n_states)):
         worlds.append(make_polymer_box(int(sides[i]), chain_fraction=chain_fraction, seed=i + 1,
                                        a_wt=float(a_wt[i]), gamma=float(gam[i]), dt=0.01,
                                        gen_seed=gen_seed * 100003 + i))

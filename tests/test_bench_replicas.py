@@ -22,7 +22,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, world_size, port, q):
+def _rank(rank, world_size, port, q, workload="polymer128"):
     os.environ.update({"RANK": str(rank), "LOCAL_RANK": str(rank), "WORLD_SIZE": str(world_size),
                        "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
     sys.path.insert(0, ROOT)
@@ -33,7 +33,7 @@ def _rank(rank, world_size, port, q):
     slowest = bench.max_over_ranks(10.0 * (rank + 1), ws)
     rate = bench.aggregate_rate(1000.0, slowest, ws)
     args = bench.argparse.Namespace(gpus=world_size, steps=2, warmup=3, ref_side=6,
-                                    workload="polymer128")
+                                    workload=workload)
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference_arm(args)
@@ -42,11 +42,12 @@ def _rank(rank, world_size, port, q):
 
 
 @pytest.mark.timeout(300)
-def test_replicas_two_gloo_ranks():
+@pytest.mark.parametrize("workload", ["polymer128", "batched512"])
+def test_replicas_two_gloo_ranks(workload):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(k, 2, port, q)) for k in range(2)]
+    procs = [ctx.Process(target=_rank, args=(k, 2, port, q, workload)) for k in range(2)]
     for p in procs:
         p.start()
     res = sorted(q.get(timeout=240) for _ in procs)
