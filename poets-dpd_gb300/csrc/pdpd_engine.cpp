@@ -371,15 +371,25 @@ struct pdpd_engine {
         a.bricks = nullptr;
         a.n_bricks = 0;
         if (fp64() || a.force_kernel == 1) return PDPD_OK;
+        // Each axis of a world is cut into ceil(L / b) bricks of as equal extents as possible
+        // (e.g. a side of 9 with b = 4 into 3 + 3 + 3, not 4 + 4 + 1): no extent exceeds the
+        // configured one, and no thin remainder brick stages a halo for a few home cells.
         std::vector<Brick> bricks;
+        auto cuts = [](int L, int b) {
+            std::vector<int> c;
+            const int n = (L + b - 1) / b;
+            for (int k = 0; k <= n; k++) c.push_back((int)((int64_t)L * k / n));
+            return c;
+        };
         for (uint32_t i = 0; i < worlds.size(); i++) {
             const int32_t *L = worlds[i].dev.L;
-            for (int x0 = 0; x0 < L[0]; x0 += cfg_brick[0])
-                for (int y0 = 0; y0 < L[1]; y0 += cfg_brick[1])
-                    for (int z0 = 0; z0 < L[2]; z0 += cfg_brick[2])
-                        bricks.push_back({i, x0, y0, z0, std::min(cfg_brick[0], L[0] - x0),
-                                          std::min(cfg_brick[1], L[1] - y0),
-                                          std::min(cfg_brick[2], L[2] - z0), 0});
+            const std::vector<int> cx = cuts(L[0], cfg_brick[0]), cy = cuts(L[1], cfg_brick[1]),
+                                   cz = cuts(L[2], cfg_brick[2]);
+            for (size_t a0 = 0; a0 + 1 < cx.size(); a0++)
+                for (size_t a1 = 0; a1 + 1 < cy.size(); a1++)
+                    for (size_t a2 = 0; a2 + 1 < cz.size(); a2++)
+                        bricks.push_back({i, cx[a0], cy[a1], cz[a2], cx[a0 + 1] - cx[a0],
+                                          cy[a1 + 1] - cy[a1], cz[a2 + 1] - cz[a2], 0});
         }
         size_t bytes_needed = sizeof(Brick) * std::max<size_t>(1, bricks.size());
         if (d_bricks.bytes < bytes_needed) {
