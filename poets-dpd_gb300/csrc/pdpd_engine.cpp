@@ -196,7 +196,7 @@ struct pdpd_engine {
     DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
-    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo, d_brick_next;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
@@ -250,7 +250,7 @@ struct pdpd_engine {
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
-                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo};
+                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -859,6 +859,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_start, sizeof(uint32_t) * ((size_t)nc + 1));
     A(e->d_cnt, sizeof(uint32_t) * (size_t)nc);
     A(e->d_zlo, f64 ? 16 : sizeof(uint16_t) * std::max<size_t>(1, (size_t)nc));
+    A(e->d_brick_next, 16);
     A(e->d_blocksums, sizeof(uint32_t) * (scan_blocks((uint32_t)nc) + 1));
     A(e->d_posA, P * nb);
     A(e->d_velA, P * nb);
@@ -1013,6 +1014,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     a.fbond = e->d_fbond.as<float4>();
     a.posf = f64 ? e->d_posf.as<float4>() : nullptr;
     a.zlo = f64 ? nullptr : e->d_zlo.as<uint16_t>();
+    a.brick_next = f64 ? nullptr : e->d_brick_next.as<uint32_t>();
     a.bterm = f64 ? e->d_bterm.p : nullptr;
     a.staging = e->d_staging[0].as<double>();
     a.block_threads = 128;

@@ -29,7 +29,19 @@ struct BrickHeader {
     WorldCache wc;
     uint32_t wsum[BRICK_MAX_WARPS];
     uint32_t home_rows[BRICK_MAX_ROWS + 1];
+    uint32_t next;  // the block's next brick
 };
+
+// A block's next brick: after its first (blockIdx.x), blocks take bricks from a shared
+// counter in the order they finish, so a block that drew small bricks takes more of them.
+// Which block computes a brick does not change any result.
+__device__ __forceinline__ uint32_t brick_fetch(const KArgs &a, BrickHeader &H)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) H.next = gridDim.x + atomicAdd(a.brick_next, 1u);
+    __syncthreads();
+    return H.next;
+}
 
 // Shared-memory layout of one block: header, hstart[HC+1], hslot[HC], pos[maxb], vel[maxb],
 // list[BLIST_MAX][threads].
@@ -419,7 +431,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
     const float min2 = min_dist_sqr_f();
     const float PRUNE = 1.0001f;
     const int cap = (a.list_capacity > 0 && a.list_capacity < BLIST_MAX) ? a.list_capacity : BLIST_MAX;
-    for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi += gridDim.x) {
+    for (uint32_t bi = blockIdx.x; bi < a.n_bricks; bi = brick_fetch(a, H)) {
         const Brick br = a.bricks[bi];
         load_world(a, br.world, H.wc, spair);
         __syncthreads();

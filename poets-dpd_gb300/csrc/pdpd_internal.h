@@ -124,6 +124,8 @@ struct KArgs {
     uint32_t brick_hc_max;  // halo cells of the nominal brick shape
     uint32_t brick_maxb;    // staged-bead capacity of one brick
     uint32_t brick_npair;   // staged pair-table entries: the largest n_types^2 of the worlds
+    uint32_t *brick_next;   // FP32: the brick queue's next free entry beyond the first
+                            // gridDim.x (zeroed by the sort, which precedes every force pass)
 };
 
 // Kernel launchers.  Each returns the number of kernels it launched.

@@ -49,8 +49,10 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *sh)
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *__restrict__ cnt,
                                                                uint32_t n, uint32_t *blocksums,
                                                                WorldDev *worlds, uint32_t n_worlds,
-                                                               int tick)
+                                                               int tick, uint32_t *brick_next)
 {
+    // the next force pass takes its bricks from a fresh queue
+    if (brick_next && blockIdx.x == 0 && threadIdx.x == 0) *brick_next = 0u;
     __shared__ uint32_t sh[32];
     const uint32_t base = blockIdx.x * SCAN_CHUNK + threadIdx.x * SCAN_ITEMS;
     uint32_t s = 0;
@@ -182,7 +184,7 @@ int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t
 {
     const uint32_t nb = scan_blocks(a.n_cells);
     k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(a.cnt, a.n_cells, a.blocksums, a.worlds, a.n_worlds,
-                                              tick);
+                                              tick, a.brick_next);
     k_scan_final<<<nb, SCAN_THREADS, 0, s>>>(a.cnt, a.n_cells, a.blocksums, a.start);
     const int T = 256;
     const uint32_t g = (a.n_beads + T - 1) / T;
