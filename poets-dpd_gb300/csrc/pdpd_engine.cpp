@@ -910,30 +910,34 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // --- stage and upload
     double *hs = (double *)e->h_staging[0].p;
     uint32_t *hh = (uint32_t *)(hs + 9 * nb);
-    for (uint32_t i = 0; i < n_worlds; i++) {
-        const pdpd_world &w = ws[i];
-        uint32_t bb = wdev[i].bead_base;
-        if (keep_old && keep_old[i] >= 0) {  // bead state comes from the old arena (below)
-            parallel_for(w.n_beads, 1 << 18, [&, bb](size_t k0, size_t k1) {
-                memcpy(hh + bb + k0, w.hash + k0, sizeof(uint32_t) * (k1 - k0));
-            });
-            continue;
-        }
-        parallel_for(w.n_beads, 1 << 16, [&, bb](size_t k0, size_t k1) {
-            for (size_t k = k0; k < k1; k++) {
-                const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
-                const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
-                const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
-                double *o = hs + 9 * (size_t)(bb + k);
-                for (int d = 0; d < 3; d++) {
-                    o[d] = x[d];
-                    o[3 + d] = v[d];
-                    o[6 + d] = f[d];
+    // One pass over the whole batch's beads (global slot g of world i = bead_base_i + k),
+    // split across host threads whatever the worlds' sizes.
+    parallel_for(nb, 1 << 16, [&](size_t g0, size_t g1) {
+        uint32_t i = (uint32_t)(std::upper_bound(wdev.begin(), wdev.end(), (uint32_t)g0,
+                                                 [](uint32_t g, const WorldDev &d) { return g < d.bead_base; }) -
+                                wdev.begin()) - 1;
+        for (size_t g = g0; g < g1;) {
+            while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
+            const pdpd_world &w = ws[i];
+            const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, w.n_beads);
+            const bool kept = keep_old && keep_old[i] >= 0;  // bead state from the old arena (below)
+            for (size_t k = g - bb; k < k1; k++) {
+                if (!kept) {
+                    const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
+                    const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
+                    const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
+                    double *o = hs + 9 * (bb + k);
+                    for (int d = 0; d < 3; d++) {
+                        o[d] = x[d];
+                        o[3 + d] = v[d];
+                        o[6 + d] = f[d];
+                    }
                 }
                 hh[bb + k] = w.hash[k];
             }
-        });
-    }
+            g = bb + k1;
+        }
+    });
     cudaStream_t s = e->stream;
     auto H2D = [&](DevBuf &b, const void *src, size_t n) {
         if (ce == cudaSuccess && n) ce = cudaMemcpyAsync(b.p, src, n, cudaMemcpyHostToDevice, s);
