@@ -152,8 +152,8 @@ const ConfigEntry kConfig[] = {
                      "5 = warp per home cell, 6 = as 0 with the neighbour cells walked row by row, "
                      "7 = as 6 with the lists evaluated balanced across lanes, "
                      "8 = as 6 with 512-thread blocks for larger bricks."},
-    {"brick_x", "Brick extent in cells along x (FP32 brick kernel; default by size: 4x8x8, "
-                "3x4x6 from about 400 cells per SM, 2x4x4 below)."},
+    {"brick_x", "Brick extent in cells along x (FP32 brick kernel; default by size: 5x8x8, "
+                "3x4x6 from about 200 cells per SM, 2x4x4 below)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
     {"autotune", "FP32: time the force-kernel variants and brick shapes on the first steps of "
@@ -343,8 +343,8 @@ struct pdpd_engine {
 
     // Default kernel variant and brick shape for the attached batch, where the config does not
     // name them.  The persistent brick kernels want several bricks per SM: the 512-thread row
-    // walk on 4x8x8 bricks is fastest from about 1,300 cells per SM (a 58^3 box on 152 SMs),
-    // the 128-thread row walk on 3x4x6 bricks from about 400, and on 2x4x4 bricks below that.
+    // walk on 5x8x8 bricks is fastest from about 1,300 cells per SM (a 58^3 box on 152 SMs),
+    // the 128-thread row walk on 3x4x6 bricks from about 200, and on 2x4x4 bricks below that.
     // All of them give the same trajectory.
     void default_shape()
     {
@@ -354,9 +354,33 @@ struct pdpd_engine {
         const uint64_t per_sm = cells / (uint64_t)std::max(1, sm_count);
         if (!kernel_user) cfg_force_kernel = per_sm >= 1300 ? 8 : 6;
         if (brick_user) return;
-        static const int big[3] = {4, 8, 8}, mid[3] = {3, 4, 6}, small[3] = {2, 4, 4};
-        const int *b = cfg_force_kernel == 8 || per_sm >= 1300 ? big : (per_sm >= 400 ? mid : small);
+        static const int big[][3] = {{5, 8, 8}, {4, 8, 8}, {4, 6, 8}, {4, 4, 6}, {3, 4, 4}};
+        static const int mid[3] = {3, 4, 6}, small[3] = {2, 4, 4};
+        const int *b = per_sm >= 200 ? mid : small;
+        if (cfg_force_kernel == 8 || per_sm >= 1300) {
+            // the largest brick whose halo (at the batch's highest density) fits the staging
+            // capacity 5 Poisson deviations above its mean, so dense boxes do not overflow it
+            uint32_t npair = 1;
+            for (const WorldHost &wh : worlds) npair = std::max(npair, wh.dev.n_types * wh.dev.n_types);
+            b = big[4];
+            for (const auto &c : big) {
+                const uint32_t hc = (uint32_t)(c[0] + 2) * (c[1] + 2) * (c[2] + 2);
+                const double mean = max_density * hc;
+                if (mean + 5.0 * std::sqrt(mean) <= (double)brick_maxb_limit(8, hc, npair)) {
+                    b = c;
+                    break;
+                }
+            }
+        }
         for (int d = 0; d < 3; d++) cfg_brick[d] = b[d];
+    }
+
+    // Staged beads a brick of hc halo cells should have room for: the mean halo population
+    // of the densest world + 6 standard deviations (Poisson), at least 1.2x the mean, + 32.
+    double staging_want(uint32_t hc) const
+    {
+        const double mean = max_density * hc;
+        return std::max(mean + 6.0 * std::sqrt(mean), 1.2 * mean) + 32;
     }
 
     // Build the brick work queue of the FP32 force kernel for the current brick shape: every
@@ -402,18 +426,16 @@ struct pdpd_engine {
         if (ce != cudaSuccess) return cuda_fail(ce, "brick table upload");
         a.bricks = d_bricks.as<Brick>();
         a.n_bricks = (uint32_t)bricks.size();
-        // Staged-bead capacity: 1.5x the expected halo population of the densest world (at
-        // most 2047, the list entries' 11-bit index); denser bricks take the fallback path.
         a.brick_hc_max = (uint32_t)(cfg_brick[0] + 2) * (cfg_brick[1] + 2) * (cfg_brick[2] + 2);
-        // staged-bead capacity: the mean halo population + 6 standard deviations (Poisson) and
-        // a floor of 1.2x the mean; a fuller brick takes the (bit-identical) global path
-        const double mean = max_density * a.brick_hc_max;
-        double want = std::max(mean + 6.0 * std::sqrt(mean), 1.2 * mean) + 32;
-        a.brick_maxb = (uint32_t)std::min(2047.0, std::max(64.0, want));
-        int grid = 0;
-        uint32_t bytes = 0;
         a.brick_npair = 1;
         for (const WorldHost &wh : worlds) a.brick_npair = std::max(a.brick_npair, wh.dev.n_types * wh.dev.n_types);
+        // staged-bead capacity (staging_want) within the variant's limit; a fuller brick takes
+        // the (bit-identical) global path
+        const double want = staging_want(a.brick_hc_max);
+        const double limit = (double)brick_maxb_limit(a.force_kernel, a.brick_hc_max, a.brick_npair);
+        a.brick_maxb = (uint32_t)std::min(limit, std::max(64.0, want));
+        int grid = 0;
+        uint32_t bytes = 0;
         int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, a.brick_npair, &grid, &bytes);
         if (rc)
             return fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
@@ -430,8 +452,8 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
-        static const int cand[][4] = {{8, 4, 8, 8}, {8, 6, 8, 6}, {8, 4, 6, 10}, {8, 4, 7, 10},
-                                      {6, 3, 4, 6}, {6, 3, 3, 8}, {6, 4, 4, 6}, {1, 4, 4, 4}};
+        static const int cand[][4] = {{8, 5, 8, 8}, {8, 4, 10, 8}, {8, 4, 8, 10}, {8, 4, 8, 8},
+                                      {8, 6, 8, 6}, {6, 3, 4, 6}, {6, 4, 4, 6}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
         const uint32_t trial = 3;
         if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;

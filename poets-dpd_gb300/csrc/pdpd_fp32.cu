@@ -591,6 +591,22 @@ int launch_begin32(const KArgs &a, cudaStream_t s)
 
 // Set up the brick kernel for a brick shape: opt in to the shared memory it needs and
 // return its persistent grid (resident blocks x SMs) and dynamic shared-memory bytes.
+uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair)
+{
+    // Variants 0 and 3 keep the neighbour direction in 5 of a list entry's 16 bits (11-bit
+    // staged index); 6 and 7 stay within the same bound, which their bricks do not reach.
+    if (variant != 8) return 2047u;
+    // Variant 8: the entry is the staged index alone; the capacity is what leaves room for
+    // two 512-thread blocks per SM.
+    int dev = 0, smem_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+        return 2047u;
+    const BrickLayout L = brick_layout(hc_max, 0, npair, 1, 0, BRICK_THREADS_WIDE);
+    const int budget = smem_sm / 2 - 1024 - (int)L.bytes - 64;
+    return (uint32_t)std::max(64, std::min(65535, budget / 32));
+}
+
 int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
                 uint32_t *smem_bytes)
 {

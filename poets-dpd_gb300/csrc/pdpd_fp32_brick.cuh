@@ -145,6 +145,56 @@ __device__ __forceinline__ void brick_list_eval(const float4 *__restrict__ spos,
     brick_list_eval_col<T>(spos, svel, list, threadIdx.x, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
+// Halo cell of a staged bead, kept by the staging in the w of its staged velocity:
+// hx | hy << 8 | hz << 16 (brick-local halo coordinates; a halo side is at most 34 cells).
+__device__ __forceinline__ uint32_t staged_cell(const float4 v)
+{
+    return __float_as_uint(v.w);
+}
+
+// Evaluate list entries [0, n) of column `col` in order, adding to F, for the row walk's
+// lists (variants 6-8): an entry is the staged index alone, and the neighbour direction is
+// the difference of the two beads' staged halo cells (vi is the home bead's staged velocity).
+// The direction's values and so every operation are those of brick_list_eval_col.
+template <int T = BRICK_THREADS>
+__device__ __forceinline__ void brick_rows_eval_col(const float4 *__restrict__ spos,
+                                                    const float4 *__restrict__ svel,
+                                                    const uint16_t *__restrict__ list, int col, int n,
+                                                    const float4 pi, const float4 vi,
+                                                    const float2 *pair, uint32_t nt, uint32_t th_lo,
+                                                    uint32_t th_hi, float scale, float F[3])
+{
+    const uint32_t hi = __float_as_uint(pi.w);
+    const uint32_t ti = min(hi >> 28, nt - 1u);
+    const uint32_t hc = staged_cell(vi);
+    const int hx = (int)(hc & 255u), hy = (int)((hc >> 8) & 255u), hz = (int)(hc >> 16);
+    for (int k = 0; k < n; k++) {
+        const uint32_t j = list[k * T + col];
+        const float4 pj = spos[j];
+        const float4 vj = svel[j];
+        const uint32_t cj = staged_cell(vj);
+        const float ax = __fsub_rn(pi.x, (float)((int)(cj & 255u) - hx));
+        const float ay = __fsub_rn(pi.y, (float)((int)((cj >> 8) & 255u) - hy));
+        const float az = __fsub_rn(pi.z, (float)((int)(cj >> 16) - hz));
+        float dx, dy, dz;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+        const uint32_t hj = __float_as_uint(pj.w);
+        pair_accumulate(dx, dy, dz, r2, vi, vj, hi, hj, pair[ti * nt + min(hj >> 28, nt - 1u)],
+                        th_lo, th_hi, scale, F);
+    }
+}
+
+template <int T = BRICK_THREADS>
+__device__ __forceinline__ void brick_rows_eval(const float4 *__restrict__ spos,
+                                                const float4 *__restrict__ svel,
+                                                const uint16_t *__restrict__ list, int n,
+                                                const float4 pi, const float4 vi,
+                                                const float2 *pair, uint32_t nt, uint32_t th_lo,
+                                                uint32_t th_hi, float scale, float F[3])
+{
+    brick_rows_eval_col<T>(spos, svel, list, threadIdx.x, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+}
+
 // Pair forces of one staged home bead, with the 27 neighbour cells walked as one flat
 // sequence: the 9 neighbour rows (dx, dy) in order, each row's 3 cells (dz = -1, 0, +1) being
 // one contiguous range of staged beads.  Each thread's loop then runs for its own total
@@ -302,17 +352,15 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
             const int hc0 = row * HZ;
             const uint32_t base = hstart[hc0];
             const uint32_t len = hstart[hc0 + HZ] - base;
+            const uint32_t rowcell = (uint32_t)(row / HY) | ((uint32_t)(row - (row / HY) * HY) << 8);
+            int z = 0;  // the lane's halo z cell: k only grows, so z only moves up
             for (uint32_t k = lane; k < len; k += 32) {
-                uint32_t slot;
-                if (zrun) {
-                    slot = hslot[hc0] + k;
-                } else {
-                    int z = 0;
-                    while (hstart[hc0 + z + 1] - base <= k) z++;
-                    slot = hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
-                }
+                while (hstart[hc0 + z + 1] - base <= k) z++;
+                const uint32_t slot = zrun ? hslot[hc0] + k : hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
                 spos[base + k] = ((const float4 *)a.posA)[slot];
-                svel[base + k] = ((const float4 *)a.velA)[slot];
+                float4 v = ((const float4 *)a.velA)[slot];
+                v.w = __uint_as_float(rowcell | ((uint32_t)z << 16));  // staged_cell
+                svel[base + k] = v;
             }
         }
     }
@@ -360,9 +408,8 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
         const uint32_t j0 = gxy + gzm * gzm >= PRUNE ? c1 : (gxy + gzm2 * gzm2 >= PRUNE ? c0 + hlo[rowc - 1] : c0);
         const uint32_t j1 = gxy + gzp * gzp >= PRUNE ? c2 : (gxy + gzp2 * gzp2 >= PRUNE ? c2 + hlo[rowc + 1] : c3);
         const float ax = __fsub_rn(pi.x, (float)ddx), ay = __fsub_rn(pi.y, (float)ddy);
-        const uint32_t dbase = (uint32_t)(rr * 3) << 11;
         if (n + (int)(j1 - j0) > cap) {  // room for the whole row, or evaluate the list first
-            brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+            brick_rows_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
             n = 0;
         }
         if ((int)(j1 - j0) <= cap) {
@@ -372,8 +419,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-                list[n * T + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                list[n * T + threadIdx.x] = (uint16_t)j;
                 n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
             }
         } else {
@@ -382,11 +428,10 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 const float az = j < c1 ? azm : (j < c2 ? pi.z : azp);
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-                const uint32_t dz3 = j < c1 ? 0u : (j < c2 ? 1u : 2u);
-                list[n * T + threadIdx.x] = (uint16_t)(j | (dbase + (dz3 << 11)));
+                list[n * T + threadIdx.x] = (uint16_t)j;
                 n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
                 if (n == cap) {
-                    brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
+                    brick_rows_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
                     n = 0;
                 }
             }
@@ -414,7 +459,7 @@ __device__ __forceinline__ void brick_fallback_bead(const KArgs &a, const WorldD
 }
 
 template <int FINAL, int LIST, int FLAT, int T = BRICK_THREADS>
-__global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
+__global__ void __launch_bounds__(T, T == BRICK_THREADS_WIDE ? 2 : 6) k_force32_brick(KArgs a, BrickLayout lay)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BrickHeader &H = *reinterpret_cast<BrickHeader *>(smem_raw);
@@ -507,7 +552,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
                     if (no > 0) {
                         const uint32_t so = B.si[o];
                         float G[3] = {B.f[0][o], B.f[1][o], B.f[2][o]};
-                        brick_list_eval_col(spos, svel, list, (int)o, no, spos[so], svel[so], spair, nt,
+                        brick_rows_eval_col(spos, svel, list, (int)o, no, spos[so], svel[so], spair, nt,
                                             th_lo, th_hi, scale, G);
                         B.f[0][o] = G[0];
                         B.f[1][o] = G[1];
@@ -551,7 +596,7 @@ __global__ void __launch_bounds__(T) k_force32_brick(KArgs a, BrickLayout lay)
             if (FLAT >= 2) {  // variant 6 (and 7 when not staged, never reached)
                 const int nl = brick_rows_collect<T>(spos, svel, list, cap, hstart, hlo, HY, HZ, hx, hy, hz, pi,
                                                   vi, spair, nt, th_lo, th_hi, scale, F);
-                brick_list_eval<T>(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
+                brick_rows_eval<T>(spos, svel, list, nl, pi, vi, spair, nt, th_lo, th_hi, scale, F);
                 const int c[3] = {br.x0 + lx, br.y0 + ly, br.z0 + z};
                 integrate32<FINAL>(a, w, s, c, pi, vi, F, err);
                 continue;

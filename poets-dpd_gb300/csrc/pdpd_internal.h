@@ -153,6 +153,9 @@ int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uin
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
 
 size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
+// Largest staged-bead capacity of a brick for force variant `variant` (the list entries'
+// index range, and for variant 8 two blocks per SM of shared memory).
+uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair);
 int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
                 uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
