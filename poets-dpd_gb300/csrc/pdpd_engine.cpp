@@ -196,7 +196,7 @@ struct pdpd_engine {
     DevBuf d_worlds, d_tiles, d_bricks, d_start, d_cnt, d_blocksums;
     DevBuf d_posA, d_velA, d_frc, d_posB, d_velB, d_frcB;
     DevBuf d_ids, d_cellg, d_slot_of_id, d_keyrank, d_tmp;
-    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo, d_brick_next;
+    DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo, d_brick_next, d_hash_old;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
     HostPinned h_err;
@@ -250,7 +250,7 @@ struct pdpd_engine {
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
-                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next};
+                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next, &d_hash_old};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -709,6 +709,12 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         if (rc) return rc;
         snap = e->d_staging[1].as<double>();
         for (const WorldHost &wh : e->worlds) old_base.push_back(wh.dev.bead_base);
+        // the kept worlds' hashes too stay on the device (the new layout reuses d_hash)
+        if (e->d_hash_old.alloc(sizeof(uint32_t) * std::max<size_t>(1, e->n_beads)) != cudaSuccess)
+            return e->fail(PDPD_E_NOMEM, "device allocation failed");
+        cudaError_t hce = cudaMemcpyAsync(e->d_hash_old.p, e->d_hash.p, sizeof(uint32_t) * e->n_beads,
+                                          cudaMemcpyDeviceToDevice, e->stream);
+        if (hce != cudaSuccess) return e->cuda_fail(hce, "re-pack hash copy");
     }
     e->reset();
     char reason[256];
@@ -942,18 +948,16 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
             const pdpd_world &w = ws[i];
             const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, w.n_beads);
-            const bool kept = keep_old && keep_old[i] >= 0;  // bead state from the old arena (below)
-            for (size_t k = g - bb; k < k1; k++) {
-                if (!kept) {
-                    const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
-                    const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
-                    const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
-                    double *o = hs + 9 * (bb + k);
-                    for (int d = 0; d < 3; d++) {
-                        o[d] = x[d];
-                        o[3 + d] = v[d];
-                        o[6 + d] = f[d];
-                    }
+            const bool kept = keep_old && keep_old[i] >= 0;  // state and hashes from the old arena (below)
+            for (size_t k = g - bb; k < k1 && !kept; k++) {
+                const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
+                const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
+                const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
+                double *o = hs + 9 * (bb + k);
+                for (int d = 0; d < 3; d++) {
+                    o[d] = x[d];
+                    o[3 + d] = v[d];
+                    o[6 + d] = f[d];
                 }
                 hh[bb + k] = w.hash[k];
             }
@@ -995,7 +999,19 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
                              snap + 9 * (size_t)old_base[keep_old[i]],
                              sizeof(double) * 9 * ws[i].n_beads, cudaMemcpyDeviceToDevice, s);
     }
-    H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
+    if (!any_kept) {
+        H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
+    } else {
+        for (uint32_t i = 0; i < n_worlds && ce == cudaSuccess; i++) {
+            if (ws[i].n_beads == 0) continue;
+            uint32_t *dst = e->d_hash.as<uint32_t>() + wdev[i].bead_base;
+            const size_t n = sizeof(uint32_t) * ws[i].n_beads;
+            ce = keep_old[i] < 0
+                     ? cudaMemcpyAsync(dst, hh + wdev[i].bead_base, n, cudaMemcpyHostToDevice, s)
+                     : cudaMemcpyAsync(dst, e->d_hash_old.as<uint32_t>() + old_base[keep_old[i]], n,
+                                       cudaMemcpyDeviceToDevice, s);
+        }
+    }
     H2D(e->d_bonded, bonded.data(), sizeof(uint32_t) * bonded.size());
     if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_cnt.p, 0, sizeof(uint32_t) * nc, s);
     uint32_t total = (uint32_t)nb;  // start[n_cells] = total beads, fixed for the attach
