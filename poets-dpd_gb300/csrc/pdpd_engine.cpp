@@ -838,43 +838,50 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         parallel_for(nb, 1 << 18, [&](size_t i0, size_t i1) {
             memcpy(fill.data() + i0, row.data() + i0, sizeof(uint32_t) * (i1 - i0));
         });
-    std::vector<double> bp64;
-    std::vector<float> bp32;
-    uint32_t pidx = 0;
+    // Parameters: every world's Hookean bonds in order, then every world's angle bonds.  The
+    // worlds' terms fill disjoint CSR rows, so the worlds are filled in parallel.
+    std::vector<uint32_t> bond_off(n_worlds + 1, 0), angle_off(n_worlds + 1, 0);
     for (uint32_t i = 0; i < n_worlds; i++) {
-        const pdpd_world &w = ws[i];
-        uint32_t bb = wdev[i].bead_base;
-        for (uint32_t k = 0; k < w.n_bonds; k++, pidx++) {
-            uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
-            terms[fill[h]++] = {0u | (0u << 8), t, t, pidx};
-            terms[fill[t]++] = {0u | (1u << 8), h, h, pidx};
-            double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
-            for (double v : p) {
-                bp64.push_back(v);
-                bp32.push_back((float)v);
-            }
-        }
+        bond_off[i + 1] = bond_off[i] + ws[i].n_bonds;
+        angle_off[i + 1] = angle_off[i] + ws[i].n_angles;
     }
-    for (uint32_t i = 0; i < n_worlds; i++) {
-        const pdpd_world &w = ws[i];
-        uint32_t bb = wdev[i].bead_base;
-        for (uint32_t k = 0; k < w.n_angles; k++, pidx++) {
-            uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
-                     t = bb + w.angle_beads[3 * k + 2];
-            terms[fill[h]++] = {1u | (0u << 8), m, t, pidx};
-            terms[fill[m]++] = {1u | (1u << 8), h, t, pidx};
-            terms[fill[t]++] = {1u | (2u << 8), h, m, pidx};
-            double th = w.angle_theta0[k];
-            double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
-            for (double v : p) {
-                bp64.push_back(v);
-                bp32.push_back((float)v);
-            }
+    const uint32_t n_bond_par = bond_off[n_worlds];
+    std::vector<double> bp64(f64 ? 4 * (size_t)n_bparams : 0);
+    std::vector<float> bp32(f64 ? 0 : 4 * (size_t)n_bparams);
+    auto put = [&](uint32_t pidx, const double p[4]) {
+        for (int q = 0; q < 4; q++) {
+            if (f64) bp64[4 * (size_t)pidx + q] = p[q];
+            else bp32[4 * (size_t)pidx + q] = (float)p[q];
         }
-    }
-    // The per-bead order must be: this bead's Hookean terms in flat order, then its angle
-    // terms in flat order.  Filling all Hookean bonds of all worlds before any angle bond
-    // gives exactly that.
+    };
+    if (n_terms)
+        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; i++) {
+                const pdpd_world &w = ws[i];
+                const uint32_t bb = wdev[i].bead_base;
+                for (uint32_t k = 0; k < w.n_bonds; k++) {
+                    const uint32_t pidx = bond_off[i] + k;
+                    uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
+                    terms[fill[h]++] = {0u | (0u << 8), t, t, pidx};
+                    terms[fill[t]++] = {0u | (1u << 8), h, h, pidx};
+                    const double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
+                    put(pidx, p);
+                }
+                for (uint32_t k = 0; k < w.n_angles; k++) {
+                    const uint32_t pidx = n_bond_par + angle_off[i] + k;
+                    uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
+                             t = bb + w.angle_beads[3 * k + 2];
+                    terms[fill[h]++] = {1u | (0u << 8), m, t, pidx};
+                    terms[fill[m]++] = {1u | (1u << 8), h, t, pidx};
+                    terms[fill[t]++] = {1u | (2u << 8), h, m, pidx};
+                    const double th = w.angle_theta0[k];
+                    const double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
+                    put(pidx, p);
+                }
+            }
+        });
+    // The per-bead order is this bead's Hookean terms in flat order, then its angle terms in
+    // flat order: each bead belongs to one world, whose bonds are filled before its angles.
 
     // --- allocate
     const size_t P = payload_bytes(f64);
@@ -906,17 +913,28 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
     A(e->d_cellpair, std::max<size_t>(16, f64 ? sizeof(double) * cp64.size() : sizeof(float) * cp32.size()));
     A(e->d_hash, sizeof(uint32_t) * nb);
-    // Polymer beads (monomer bit of the hash clear), for the bond kernels.
+    // Polymer beads (monomer bit of the hash clear), for the bond kernels: one pass over the
+    // whole batch in chunks of global slots, concatenated in slot order.
     std::vector<uint32_t> bonded;
-    for (uint32_t i = 0; i < n_worlds; i++) {
-        const uint32_t n = ws[i].n_beads, bb = wdev[i].bead_base;
-        const size_t chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
-        const size_t per = (n + chunks - 1) / chunks;
+    {
+        const size_t chunks = std::min<size_t>(256, std::max<size_t>(1, nb >> 16));
+        const size_t per = (nb + chunks - 1) / chunks;
         std::vector<std::vector<uint32_t>> part(chunks);
         parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
-            for (size_t c = c0; c < c1; c++)
-                for (size_t k = c * per; k < std::min<size_t>(n, (c + 1) * per); k++)
-                    if (!(ws[i].hash[k] & (1u << 27))) part[c].push_back(bb + (uint32_t)k);
+            for (size_t c = c0; c < c1; c++) {
+                const size_t g0 = c * per, g1 = std::min<size_t>(nb, g0 + per);
+                if (g0 >= g1) continue;
+                uint32_t i = (uint32_t)(std::upper_bound(wdev.begin(), wdev.end(), (uint32_t)g0,
+                                                         [](uint32_t g, const WorldDev &d) { return g < d.bead_base; }) -
+                                        wdev.begin()) - 1;
+                for (size_t g = g0; g < g1;) {
+                    while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
+                    const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, ws[i].n_beads);
+                    for (size_t k = g - bb; k < k1; k++)
+                        if (!(ws[i].hash[k] & (1u << 27))) part[c].push_back((uint32_t)(bb + k));
+                    g = bb + k1;
+                }
+            }
         });
         for (const auto &p : part) bonded.insert(bonded.end(), p.begin(), p.end());
     }
