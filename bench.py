@@ -621,7 +621,7 @@ def run_engine_arm(args):
     print(json.dumps(line), flush=True)
 
 
-METRIC = "bead-steps/s (FP32 batched vs plain FP64); served p50/p99 job latency"
+METRIC = "bead-steps/s on 1 GB300 (FP32 batched vs plain FP64); served p50/p99 job latency"
 
 
 def main():
