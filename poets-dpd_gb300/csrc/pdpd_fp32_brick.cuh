@@ -265,6 +265,19 @@ __device__ __forceinline__ void brick_gather_flat(const float4 *__restrict__ spo
     if (LIST) brick_list_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
 }
 
+// 16-byte asynchronous global-to-shared copy (cp.async, no register round trip) and the wait
+// for all of this thread's copies.  Both addresses are 16-byte aligned (float4 arrays).
+__device__ __forceinline__ void cp_async16(float4 *dst_shared, const float4 *src_global)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst_shared);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src_global) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Halo setup and staging of one brick, block-wide (ends with __syncthreads):
 //   hstart[hc] = first staged index of halo cell hc (hc = (hx * HY + hy) * HZ + hz, z fastest),
 //   hstart[HC] = total, hslot[hc] = its first slot in the sorted state,
@@ -334,20 +347,39 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
     }
     if (tid == 0) hstart[HC] = tot;
     __syncthreads();
-    if (tid == 0) {
-        uint32_t acc = 0;
-        for (int r = 0; r < br.bx * br.by; r++) {
-            H.home_rows[r] = acc;
-            const int lx = r / br.by, ly = r - lx * br.by;
-            const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
-            acc += hstart[hc0 + br.bz] - hstart[hc0];
+    if (warp == 0) {  // home rows (at most 64): counts, then a warp prefix sum
+        const int nr = br.bx * br.by;
+        uint32_t c[2] = {0u, 0u};
+        for (int q = 0; q < 2; q++) {
+            const int r = lane + 32 * q;
+            if (r < nr) {
+                const int lx = r / br.by, ly = r - lx * br.by;
+                const int hc0 = ((lx + 1) * HY + (ly + 1)) * HZ + 1;
+                c[q] = hstart[hc0 + br.bz] - hstart[hc0];
+            }
         }
-        H.home_rows[br.bx * br.by] = acc;
+        uint32_t i0 = c[0], i1 = c[1];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y0 = __shfl_up_sync(0xffffffffu, i0, off);
+            const uint32_t y1 = __shfl_up_sync(0xffffffffu, i1, off);
+            if (lane >= off) {
+                i0 += y0;
+                i1 += y1;
+            }
+        }
+        const uint32_t tot0 = __shfl_sync(0xffffffffu, i0, 31);
+        if (lane < nr) H.home_rows[lane] = i0 - c[0];
+        if (lane + 32 < nr) H.home_rows[lane + 32] = tot0 + i1 - c[1];
+        if (lane == 31) H.home_rows[nr] = tot0 + i1;  // nr <= 64: lane 31 holds both totals
     }
     // staging, one (x, y) halo row per warp iteration (coalesced); a row whose z range does not
-    // wrap is one contiguous run of slots
+    // wrap is one contiguous run of slots.  Positions go by asynchronous 16-byte copies (no
+    // register round trip); velocities through registers, to record the bead's halo cell in
+    // the spare w (staged_cell).
     if (tot <= maxb) {
         const bool zrun = br.z0 >= 1 && br.z0 + br.bz + 1 <= L2;
+        const float4 *pos = (const float4 *)a.posA, *vel = (const float4 *)a.velA;
         for (int row = warp; row < HX * HY; row += T / 32) {
             const int hc0 = row * HZ;
             const uint32_t base = hstart[hc0];
@@ -357,12 +389,13 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
             for (uint32_t k = lane; k < len; k += 32) {
                 while (hstart[hc0 + z + 1] - base <= k) z++;
                 const uint32_t slot = zrun ? hslot[hc0] + k : hslot[hc0 + z] + (k - (hstart[hc0 + z] - base));
-                spos[base + k] = ((const float4 *)a.posA)[slot];
-                float4 v = ((const float4 *)a.velA)[slot];
+                cp_async16(spos + base + k, pos + slot);
+                float4 v = vel[slot];
                 v.w = __uint_as_float(rowcell | ((uint32_t)z << 16));  // staged_cell
                 svel[base + k] = v;
             }
         }
+        cp_async_wait_all();
     }
     __syncthreads();
     total = tot;
