@@ -119,36 +119,37 @@ class World:
         """
         bonds = {"beads": [], "kappa": [], "r0": [], "poly": []}
         angles = {"beads": [], "kappa": [], "theta0": [], "poly": []}
+        single = len(self.polymer_types) == 1
         for pt_index, pt in enumerate(self.polymer_types):
-            sel = np.nonzero(self.poly_type == pt_index)[0]
+            sel = (np.arange(self.poly_type.shape[0]) if single
+                   else np.nonzero(self.poly_type == pt_index)[0])
             if sel.size == 0:
                 continue
             starts = self.poly_start[sel].astype(np.int64)
             if pt.bonds:
-                heads = np.array([b[0] for b in pt.bonds], dtype=np.int64)
-                tails = np.array([b[1] for b in pt.bonds], dtype=np.int64)
-                hb = self.poly_beads[starts[:, None] + heads[None, :]]
-                tb = self.poly_beads[starts[:, None] + tails[None, :]]
-                bonds["beads"].append(np.stack([hb, tb], axis=-1).reshape(-1, 2))
+                ht = np.array([[b[0], b[1]] for b in pt.bonds], dtype=np.int64)  # (bonds, 2)
+                bonds["beads"].append(self.poly_beads[starts[:, None, None] + ht[None, :, :]].reshape(-1, 2))
                 bonds["kappa"].append(np.tile(np.array([b[2] for b in pt.bonds], float), sel.size))
                 bonds["r0"].append(np.tile(np.array([b[3] for b in pt.bonds], float), sel.size))
-                bonds["poly"].append(np.repeat(sel, len(pt.bonds)))
+                if not single:
+                    bonds["poly"].append(np.repeat(sel, len(pt.bonds)))
             if pt.bond_pairs:
-                offs = [np.array([pt.bonds[p[0]][0] for p in pt.bond_pairs], dtype=np.int64),
-                        np.array([pt.bonds[p[0]][1] for p in pt.bond_pairs], dtype=np.int64),
-                        np.array([pt.bonds[p[1]][1] for p in pt.bond_pairs], dtype=np.int64)]
-                trip = np.stack([self.poly_beads[starts[:, None] + o[None, :]] for o in offs],
-                                axis=-1)
-                angles["beads"].append(trip.reshape(-1, 3))
+                hmt = np.array([[pt.bonds[q[0]][0], pt.bonds[q[0]][1], pt.bonds[q[1]][1]]
+                                for q in pt.bond_pairs], dtype=np.int64)  # (pairs, 3)
+                angles["beads"].append(self.poly_beads[starts[:, None, None] + hmt[None, :, :]].reshape(-1, 3))
                 angles["kappa"].append(
-                    np.tile(np.array([p[2] for p in pt.bond_pairs], float), sel.size))
+                    np.tile(np.array([q[2] for q in pt.bond_pairs], float), sel.size))
                 angles["theta0"].append(
-                    np.tile(np.array([p[3] for p in pt.bond_pairs], float), sel.size))
-                angles["poly"].append(np.repeat(sel, len(pt.bond_pairs)))
+                    np.tile(np.array([q[3] for q in pt.bond_pairs], float), sel.size))
+                if not single:
+                    angles["poly"].append(np.repeat(sel, len(pt.bond_pairs)))
 
         def finish(d, width, keys):
             if not d["beads"]:
                 return [np.zeros((0, width), np.uint32)] + [np.zeros(0) for _ in keys]
+            if len(d["beads"]) == 1:  # one polymer type: already in polymer id order
+                return ([np.ascontiguousarray(d["beads"][0], dtype=np.uint32)] +
+                        [np.ascontiguousarray(d[k][0], dtype=np.float64) for k in keys])
             order = np.argsort(np.concatenate(d["poly"]), kind="stable")
             out = [np.concatenate(d["beads"]).astype(np.uint32)[order]]
             out += [np.concatenate(d[k]).astype(np.float64)[order] for k in keys]
