@@ -129,6 +129,17 @@ void *pdpd_stream(pdpd_engine *e);
 int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
                     size_t bead_stride_bytes, int64_t *t);
 
+/* Every world of an attached batch at once (after Run(nSteps) of a batch, DPDEngine::Run's
+ * write-back of dpd_engine.hpp:179-184 for each state): one device unsort, one copy and a
+ * parallel host scatter instead of one round trip per world.  out[i] receives world i's
+ * state as pdpd_read_state would (any of its pointers may be NULL). */
+typedef struct pdpd_state_view {
+    double *x, *v, *f;
+    int64_t *t;
+} pdpd_state_view;
+int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *out,
+                     size_t bead_stride_bytes);
+
 /* DPDEngine::Run(interval_count, interval_size, callback) (dpd_engine.hpp:195-215) for a
  * single attached world: after each interval the state is written to x/v/f (layout as in
  * pdpd_world) and cb is called; the next interval already runs on the device meanwhile.

@@ -1223,6 +1223,47 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     return PDPD_OK;
 }
 
+int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *out,
+                     size_t stride)
+{
+    if (!e || (!out && n_worlds)) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (n_worlds != e->worlds.size())
+        return e->fail(PDPD_E_INVALID, "%u views for a batch of %zu worlds", n_worlds, e->worlds.size());
+    cudaSetDevice(e->device);
+    int rc = download(e, 0, e->stream);
+    if (rc) return rc;
+    const size_t nbytes = sizeof(double) * 9 * (size_t)e->n_beads;
+    if (e->h_staging[0].alloc(nbytes) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    if (nbytes) {
+        cudaError_t ce = cudaMemcpyAsync(e->h_staging[0].p, e->d_staging[0].p, nbytes, cudaMemcpyDeviceToHost,
+                                         e->stream);
+        if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
+    }
+    rc = e->check_device_errors();  // synchronises
+    if (rc) return rc;
+    // one pass over the batch's beads, split across host threads whatever the worlds' sizes
+    const size_t sb = stride ? stride : 3 * sizeof(double);
+    const double *src = (const double *)e->h_staging[0].p;
+    std::vector<uint32_t> base(n_worlds + 1);
+    for (uint32_t i = 0; i < n_worlds; i++) base[i] = e->worlds[i].dev.bead_base;
+    base[n_worlds] = e->n_beads;
+    parallel_for(e->n_beads, 1 << 16, [&](size_t g0, size_t g1) {
+        uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
+        for (size_t g = g0; g < g1; g++) {
+            while (g >= base[i + 1]) i++;
+            const size_t k = g - base[i];
+            const double *r = src + 9 * g;
+            if (out[i].x) memcpy((char *)out[i].x + sb * k, r, 3 * sizeof(double));
+            if (out[i].v) memcpy((char *)out[i].v + sb * k, r + 3, 3 * sizeof(double));
+            if (out[i].f) memcpy((char *)out[i].f + sb * k, r + 6, 3 * sizeof(double));
+        }
+    });
+    for (uint32_t i = 0; i < n_worlds; i++)
+        if (out[i].t) *out[i].t = e->worlds[i].dev.t;
+    return PDPD_OK;
+}
+
 int pdpd_run_intervals(pdpd_engine *e, int32_t interval_count, uint32_t interval_size, double *x,
                        double *v, double *f, size_t stride, pdpd_interval_fn cb, void *user,
                        uint32_t *steps_done)

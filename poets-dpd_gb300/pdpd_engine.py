@@ -35,7 +35,7 @@ STATUS = {0: "PDPD_OK", 1: "PDPD_E_INVALID", 2: "PDPD_E_UNSUPPORTED", 3: "PDPD_E
 # Every symbol include/pdpd_gpu.h declares.
 EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support",
             "pdpd_max_bond_length", "pdpd_attach", "pdpd_attach_batch", "pdpd_run",
-            "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state",
+            "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state", "pdpd_read_states",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
             "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc",
             "pdpd_observe", "pdpd_v2binary_prepare", "pdpd_v2binary_encode",
@@ -55,6 +55,10 @@ class PdpdWorld(C.Structure):
         ("angle_beads", C.c_void_p), ("angle_kappa", C.c_void_p), ("angle_theta0", C.c_void_p),
         ("cell_conservative", C.c_void_p), ("cell_dissipative", C.c_void_p),
     ]
+
+
+class PdpdStateView(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("v", C.c_void_p), ("f", C.c_void_p), ("t", C.c_void_p)]
 
 
 class PdpdTimings(C.Structure):
@@ -110,6 +114,7 @@ def lib():
         "pdpd_sync": (i32, [vp]),
         "pdpd_stream": (vp, [vp]),
         "pdpd_read_state": (i32, [vp, u32, vp, vp, vp, C.c_size_t, C.POINTER(C.c_int64)]),
+        "pdpd_read_states": (i32, [vp, u32, C.POINTER(PdpdStateView), C.c_size_t]),
         "pdpd_run_intervals": (i32, [vp, C.c_int32, u32, vp, vp, vp, C.c_size_t, INTERVAL_FN, vp,
                                      C.POINTER(u32)]),
         "pdpd_get_timings": (i32, [vp, C.POINTER(PdpdTimings)]),
@@ -273,8 +278,10 @@ class GB300DPDEngine:
     def Run(self, *args):
         if len(args) == 1:
             self._check(lib().pdpd_run(self._h, int(args[0])), "Run")
-            for i, w in enumerate(self._worlds):
-                self.read_state(i, into=w)
+            if len(self._worlds) == 1:
+                self.read_state(0, into=self._worlds[0])
+            elif self._worlds:
+                self.read_states(into=self._worlds)
             return None
         count, size, cb = args
         return self._run_intervals(int(count), int(size), cb)
@@ -392,6 +399,24 @@ class GB300DPDEngine:
                                                buf.size), "v2binary_decode")
         if self._worlds:
             self.read_state(world_index, into=self._worlds[world_index])
+
+    def read_states(self, into=None):
+        """Every attached world's x, v, f, t at once (one device unsort and copy); returns a
+        list of (x, v, f, t), and writes them into the given Worlds when ``into`` is given."""
+        n = len(self._worlds)
+        arrs = [(np.empty((w.n_beads, 3)), np.empty((w.n_beads, 3)), np.empty((w.n_beads, 3)))
+                for w in self._worlds]
+        ts = (C.c_int64 * max(1, n))()
+        views = (PdpdStateView * max(1, n))()
+        for i, (x, v, f) in enumerate(arrs):
+            views[i].x, views[i].v, views[i].f = _p(x), _p(v), _p(f)
+            views[i].t = C.addressof(ts) + 8 * i
+        self._check(lib().pdpd_read_states(self._h, n, views, 24), "read_states")
+        out = [(x, v, f, int(ts[i])) for i, (x, v, f) in enumerate(arrs)]
+        if into is not None:
+            for w, (x, v, f, t) in zip(into, out):
+                w.x, w.v, w.f, w.t = x, v, f, t
+        return out
 
     def read_state(self, world_index=0, into=None):
         """Copy world ``world_index``'s x, v, f, t to numpy (into a World when given)."""

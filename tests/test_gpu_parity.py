@@ -203,12 +203,14 @@ def test_batch_equals_alone(prec):
     batch = [w.copy() for w in worlds]
     eng = E.GB300DPDEngine(prec)
     eng.AttachBatch(batch)
-    eng.Run(20)
-    for a, b in zip(alone, batch):
+    eng.Run(20)  # reads every world back with pdpd_read_states
+    for i, (a, b) in enumerate(zip(alone, batch)):
         assert a.t == b.t
         assert np.array_equal(a.x, b.x)
         assert np.array_equal(a.v, b.v)
         assert np.array_equal(a.f, b.f)
+        x, v, f, t = eng.read_state(i)  # the per-world read gives the same state
+        assert t == b.t and np.array_equal(x, b.x) and np.array_equal(v, b.v) and np.array_equal(f, b.f)
 
 
 LAUNCH_CONFIGS = {
