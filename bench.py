@@ -294,6 +294,7 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "repacks": st["repacks"] - st0["repacks"],
             "repack_s": st["repack_s"] - st0["repack_s"],
             "wasted_bead_steps": st["wasted_bead_steps"] - st0["wasted_bead_steps"],
+            "step_s": st["step_s"] - st0["step_s"],
             "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,

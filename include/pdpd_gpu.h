@@ -300,6 +300,9 @@ typedef struct pdpd_server_stats {
     double repack_s;       /* host wall time spent in re-packs */
     uint64_t wasted_bead_steps;  /* steps of ended jobs' worlds kept in the batch until the
                                     next re-pack (not counted in bead_steps) */
+    double step_s;         /* device time of the epochs' steps (CUDA events on the engine's
+                              stream); wall_s minus it is time the GPU spent on re-packs,
+                              snapshots or waiting for the host */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.

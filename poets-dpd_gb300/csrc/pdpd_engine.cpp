@@ -1829,6 +1829,7 @@ struct pdpd_server {
     double repack_est_s = 0.005;  // recent re-pack time
     HostPinned snap[2];
     cudaEvent_t ev_unsorted = nullptr, ev_copied[2] = {nullptr, nullptr};
+    cudaEvent_t ev_step0 = nullptr, ev_step1 = nullptr;  // around an epoch's steps
     std::thread worker;
 
     void run();
@@ -1989,7 +1990,9 @@ void pdpd_server::run()
         if (epoch == UINT32_MAX) epoch = 0;  // only ended jobs: they leave at the next iteration
         const double t_epoch0 = now_s();
         if (epoch > 0) {
+            cudaEventRecord(ev_step0, eng->stream);
             rc = pdpd_run_async(eng, epoch);
+            cudaEventRecord(ev_step1, eng->stream);
             std::vector<size_t> at_boundary;
             for (size_t i = 0; i < active.size(); i++) {
                 ServerJob &j = *active[i];
@@ -2045,8 +2048,11 @@ void pdpd_server::run()
                 changed = false;
             }
             uint64_t stepped = 0, live_phase = 0;
+            float step_ms = 0.f;
+            if (rc == PDPD_OK && cudaEventElapsedTime(&step_ms, ev_step0, ev_step1) != cudaSuccess) step_ms = 0.f;
             {
                 std::lock_guard<std::mutex> lk(mu);
+                st.step_s += 1e-3 * step_ms;
                 for (auto &j : active) {
                     stepped += (uint64_t)j->desc.n_beads * epoch;
                     if (!j->ended) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
@@ -2105,6 +2111,8 @@ int pdpd_server_create(int precision, int device, size_t memory_budget_bytes, ui
     cudaEventCreateWithFlags(&s->ev_unsorted, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&s->ev_copied[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&s->ev_copied[1], cudaEventDisableTiming);
+    cudaEventCreate(&s->ev_step0);
+    cudaEventCreate(&s->ev_step1);
     s->worker = std::thread([s] { s->run(); });
     *out = s;
     return PDPD_OK;
@@ -2255,6 +2263,8 @@ void pdpd_server_destroy(pdpd_server *s)
     cudaSetDevice(s->eng->device);
     cudaStreamSynchronize(s->eng->side);
     if (s->ev_unsorted) cudaEventDestroy(s->ev_unsorted);
+    if (s->ev_step0) cudaEventDestroy(s->ev_step0);
+    if (s->ev_step1) cudaEventDestroy(s->ev_step1);
     for (cudaEvent_t ev : s->ev_copied)
         if (ev) cudaEventDestroy(ev);
     s->snap[0].release();
