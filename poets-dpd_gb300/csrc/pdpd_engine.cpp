@@ -2007,7 +2007,12 @@ void pdpd_server::run()
                     rc = eng->fail(PDPD_E_NOMEM, "pinned snapshot allocation failed");
                 // the previous copy out of the device staging rows must be done before the unsort
                 if (rc == PDPD_OK) cudaStreamWaitEvent(eng->stream, ev_copied[b ^ 1], 0);
-                if (rc == PDPD_OK) rc = download(eng, 1, eng->stream);
+                // unsort the arena, or only the worlds at a boundary when they are few (a job
+                // ending mid-interval splits an epoch for its own snapshot)
+                if (rc == PDPD_OK && at_boundary.size() * 4 >= active.size()) rc = download(eng, 1, eng->stream);
+                else
+                    for (size_t i : at_boundary)
+                        if (rc == PDPD_OK) rc = download_world(eng, 1, active[i]->slot, eng->stream);
                 if (rc == PDPD_OK) {
                     cudaEventRecord(ev_unsorted, eng->stream);
                     cudaStreamWaitEvent(eng->side, ev_unsorted, 0);
