@@ -422,6 +422,11 @@ def force_roofline(phases, beads, precision, traffic_key=None):
     return roof, ph
 
 
+def kernel_config(eng):
+    return {k: v for k, _, v in eng.GetConfigEntries()
+            if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+
+
 def tune(eng, attach, steps=64):
     """Autotune once (its trials are ordinary steps: the trajectory does not depend on the
     choice), then keep the chosen kernel and brick shape fixed."""
@@ -431,6 +436,9 @@ def tune(eng, attach, steps=64):
     eng.sync()
     tuned = {k: v for k, _, v in eng.GetConfigEntries()}
     eng.SetConfigEntry("autotune", 0)
+    # keep the pick: configured entries are not replaced by the size-aware default
+    for k in ("force_kernel", "brick_x", "brick_y", "brick_z"):
+        eng.SetConfigEntry(k, int(tuned[k]))
     return {k: tuned.get(k) for k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
 
 
@@ -470,11 +478,7 @@ def measure_grid(args, dev, local, world_size):
     worlds = W.make_batched_grid(GRID_STATES, count=n_states)
     total = sum(w.n_beads for w in worlds)
     eng = E.GB300DPDEngine("fp32", device=local)
-    if args.autotune:
-        tuned = tune(eng, lambda: eng.AttachBatch([w.copy() for w in worlds]))
-    else:
-        tuned = {k: v for k, _, v in eng.GetConfigEntries()
-                 if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+    tuned = tune(eng, lambda: eng.AttachBatch([w.copy() for w in worlds])) if args.autotune else None
     # e2e: AttachBatch (upload) + Run(K) + read-back of every state, host buffers
     eng.AttachBatch([w.copy() for w in worlds])
     eng.Run(args.warmup)
@@ -490,6 +494,8 @@ def measure_grid(args, dev, local, world_size):
                    "state; bytes are per step of K"}
     ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
                                      lambda: eng.AttachBatch([w.copy() for w in worlds]))
+    if tuned is None:  # the size-aware default the engine chose for this batch
+        tuned = kernel_config(eng)
     roof, ph = force_roofline(eng.profile_run(args.steps), total, "fp32", "fp32_grid")
     eng.close()
     plain = plain_fp64_metrics(worlds, device=local) if not args.no_plain else None
@@ -511,11 +517,7 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
     world = make_world(name, side=side)
     n = world.n_beads
     eng = E.GB300DPDEngine(precision, device=local)
-    if precision == "fp32" and autotune:
-        tuned = tune(eng, lambda: eng.Attach(world.copy()))
-    else:
-        tuned = {k: v for k, _, v in eng.GetConfigEntries()
-                 if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
+    tuned = tune(eng, lambda: eng.Attach(world.copy())) if precision == "fp32" and autotune else None
     # e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
     eng.Attach(world.copy())
     eng.Run(args.warmup)
@@ -530,6 +532,8 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
            "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"}
     ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
                                      lambda: eng.Attach(world.copy()))
+    if tuned is None:  # the size-aware default the engine chose for this world
+        tuned = kernel_config(eng)
     roof, ph = force_roofline(eng.profile_run(args.steps), n, precision)
     snap = None
     if snapshot and world_size == 1:

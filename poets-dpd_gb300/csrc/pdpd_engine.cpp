@@ -455,8 +455,12 @@ struct pdpd_engine {
         static const int cand[][4] = {{8, 5, 8, 8}, {8, 4, 10, 8}, {8, 4, 8, 10}, {8, 4, 8, 8},
                                       {8, 6, 8, 6}, {6, 3, 4, 6}, {6, 4, 4, 6}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
-        const uint32_t trial = 3;
-        if (!cfg_autotune || tuned || fp64() || any_spatial() || n_steps < (trial + 1) * n_cand + 1) return 0;
+        const uint32_t timed = 3;  // steps timed per candidate, after one warm step
+        const uint32_t warm = 8;   // steps of the untimed warm-up run
+        // the warm-up run (warm + 1 timesteps), then per candidate begin .. final = timed + 2
+        if (!cfg_autotune || tuned || fp64() || any_spatial() ||
+            n_steps < warm + 1 + (timed + 2) * n_cand + 1)
+            return 0;
         const int keep[4] = {cfg_force_kernel, cfg_brick[0], cfg_brick[1], cfg_brick[2]};
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
@@ -466,23 +470,36 @@ struct pdpd_engine {
         uint32_t used = 0;
         tune_log.clear();
         tuning = true;
+        // warm-up with the first candidate, untimed: the first steps after an attach run slower
+        // (first launches, clocks), which would bias whichever candidate came first
+        cfg_force_kernel = cand[0][0];
+        cfg_brick[0] = cand[0][1];
+        cfg_brick[1] = cand[0][2];
+        cfg_brick[2] = cand[0][3];
+        if (configure_bricks() == PDPD_OK) {
+            launches += enqueue_begin(stream);
+            for (uint32_t k = 0; k < warm; k++) launches += enqueue_step(stream);
+            launches += enqueue_final(stream);
+            used += warm + 1;
+        }
         for (int i = 0; i < n_cand; i++) {
             cfg_force_kernel = cand[i][0];
             cfg_brick[0] = cand[i][1];
             cfg_brick[1] = cand[i][2];
             cfg_brick[2] = cand[i][3];
             if (configure_bricks() != PDPD_OK) continue;
-            // one warm step, then the timed trial (steps launched one by one, no graph)
+            // one warm step, then the timed steps (launched one by one, no graph)
             launches += enqueue_begin(stream);
-            for (uint32_t k = 0; k + 1 < trial; k++) launches += enqueue_step(stream);
-            cudaEventRecord(e0, stream);
             launches += enqueue_step(stream);
+            cudaEventRecord(e0, stream);
+            for (uint32_t k = 0; k < timed; k++) launches += enqueue_step(stream);
             cudaEventRecord(e1, stream);
             launches += enqueue_final(stream);
             cudaEventSynchronize(e1);
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
-            used += trial + 1;  // begin .. final completes trial + 1 timesteps
+            ms /= (float)timed;
+            used += timed + 2;  // begin .. final completes timed + 2 timesteps
             char line[96];
             snprintf(line, sizeof line, "%d:%dx%dx%d=%.3fms ", cand[i][0], cand[i][1], cand[i][2],
                      cand[i][3], ms);

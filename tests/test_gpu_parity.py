@@ -247,18 +247,18 @@ def test_autotune_and_mid_run_reconfiguration_keep_the_trajectory():
     ref = world.copy()
     e1 = E.GB300DPDEngine("fp32")
     e1.Attach(ref)
-    e1.Run(60)
+    e1.Run(80)
     w = world.copy()
     e2 = E.GB300DPDEngine("fp32")
     e2.SetConfigEntry("autotune", 1)
     e2.Attach(w)
-    e2.Run(45)
+    e2.Run(65)  # the autotuner's warm-up and trials take the first 49 steps
     cfg = {n: v for n, _, v in e2.GetConfigEntries()}
     assert "trials" in cfg["autotune"]
     e2.SetConfigEntry("force_kernel", 2)
     e2.SetConfigEntry("brick_z", 8)
     e2.Run(15)
-    assert w.t == ref.t == 60
+    assert w.t == ref.t == 80
     assert np.array_equal(w.x, ref.x) and np.array_equal(w.v, ref.v) and np.array_equal(w.f, ref.f)
 
 
