@@ -119,9 +119,12 @@ class World:
         """
         bonds = {"beads": [], "kappa": [], "r0": [], "poly": []}
         angles = {"beads": [], "kappa": [], "theta0": [], "poly": []}
-        single = len(self.polymer_types) == 1
-        for pt_index, pt in enumerate(self.polymer_types):
-            sel = (np.arange(self.poly_type.shape[0]) if single
+        with_terms = [i for i, pt in enumerate(self.polymer_types) if pt.bonds or pt.bond_pairs]
+        # one polymer type with bond terms: its polymers, in id order, give the lists in order
+        single = len(with_terms) == 1
+        for pt_index in with_terms:
+            pt = self.polymer_types[pt_index]
+            sel = (np.arange(self.poly_type.shape[0]) if len(self.polymer_types) == 1
                    else np.nonzero(self.poly_type == pt_index)[0])
             if sel.size == 0:
                 continue

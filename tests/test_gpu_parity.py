@@ -211,6 +211,10 @@ def test_batch_equals_alone(prec):
         assert np.array_equal(a.f, b.f)
         x, v, f, t = eng.read_state(i)  # the per-world read gives the same state
         assert t == b.t and np.array_equal(x, b.x) and np.array_equal(v, b.v) and np.array_equal(f, b.f)
+    # pdpd_read_states wants one view per attached world
+    views = (E.PdpdStateView * 2)()
+    assert E.lib().pdpd_read_states(eng._h, 2, views, 24) == 1  # PDPD_E_INVALID
+    assert "views for a batch of 3 worlds" in E.lib().pdpd_last_error(eng._h).decode()
 
 
 LAUNCH_CONFIGS = {
