@@ -965,14 +965,24 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         e->release();
         return e->fail(PDPD_E_NOMEM, "device allocation failed: %s", cudaGetErrorString(ce));
     }
-    if (e->h_staging[0].alloc(sizeof(double) * 9 * nb + sizeof(uint32_t) * nb) != cudaSuccess) {
+    // Host staging rows of the worlds that come from their descriptors: the whole batch in
+    // slot order, or in a re-pack only the new worlds, packed (the kept worlds' rows stay on
+    // the device, and the pinned buffer stays the size of what a re-pack brings in).
+    std::vector<size_t> hoff(n_worlds);
+    size_t h_rows = 0;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        hoff[i] = any_kept ? h_rows : (size_t)wdev[i].bead_base;
+        if (!any_kept || keep_old[i] < 0) h_rows += ws[i].n_beads;
+    }
+    if (!any_kept) h_rows = nb;
+    if (e->h_staging[0].alloc(sizeof(double) * 9 * h_rows + sizeof(uint32_t) * h_rows) != cudaSuccess) {
         e->release();
         return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
     }
 
     // --- stage and upload
     double *hs = (double *)e->h_staging[0].p;
-    uint32_t *hh = (uint32_t *)(hs + 9 * nb);
+    uint32_t *hh = (uint32_t *)(hs + 9 * h_rows);
     // One pass over the whole batch's beads (global slot g of world i = bead_base_i + k),
     // split across host threads whatever the worlds' sizes.
     parallel_for(nb, 1 << 16, [&](size_t g0, size_t g1) {
@@ -984,17 +994,18 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             const pdpd_world &w = ws[i];
             const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, w.n_beads);
             const bool kept = keep_old && keep_old[i] >= 0;  // state and hashes from the old arena (below)
+            const size_t ho = hoff[i];
             for (size_t k = g - bb; k < k1 && !kept; k++) {
                 const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
                 const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
                 const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
-                double *o = hs + 9 * (bb + k);
+                double *o = hs + 9 * (ho + k);
                 for (int d = 0; d < 3; d++) {
                     o[d] = x[d];
                     o[3 + d] = v[d];
                     o[6 + d] = f[d];
                 }
-                hh[bb + k] = w.hash[k];
+                hh[ho + k] = w.hash[k];
             }
             g = bb + k1;
         }
@@ -1025,7 +1036,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         for (uint32_t i = 0; i < n_worlds; i++)
             if (keep_old[i] < 0 && ws[i].n_beads && ce == cudaSuccess)
                 ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
-                                     hs + 9 * (size_t)wdev[i].bead_base, sizeof(double) * 9 * ws[i].n_beads,
+                                     hs + 9 * hoff[i], sizeof(double) * 9 * ws[i].n_beads,
                                      cudaMemcpyHostToDevice, s);
     }
     for (uint32_t i = 0; any_kept && i < n_worlds; i++) {
@@ -1042,7 +1053,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             uint32_t *dst = e->d_hash.as<uint32_t>() + wdev[i].bead_base;
             const size_t n = sizeof(uint32_t) * ws[i].n_beads;
             ce = keep_old[i] < 0
-                     ? cudaMemcpyAsync(dst, hh + wdev[i].bead_base, n, cudaMemcpyHostToDevice, s)
+                     ? cudaMemcpyAsync(dst, hh + hoff[i], n, cudaMemcpyHostToDevice, s)
                      : cudaMemcpyAsync(dst, e->d_hash_old.as<uint32_t>() + old_base[keep_old[i]], n,
                                        cudaMemcpyDeviceToDevice, s);
         }
