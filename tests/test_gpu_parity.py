@@ -217,6 +217,30 @@ def test_batch_equals_alone(prec):
     assert "views for a batch of 3 worlds" in E.lib().pdpd_last_error(eng._h).decode()
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_batch_with_an_empty_world(prec):
+    """A world without beads in a batch: the others step as alone, and the batch read-back
+    (pdpd_read_states) returns it empty."""
+    empty, _ = load_world_fixture("empty_world")
+    a = W.make_polymer_box(9, chain_fraction=0.1, seed=21)
+    b = W.make_water(7, seed=22)
+    alone = []
+    for w in (a, b):
+        ww = w.copy()
+        eng = E.GB300DPDEngine(prec)
+        eng.Attach(ww)
+        eng.Run(12)
+        alone.append(ww)
+    batch = [a.copy(), empty.copy(), b.copy()]
+    eng = E.GB300DPDEngine(prec)
+    eng.AttachBatch(batch)
+    eng.Run(12)
+    assert batch[1].x.shape == (0, 3) and batch[1].t == empty.t + 12
+    for w_alone, w_batch in zip(alone, (batch[0], batch[2])):
+        assert np.array_equal(w_alone.x, w_batch.x) and np.array_equal(w_alone.v, w_batch.v)
+        assert np.array_equal(w_alone.f, w_batch.f) and w_alone.t == w_batch.t
+
+
 LAUNCH_CONFIGS = {
     # Every FP32 force kernel (shared-memory brick with or without neighbour lists, any brick
     # shape; thread per bead from global memory) adds the same pair terms in the same order
