@@ -498,7 +498,7 @@ def measure_grid(args, dev, local, world_size):
         tuned = kernel_config(eng)
     roof, ph = force_roofline(eng.profile_run(args.steps), total, "fp32", "fp32_grid")
     eng.close()
-    plain = plain_fp64_metrics(worlds, device=local) if not args.no_plain else None
+    plain = plain_fp64_metrics(worlds, device=local) if not args.no_plain and world_size == 1 else None
     value = aggregate_rate(total * args.steps, ms, world_size)
     if plain:
         plain["batched_vs_plain"] = value / world_size / plain["value"]
