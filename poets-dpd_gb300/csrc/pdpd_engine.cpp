@@ -465,7 +465,7 @@ struct pdpd_engine {
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        float best = 1e30f;
+        float best = 1e30f, keep_ms = 0.f;
         int best_i = -1;
         uint32_t used = 0;
         tune_log.clear();
@@ -508,9 +508,14 @@ struct pdpd_engine {
                 best = ms;
                 best_i = i;
             }
+            if (cand[i][0] == keep[0] && cand[i][1] == keep[1] && cand[i][2] == keep[2] && cand[i][3] == keep[3])
+                keep_ms = ms;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        // a few timed steps resolve about 1-2%: the configuration the run started with (the
+        // size-aware default, chosen from long runs) stays unless a candidate beats it by 2%
+        if (keep_ms > 0.f && best > 0.98f * keep_ms) best_i = -1;
         const int *pick = best_i >= 0 ? cand[best_i] : keep;
         cfg_force_kernel = pick[0];
         cfg_brick[0] = pick[1];
