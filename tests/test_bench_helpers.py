@@ -1,0 +1,47 @@
+"""The bench's own arithmetic, on the CPU: the grid sample the CPU arms time, the upload byte
+count of an attach and the roofline figures derived from per-phase device times."""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+import pdpd_world as W  # noqa: E402
+
+
+def test_grid_sample_is_the_grids_first_states():
+    sample = bench.grid_sample()
+    grid = W.make_batched_grid(bench.GRID_STATES, count=len(sample))
+    assert [w.n_beads for w in sample] == [w.n_beads for w in grid]
+    assert sum(w.n_beads for w in sample) >= bench.REF_SAMPLE_BEADS
+    assert sum(w.n_beads for w in sample[:-1]) < bench.REF_SAMPLE_BEADS
+    assert np.array_equal(sample[0].x, grid[0].x)
+
+
+def test_upload_bytes_counts_state_hashes_and_bonds():
+    w = W.make_polymer_box(8, chain_fraction=0.1, seed=3)
+    bb, _, _, ab, _, _ = w.flat_bonds()
+    n = w.n_beads
+    expect = n * (9 * 8 + 4) + (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
+    assert bench.upload_bytes([w]) == expect
+    assert bench.upload_bytes([w, w]) == 2 * expect
+
+
+def test_force_roofline_arithmetic():
+    phases = {"force_ms": 20.0, "force_launches": 10, "sort_ms": 3.0, "sort_launches": 10}
+    roof, ph = bench.force_roofline(phases, 1_000_000, "fp32")
+    assert ph == {"force": 2.0, "sort": 0.3}
+    assert roof["kernel_ms"] == 2.0
+    assert roof["achieved"] == pytest.approx(1180.0 * 1e6 / 2e-3 / 1e9)
+    assert roof["frac"] == pytest.approx(roof["achieved"] / roof["peak"])
+    assert roof["bound"] == "hbm" and roof["unit"] == "GB/s"
+
+
+def test_grid_workload_name_names_the_grid():
+    assert bench.grid_workload_name(512).startswith("batched512: 512 polymer-solvent states")
+    assert "(its first 64)" in bench.grid_workload_name(64)
