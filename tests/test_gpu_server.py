@@ -56,6 +56,7 @@ def test_server_jobs_equal_alone(prec, budget):
     st = srv.stats()
     assert st["jobs_done"] == len(jobs) and st["jobs_failed"] == 0
     assert st["bead_steps"] == sum(w.n_beads * n for w, n in jobs)
+    assert 0.0 < st["step_s"] <= st["wall_s"]  # device time of the steps, within the wall time
     for jid, (w, n) in zip(ids, jobs):
         _same(_alone(prec, w, n), srv.results[jid])
         assert srv.snapshots.get(jid, 0) == (n - 1) // 50
