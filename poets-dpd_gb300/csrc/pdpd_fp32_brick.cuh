@@ -403,13 +403,15 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
 }
 
 
-// Row walk of one staged home bead (force variants 6 and 7): the 9 neighbour rows (dx, dy) in order;
-// a row's 3 cells (dz = -1, 0, +1) are one contiguous range of staged beads, trimmed at its
-// ends by the same conservative test as the per-cell loop.  The warp pays the longest row of
-// its lanes 9 times instead of the longest cell 27 times.  The in-range candidates go to this
-// thread's list in the direction order; room for a whole row is made before the row (the list
-// is evaluated into F first when it could overflow), so the candidate loop has no capacity
-// check and no branch.  Returns the number of entries left in the list.
+// Row walk of one staged home bead (force variants 6, 7 and 8): the 9 neighbour rows (dx, dy)
+// in order; a row's 3 cells (dz = -1, 0, +1) are one contiguous range of staged beads, trimmed
+// at its ends by the same conservative test as the per-cell loop (and by the far z half of an
+// end cell: a cell's beads with z offset < 0.5 come first, hlo counts them).  The warp pays the
+// longest row of its lanes 9 times instead of the longest cell 27 times.  The in-range
+// candidates go to this thread's list, as staged indices, in the direction order; room for a
+// whole row is made before the row (the list is evaluated into F first when it could
+// overflow), so the candidate loop has no capacity check and no branch.  Returns the number
+// of entries left in the list.
 template <int T = BRICK_THREADS>
 __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spos,
                                                   const float4 *__restrict__ svel,
