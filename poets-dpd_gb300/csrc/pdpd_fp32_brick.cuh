@@ -1,22 +1,24 @@
 // FP32 brick force kernel.  Included inside pdpd_fp32.cu's anonymous namespace (it uses the
 // helpers defined there: WorldCache, load_world, advance_position, bond_forces32, pack_dir).
 //
-// A block takes one brick of cells of one world and stages the brick plus its one-cell halo
-// -- (bx+2)(by+2)(bz+2) halo cells, z fastest -- into shared memory with coalesced float4
-// loads: for each (x, y) halo row the cells z0-1 .. z0+bz are consecutive cells of the sorted
-// state, i.e. one or (at a periodic wrap) a few contiguous runs of slots.  A halo cell that
-// is a periodic image of a cell already staged (boxes smaller than the halo) is staged again,
-// so every neighbour is seen at its own image position, as the reference's direction loop
-// sees it (naive_dpd_engine_half_step.hpp:300-315).
+// A block takes a brick of cells of one world (from a queue shared by the persistent blocks)
+// and stages the brick plus its one-cell halo -- (bx+2)(by+2)(bz+2) halo cells, z fastest --
+// into shared memory with coalesced 16-byte copies: for each (x, y) halo row the cells
+// z0-1 .. z0+bz are consecutive cells of the sorted state, i.e. one or (at a periodic wrap) a
+// few contiguous runs of slots.  A halo cell that is a periodic image of a cell already
+// staged (boxes smaller than the halo) is staged again, so every neighbour is seen at its own
+// image position, as the reference's direction loop sees it
+// (naive_dpd_engine_half_step.hpp:300-315).
 //
 // Then one thread per home bead gathers its pair forces from shared memory: the 27
-// neighbour cells in the reference's direction order, each cell's beads in id order,
-// accumulated one pair at a time.  In the list variant the thread first filters the
-// candidates and keeps the in-range ones (16-bit entries: staged index + direction) in a
-// shared-memory list, then evaluates the list in order; the divergent, expensive force
-// evaluation then runs on denser warps.  Both variants, the thread-per-bead global-memory
-// kernel and the overflow fallback produce bit-identical forces: the same explicitly
-// rounded pair routine, the same order.
+// neighbour cells in the reference's direction order, each cell's beads in the sorted order,
+// accumulated one pair at a time.  In the list variants the thread first filters the
+// candidates and keeps the in-range ones (16-bit entries: staged index, with the direction in
+// its high bits for variants 0 and 3, or recovered from the staged halo cells for the row
+// walks 6-8) in a shared-memory list, then evaluates the list in order; the divergent,
+// expensive force evaluation then runs on denser warps.  All variants, the thread-per-bead
+// global-memory kernel and the overflow fallback produce bit-identical forces: the same
+// explicitly rounded pair routine, the same order.
 
 constexpr int BRICK_THREADS = 128;       // threads per block of variants 0, 2-7
 constexpr int BRICK_WARPS = BRICK_THREADS / 32;
