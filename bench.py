@@ -24,7 +24,10 @@ grid's bead payload (~1 GB) is larger than L2, so no flush is needed.
   serving   the served stream (Poisson arrivals, continuous batching): p50/p99 latency and
             served bead-steps/s against sequential execution.
   cpu_baseline  the oracle (C restatement of the reference's FP64 half-step engine) on all
-            host cores, on a bounded sample of the same workload.
+            host cores, on a bounded sample of the same workload, with the host's CPU and,
+            beside it, the reference's own TBB engine's expected rate: the port's rate times
+            the reference/port ratio measured with both on one host (oracle/ref/calibrate.py;
+            the reference sources are not present where this runs).
 
 --workload polymer128 (or polymer32, water8) makes the single box the headline instead.
 --impl reference times the reference's CPU implementation of the path (the oracle port;
@@ -154,6 +157,51 @@ def oracle_rate(world, max_seconds=12.0, max_steps=200, threads=None):
         steps += 1
     dt = time.perf_counter() - t0
     return world.n_beads * steps / dt, threads, steps, dt
+
+
+CALIBRATION = os.path.join(ROOT, "oracle", "tbb_calibration.json")
+
+
+def host_cpu():
+    """The host CPU as lscpu reports it: model, threads, SMT (threads per core), cores."""
+    info = {"threads": os.cpu_count() or 1}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.TimeoutExpired):
+        return info
+    keys = {"Model name": "model", "Thread(s) per core": "smt", "Core(s) per socket":
+            "cores_per_socket", "Socket(s)": "sockets", "Architecture": "arch"}
+    for line in out.splitlines():
+        k, _, v = line.partition(":")
+        if k.strip() in keys and keys[k.strip()] not in info:
+            v = v.strip()
+            info[keys[k.strip()]] = int(v) if v.isdigit() else v
+    return info
+
+
+def reference_estimate(port_rate, sample_key):
+    """The reference's own TBB engine's expected rate on the same sample and cores: the port's
+    measured rate times the reference/port ratio that oracle/ref/calibrate.py measured with
+    both on one host (the reference sources exist only where that ran)."""
+    if not os.path.exists(CALIBRATION):
+        return None
+    with open(CALIBRATION) as fh:
+        cal = json.load(fh)
+    s = cal["samples"].get(sample_key)
+    if not s:
+        return None
+    r = float(s["ratio_reference_over_port"])
+    return {"value": port_rate * r, "unit": "bead-steps/s", "ratio_reference_over_port": r,
+            "reference_engines": s["reference_engines"],
+            "calibrated_on": f"{cal['host'].get('model', '?')}, {cal['threads']} threads "
+                             f"({cal['host'].get('machine', '?')}), {cal['when']}",
+            "note": "estimate: the port's rate measured here x the ratio measured with both "
+                    "engines on the calibration host"}
+
+
+def calibration_key(workload):
+    """The calibration sample of a workload's CPU sample (oracle/tbb_calibration.json)."""
+    return {GRID: "grid3", "polymer128": "polymer32", "polymer32": "polymer32"}.get(workload)
 
 
 def grid_sample(n_states=GRID_STATES, min_beads=REF_SAMPLE_BEADS):
@@ -376,7 +424,9 @@ def run_reference_arm(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload, "sample": sample, "parallelism": "replicas only"},
         "cpu_baseline": {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample}, {args.steps} steps"},
+                         "sample": f"{sample}, {args.steps} steps", "host": host_cpu(),
+                         "reference_tbb_estimate": reference_estimate(
+                             rate, calibration_key(args.workload))},
         "e2e": {"value": rate, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -599,7 +649,8 @@ def run_engine_arm(args):
             rate, threads, steps, dt = oracle_rate(make_world(args.workload, side=args.ref_side))
             desc = f"{args.ref_side}^3 box of the same recipe, {steps} steps in {dt:.1f} s"
         cpu = {"value": rate, "unit": "bead-steps/s", "cores": threads, "kind": "port",
-               "sample": desc}
+               "sample": desc, "host": host_cpu(),
+               "reference_tbb_estimate": reference_estimate(rate, calibration_key(args.workload))}
     line = {
         "metric": METRIC, "value": main["value"], "unit": "bead-steps/s", "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,

@@ -203,20 +203,22 @@ int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint3
 
 /* Allocation-free stepping -- this entry point has no counterpart in the reference.
  *
- * For callers that must not allocate device memory: a host thread that is capturing a
- * CUDA stream into a graph (cudaMalloc cannot be captured), or a framework that owns all
- * device memory through its own pool and forbids side allocations.  It advances one
- * bond-free world by n_steps with the FP64 integrator (bit-identical to pdpd_run's FP64
- * engine) on caller-owned device arrays and allocates nothing: no cudaMalloc, cudaFree or
- * allocating library call.
+ * For callers that must not allocate device memory while they run: a framework that owns
+ * all device memory through its own pool and forbids side allocations, or a host loop that
+ * reserves its memory at start-up and cannot afford the device-wide synchronisation that
+ * cudaMalloc and cudaFree may cause.  It advances one bond-free world by n_steps with the
+ * FP64 integrator (bit-identical to pdpd_run's FP64 engine) on caller-owned device arrays
+ * and allocates nothing: no cudaMalloc, cudaFree or allocating library call.
  *   w       box, dt, seed, t, bead types, interaction matrices (host pointers) and n_beads;
  *           its bead-array pointers are ignored.  Step k draws the random numbers of time
  *           w->t + k; the caller advances its own t by n_steps afterwards.
  *   d_x, d_v, d_f  device arrays, 3 doubles per bead in bead-id order, read and updated
  *           in place (x(t), v(t), f(t) in; x(t+n), v(t+n), f(t+n) out).
  *   d_hash  device array of the beads' BeadHash values.
- *   stream  a cudaStream_t (NULL: the legacy default stream); the call returns after the
- *           stream has finished the steps.
+ *   stream  a cudaStream_t (NULL: the legacy default stream).  The call synchronises this
+ *           stream at its end and reads back a device error word, so it returns after the
+ *           steps have finished; a bead that leaves the box or becomes non-finite in any
+ *           of the n_steps steps makes it return PDPD_E_BEAD_LOST.
  * Limits: at most PDPD_NOALLOC_MAX_BEADS beads and PDPD_NOALLOC_MAX_CELLS cells; worlds with
  * Hookean or angle bonds are rejected (PDPD_E_UNSUPPORTED); larger worlds get PDPD_E_NOMEM.
  * Scratch memory is one fixed array inside the library (about 1.3 MB), held on every GPU that

@@ -692,11 +692,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(pdpd::Na
 namespace pdpd {
 namespace {
 
-__global__ void k_na_clear(NaScratch *S, uint32_t n_cells)
+// Zeroes the cell counts before each step; the error word only before a call's first step,
+// so that a bead lost in any step of the call is still reported at its end.
+__global__ void k_na_clear(NaScratch *S, uint32_t n_cells, int clear_err)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_cells) S->cnt[i] = 0u;
-    if (i == 0) S->err = 0u;
+    if (i == 0 && clear_err) S->err = 0u;
 }
 
 // update_pos (dpd_maths_core_half_step.hpp:22-49) and the bead's new cell and arrival rank.
@@ -926,7 +928,7 @@ extern "C" int pdpd_step_noalloc(const pdpd_world *w, double *d_x, double *d_v, 
     const uint32_t gb = (p.n + 255) / 256, gc = (p.n_cells + 255) / 256;
     for (uint32_t step = 0; step < n_steps; step++) {
         p.t = w->t + (int64_t)step;
-        k_na_clear<<<gc, 256, 0, s>>>(S, p.n_cells);
+        k_na_clear<<<gc, 256, 0, s>>>(S, p.n_cells, step == 0 ? 1 : 0);
         k_na_update_pos<<<gb, 256, 0, s>>>(p, S, d_x, d_v, d_f);
         k_na_scan<<<1, 1024, 0, s>>>(S, p.n_cells, p.n);
         k_na_place<<<gb, 256, 0, s>>>(S, p.n);

@@ -29,6 +29,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpdpd_gb300.so")
 
 PDPD_FP32, PDPD_FP64 = 0, 1
+# PDPD_NOALLOC_MAX_BEADS / PDPD_NOALLOC_MAX_CELLS: the fixed scratch size of pdpd_step_noalloc.
+NOALLOC_MAX_BEADS, NOALLOC_MAX_CELLS = 65536, 32768
 STATUS = {0: "PDPD_OK", 1: "PDPD_E_INVALID", 2: "PDPD_E_UNSUPPORTED", 3: "PDPD_E_CUDA",
           4: "PDPD_E_STATE", 5: "PDPD_E_BOND_SNAPPED", 6: "PDPD_E_BEAD_LOST", 7: "PDPD_E_NOMEM"}
 

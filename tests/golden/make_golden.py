@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference's own code.
 
-Run in a container that has the reference sources (default /root/reference):
+Run in a container that has the reference sources (oracle/ref/Makefile says where it looks;
+PDPD_REFERENCE_ROOT overrides it):
 
-    make -C oracle/ref REF_ROOT=/root/reference     # builds oracle/_ref/ref_harness
+    make -C oracle/ref all                           # builds oracle/_ref/ref_harness
     python tests/golden/make_golden.py
 
 The harness (oracle/ref/ref_harness.cpp) compiles the reference's FP64 engines unchanged from
@@ -369,8 +370,9 @@ def main():
         raise SystemExit("build the reference harness first: make -C oracle/ref")
     hash_fixture()
     testbase_fixture()
-    save_world_fixture("water8_seed1", W.make_water(8, seed=1), [1, 10, 100],
-                       "8^3 water, density 3 (1536 beads), a=25, gamma=4.5, dt=0.02, seed=1")
+    save_world_fixture("water8_seed1", W.make_water(8, seed=1), [1, 10, 100, 1000],
+                       "8^3 water, density 3 (1536 beads), a=25, gamma=4.5, dt=0.02, seed=1 (the reference's "
+                       "1000-step FP64 configuration)")
     save_world_fixture("polymer10_seed2", W.make_polymer_box(10, chain_fraction=0.1, seed=2),
                        [1, 10, 50],
                        "10^3 W/H/T polymer-solvent box, 10% in H-T5 chains, k=128 r0=0.5, "

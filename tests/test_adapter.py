@@ -15,11 +15,26 @@ import v2binary as V
 from _helpers import load_v2_fixture, v2_fixture_names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INCLUDE = os.environ.get("PDPD_REFERENCE_INCLUDE", "/root/reference/include")
+
+
+def _reference_include():
+    """PDPD_REFERENCE_INCLUDE, else what the reference build recipe (oracle/ref/Makefile)
+    reports: the reference's include directory, or nothing where the sources are absent."""
+    if os.environ.get("PDPD_REFERENCE_INCLUDE"):
+        return os.environ["PDPD_REFERENCE_INCLUDE"]
+    try:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"),
+                            "print-include"], capture_output=True, text=True, timeout=60)
+        return r.stdout.strip()
+    except (OSError, subprocess.TimeoutExpired):
+        return ""
+
+
+REF_INCLUDE = _reference_include()
 BUILD = os.path.join(ROOT, "poets-dpd_gb300", "_build")
 EXE = os.path.join(BUILD, "adapter_check")
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_INCLUDE, "dpd")),
+pytestmark = pytest.mark.skipif(not REF_INCLUDE or not os.path.isdir(os.path.join(REF_INCLUDE, "dpd")),
                                 reason="reference sources not present")
 
 
