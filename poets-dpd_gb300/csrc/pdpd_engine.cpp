@@ -146,12 +146,14 @@ const ConfigEntry kConfig[] = {
     {"graph_steps", "Timesteps captured per CUDA graph replay (0 = automatic)."},
     {"use_graphs", "Replay captured CUDA graphs (1) or launch kernels directly (0)."},
     {"force_kernel", "FP32 force kernel (default by size: 8 from about 1,300 cells per SM, else 6): "
-                     "0 = shared-memory brick with neighbour lists, "
-                     "1 = thread per bead from global memory, 2 = shared-memory brick, "
-                     "3 / 4 = as 0 / 2 with the neighbour cells walked as one flat sequence, "
-                     "5 = warp per home cell, 6 = as 0 with the neighbour cells walked row by row, "
-                     "7 = as 6 with the lists evaluated balanced across lanes, "
-                     "8 = as 6 with 512-thread blocks for larger bricks."},
+                     "1 = thread per bead from global memory, "
+                     "6 = shared-memory brick, full shell, neighbour rows walked into lists, "
+                     "128-thread blocks; 8 = as 6 with 512-thread blocks for larger bricks; "
+                     "9 = shared-memory brick, half shell (each pair inside a brick evaluated "
+                     "once, its reaction passed to the other bead), fixed-point force sums, "
+                     "384-thread blocks.  1, 6 and 8 give the same forces to the bit; 9 gives the "
+                     "same forces to the bit whatever its brick shape, grid or batch, within the "
+                     "FP32 tolerance of the others."},
     {"brick_x", "Brick extent in cells along x (FP32 brick kernel; default by size: 5x8x8, "
                 "3x4x6 from about 200 cells per SM, 2x4x4 below)."},
     {"brick_y", "Brick extent in cells along y (FP32 brick kernel)."},
@@ -357,16 +359,19 @@ struct pdpd_engine {
         static const int big[][3] = {{5, 8, 8}, {4, 8, 8}, {4, 6, 8}, {4, 4, 6}, {3, 4, 4}};
         static const int mid[3] = {3, 4, 6}, small[3] = {2, 4, 4};
         const int *b = per_sm >= 200 ? mid : small;
-        if (cfg_force_kernel == 8 || per_sm >= 1300) {
+        if (cfg_force_kernel == 8 || cfg_force_kernel == 9 || per_sm >= 1300) {
             // the largest brick whose halo (at the batch's highest density) fits the staging
             // capacity 5 Poisson deviations above its mean, so dense boxes do not overflow it
+            const int v = cfg_force_kernel == 9 ? 9 : 8;
             uint32_t npair = 1;
             for (const WorldHost &wh : worlds) npair = std::max(npair, wh.dev.n_types * wh.dev.n_types);
             b = big[4];
             for (const auto &c : big) {
+                if (v == 9 && c[0] * c[1] * c[2] > 256) continue;  // the half shell's home sums
                 const uint32_t hc = (uint32_t)(c[0] + 2) * (c[1] + 2) * (c[2] + 2);
                 const double mean = max_density * hc;
-                if (mean + 5.0 * std::sqrt(mean) <= (double)brick_maxb_limit(8, hc, npair)) {
+                const uint32_t hm = home_want((uint32_t)(c[0] * c[1] * c[2]));
+                if (mean + 5.0 * std::sqrt(mean) <= (double)brick_maxb_limit(v, hc, npair, hm)) {
                     b = c;
                     break;
                 }
@@ -381,6 +386,15 @@ struct pdpd_engine {
     {
         const double mean = max_density * hc;
         return std::max(mean + 6.0 * std::sqrt(mean), 1.2 * mean) + 32;
+    }
+
+    // Home beads the half-shell kernel keeps force sums for, for bricks of `cells` home cells:
+    // the mean of the densest world + 6 standard deviations + 32 (a fuller brick takes the
+    // global-memory path, with the same result).
+    uint32_t home_want(uint32_t cells) const
+    {
+        const double mean = max_density * cells;
+        return (uint32_t)(mean + 6.0 * std::sqrt(mean) + 32);
     }
 
     // Build the brick work queue of the FP32 force kernel for the current brick shape: every
@@ -431,12 +445,14 @@ struct pdpd_engine {
         for (const WorldHost &wh : worlds) a.brick_npair = std::max(a.brick_npair, wh.dev.n_types * wh.dev.n_types);
         // staged-bead capacity (staging_want) within the variant's limit; a fuller brick takes
         // the (bit-identical) global path
+        a.brick_home_max = a.force_kernel == 9 ? home_want((uint32_t)(cfg_brick[0] * cfg_brick[1] * cfg_brick[2])) : 0u;
         const double want = staging_want(a.brick_hc_max);
-        const double limit = (double)brick_maxb_limit(a.force_kernel, a.brick_hc_max, a.brick_npair);
+        const double limit = (double)brick_maxb_limit(a.force_kernel, a.brick_hc_max, a.brick_npair, a.brick_home_max);
         a.brick_maxb = (uint32_t)std::min(limit, std::max(64.0, want));
         int grid = 0;
         uint32_t bytes = 0;
-        int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, a.brick_npair, &grid, &bytes);
+        int rc = brick_setup(sm_count, a.force_kernel, a.brick_hc_max, a.brick_maxb, a.brick_npair,
+                             a.brick_home_max, &grid, &bytes);
         if (rc)
             return fail(PDPD_E_CUDA, "brick kernel setup (%u bytes of shared memory): %s", bytes,
                         cudaGetErrorString((cudaError_t)rc));
@@ -452,6 +468,7 @@ struct pdpd_engine {
     // Returns the number of steps consumed.
     uint32_t autotune(uint32_t n_steps)
     {
+        // (variant 9 is left out: its forces are not bit-identical with these)
         static const int cand[][4] = {{8, 5, 8, 8}, {8, 4, 10, 8}, {8, 4, 8, 10}, {8, 4, 8, 8},
                                       {8, 6, 8, 6}, {6, 3, 4, 6}, {6, 4, 4, 6}, {1, 4, 4, 4}};
         const int n_cand = (int)(sizeof cand / sizeof cand[0]);
@@ -1420,7 +1437,8 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     else if (k == "graph_steps") e->cfg_graph_steps = (int)v;
     else if (k == "use_graphs") e->cfg_use_graphs = v ? 1 : 0;
     else if (k == "force_kernel") {
-        if (v > 8) return e->fail(PDPD_E_INVALID, "force_kernel must be 0..8");
+        if (v != 1 && v != 6 && v != 8 && v != 9)
+            return e->fail(PDPD_E_INVALID, "force_kernel must be 1, 6, 8 or 9");
         e->cfg_force_kernel = (int)v;
         e->kernel_user = true;
     } else if (k == "brick_x" || k == "brick_y" || k == "brick_z") {

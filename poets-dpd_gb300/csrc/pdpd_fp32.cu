@@ -204,8 +204,12 @@ __device__ __forceinline__ float slab_gap(float o, int d)
 }
 
 // Separation of a neighbour bead pj from a home position already shifted by the neighbour
-// cell's direction (a = o_home - dir), and its square.  Every FP32 force path uses this and
-// pair_accumulate, with explicit roundings, so all paths give bit-identical forces.
+// cell's direction (a = o_home - dir), and its square: the neighbour walks' cheap prefilter.
+// A walk keeps a candidate when this r^2 is below R2_PREFILTER; the evaluation decides with
+// the exact test on pair_sep's r^2, which differs from this one by at most a few units in the
+// last place (|dr^2| < 4e-6), so no pair in range is lost.
+constexpr float R2_PREFILTER = 1.0f + 0x1p-17f;
+
 __device__ __forceinline__ float pair_r2(float ax, float ay, float az, const float4 pj, float &dx,
                                          float &dy, float &dz)
 {
@@ -236,6 +240,125 @@ __device__ __forceinline__ void pair_accumulate(float dx, float dy, float dz, fl
     F[0] = __fmaf_rn(ex, scaled, F[0]);
     F[1] = __fmaf_rn(ey, scaled, F[1]);
     F[2] = __fmaf_rn(ez, scaled, F[2]);
+}
+
+// Separation of the pair (i, j), d = cell_j - cell_i, per axis (o_i - [d > 0]) - (o_j - [d < 0]),
+// and its square: the separation every pair force is evaluated with.  When the pair is close
+// across a cell face the offset next to the face is >= 0.5, so its shift by one cell is exact
+// and the separation carries one rounding relative to its own (small) size -- the unit vector
+// keeps FP32 precision however close the beads are (o_i - d - o_j in the other order loses
+// up to 6e-8 absolute).  Rounding to nearest is symmetric under a change of sign, so the
+// separation computed on j's side is exactly the negation and r^2 is the same to the bit.
+__device__ __forceinline__ float sep_axis(float oi, float oj, int d)
+{
+    const float a = d > 0 ? __fsub_rn(oi, 1.0f) : oi;
+    const float b = d < 0 ? __fsub_rn(oj, 1.0f) : oj;
+    return __fsub_rn(a, b);
+}
+
+__device__ __forceinline__ float pair_sep(const float4 pi, const float4 pj, int ddx, int ddy, int ddz,
+                                          float &dx, float &dy, float &dz)
+{
+    dx = sep_axis(pi.x, pj.x, ddx);
+    dy = sep_axis(pi.y, pj.y, ddy);
+    dz = sep_axis(pi.z, pj.z, ddz);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// The pair test of update_bead_pair (naive_dpd_engine_half_step.hpp:358-368 and
+// dpd_state.hpp:138-139) on the canonical r^2.
+__device__ __forceinline__ bool pair_in_range(float r2)
+{
+    return r2 < 1.0f && r2 >= min_dist_sqr_f();
+}
+
+// Pair forces are summed in fixed point by the half-shell kernel: each pair force component,
+// scaled by 2^20, is rounded to an integer (rounding to nearest is symmetric, so the two beads
+// of a pair receive exact negatives; the rounding error, <= 2^-21 per term, is far below the
+// FP32 engine's tolerance) and the integers are added in 64 bits.  Integer sums do not depend
+// on their order, so a bead's total force is the same whichever brick shape, batch or thread
+// evaluated its pairs, and whether a pair was evaluated from one side with the reaction
+// passed on (inside a brick) or from both sides (across a brick face).  Terms below 2^31 (pair
+// forces below 2048) convert with the full-rate 32-bit conversion; larger ones with the
+// 64-bit one (slow on this part, and rare).  A pair force of 2^20 or more, or not finite, is
+// reported as ERR_NONFINITE.
+constexpr float FX_ONE = 1048576.0f;             // 2^20
+constexpr float FX_INV = 9.5367431640625e-07f;   // 2^-20
+constexpr float FX_FAST = 2147483520.0f;         // largest float below 2^31
+constexpr float FX_LIMIT = 1048576.0f;           // |pair force| reported as an error
+
+// A 64-bit fixed-point sum as a float force: one correctly rounded conversion of the whole
+// integer (converting its two 32-bit halves separately rounds the low half to 24 bits, an
+// error of up to 2^7 units that cancels badly for negative sums), then an exact scaling by a
+// power of two.  Once per bead and axis, so the slower 64-bit conversion costs nothing.
+__device__ __forceinline__ float fx_to_float(long long q)
+{
+    return __fmul_rn(__ll2float_rn(q), FX_INV);
+}
+
+__device__ __forceinline__ void fx_to_force(const long long q[3], float F[3])
+{
+    F[0] = fx_to_float(q[0]);
+    F[1] = fx_to_float(q[1]);
+    F[2] = fx_to_float(q[2]);
+}
+
+// One DPD pair force on the home bead i (calc_force, dpd_maths_core_half_step.hpp:69-157):
+// conservative a (1-r), dissipative -gamma w^2 (e.dv), random sqrt(gamma) w sqrt(24 kT/dt) u
+// with kT = 1, along e = dx / r, from the canonical separation (dx, dy, dz) and r2 in range.
+// Every operation is explicitly rounded; e and dv change sign with the side the pair is
+// evaluated from and everything else does not, so the force is exactly antisymmetric.
+// Returns the force in fixed point (fx_to_force's scale); a pair force of magnitude beyond
+// FX_LIMIT (or not finite) contributes nothing and sets ERR_NONFINITE.
+__device__ __forceinline__ void pair_force_fx(float dx, float dy, float dz, float r2, const float4 vi,
+                                              const float4 vj, uint32_t hi, uint32_t hj, float2 pp,
+                                              uint32_t th_lo, uint32_t th_hi, float scale,
+                                              long long &qx, long long &qy, long long &qz,
+                                              uint32_t &err)
+{
+    const float inv_r = rsqrtf(r2);
+    const float r = __fmul_rn(r2, inv_r);
+    const float wr = __fsub_rn(1.0f, r);
+    const float ex = __fmul_rn(dx, inv_r), ey = __fmul_rn(dy, inv_r), ez = __fmul_rn(dz, inv_r);
+    const float rdotv = __fmaf_rn(ez, __fsub_rn(vi.z, vj.z),
+                                  __fmaf_rn(ey, __fsub_rn(vi.y, vj.y), __fmul_rn(ex, __fsub_rn(vi.x, vj.x))));
+    const float sg = __fmul_rn(pp.y, wr);
+    const float u = hash_u(th_lo, th_hi, hi, hj);
+    const float con_m_diss = __fmaf_rn(-__fmul_rn(sg, sg), rdotv, __fmul_rn(pp.x, wr));
+    float scaled = __fmaf_rn(__fmul_rn(sg, scale), u, con_m_diss);
+    if (!(fabsf(scaled) < FX_LIMIT)) {
+        err |= ERR_NONFINITE;
+        scaled = 0.0f;
+    }
+    const float sq = __fmul_rn(scaled, FX_ONE);
+    const float tx = __fmul_rn(ex, sq), ty = __fmul_rn(ey, sq), tz = __fmul_rn(ez, sq);
+    if (fabsf(sq) < FX_FAST) {  // |e| <= 1: every component converts in 32 bits
+        qx = __float2int_rn(tx);
+        qy = __float2int_rn(ty);
+        qz = __float2int_rn(tz);
+    } else {
+        qx = __float2ll_rn(tx);
+        qy = __float2ll_rn(ty);
+        qz = __float2ll_rn(tz);
+    }
+}
+
+// The pair (i, j) at direction d = cell_j - cell_i, added to i's fixed-point sum q when in
+// range.  Returns whether it was.
+__device__ __forceinline__ bool pair_add_fx(const float4 pi, const float4 vi, const float4 pj, const float4 vj,
+                                            int ddx, int ddy, int ddz, float2 pp, uint32_t th_lo,
+                                            uint32_t th_hi, float scale, long long q[3], uint32_t &err)
+{
+    float dx, dy, dz;
+    const float r2 = pair_sep(pi, pj, ddx, ddy, ddz, dx, dy, dz);
+    if (!pair_in_range(r2)) return false;
+    long long fx, fy, fz;
+    pair_force_fx(dx, dy, dz, r2, vi, vj, __float_as_uint(pi.w), __float_as_uint(pj.w), pp, th_lo, th_hi,
+                  scale, fx, fy, fz, err);
+    q[0] += fx;
+    q[1] += fy;
+    q[2] += fz;
+    return true;
 }
 
 // Bonds, update_mom and either the final write or the next update_pos with the cell count,
@@ -313,23 +436,19 @@ __device__ void pair_forces32_seq(const KArgs &a, const WorldDev &w, const float
     const uint32_t nt = w.n_types;
     const uint32_t hi = __float_as_uint(ph.w);
     const uint32_t ti = min(hi >> 28, nt - 1u);
-    const float min2 = min_dist_sqr_f();
     for (int ddx = -1; ddx <= 1; ddx++) {
         const int nx = wrap_index(c[0] + ddx, w.L[0]);
-        const float ax = __fsub_rn(ph.x, (float)ddx);
         for (int ddy = -1; ddy <= 1; ddy++) {
             const int ny = wrap_index(c[1] + ddy, w.L[1]);
-            const float ay = __fsub_rn(ph.y, (float)ddy);
             const uint32_t row = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2];
             for (int ddz = -1; ddz <= 1; ddz++) {
-                const float az = __fsub_rn(ph.z, (float)ddz);
                 const uint32_t nc = row + (uint32_t)wrap_index(c[2] + ddz, w.L[2]);
                 const uint32_t j1 = a.start[nc + 1];
                 for (uint32_t j = a.start[nc]; j < j1; j++) {
                     const float4 pj = pos[j];
                     float dx, dy, dz;
-                    const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-                    if (r2 < 1.0f && r2 >= min2) {
+                    const float r2 = pair_sep(ph, pj, ddx, ddy, ddz, dx, dy, dz);
+                    if (pair_in_range(r2)) {
                         const uint32_t hj = __float_as_uint(pj.w);
                         pair_accumulate(dx, dy, dz, r2, vh, vel[j], hi, hj,
                                         pair[ti * nt + min(hj >> 28, nt - 1u)], th_lo, th_hi,
@@ -339,6 +458,37 @@ __device__ void pair_forces32_seq(const KArgs &a, const WorldDev &w, const float
             }
         }
     }
+}
+
+// The same gather in fixed point (pair_add_fx): the half-shell kernel's path for a brick whose
+// halo does not fit in shared memory, with the same sums as its staged path.
+__device__ void pair_forces32_seq_fx(const KArgs &a, const WorldDev &w, const float2 *pair,
+                                     uint32_t th_lo, uint32_t th_hi, float scale, const int c[3],
+                                     const float4 ph, const float4 vh, float F[3], uint32_t &err)
+{
+    const float4 *__restrict__ pos = (const float4 *)a.posA;
+    const float4 *__restrict__ vel = (const float4 *)a.velA;
+    const uint32_t nt = w.n_types;
+    const uint32_t ti = min(__float_as_uint(ph.w) >> 28, nt - 1u);
+    long long q[3] = {0, 0, 0};
+    for (int ddx = -1; ddx <= 1; ddx++) {
+        const int nx = wrap_index(c[0] + ddx, w.L[0]);
+        for (int ddy = -1; ddy <= 1; ddy++) {
+            const int ny = wrap_index(c[1] + ddy, w.L[1]);
+            const uint32_t row = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2];
+            for (int ddz = -1; ddz <= 1; ddz++) {
+                const uint32_t nc = row + (uint32_t)wrap_index(c[2] + ddz, w.L[2]);
+                const uint32_t j1 = a.start[nc + 1];
+                for (uint32_t j = a.start[nc]; j < j1; j++) {
+                    const float4 pj = pos[j];
+                    pair_add_fx(ph, vh, pj, vel[j], ddx, ddy, ddz,
+                                pair[ti * nt + min(__float_as_uint(pj.w) >> 28, nt - 1u)], th_lo, th_hi,
+                                scale, q, err);
+                }
+            }
+        }
+    }
+    fx_to_force(q, F);
 }
 
 // Phase 2: the pair forces of the listed neighbours, in list order.
@@ -359,11 +509,10 @@ __device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
         const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
         const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
         const float4 pj = pos[j];
-        const float ax = __fsub_rn(ph.x, (float)((int)(d & 3u) - 1));
-        const float ay = __fsub_rn(ph.y, (float)((int)((d >> 2) & 3u) - 1));
-        const float az = __fsub_rn(ph.z, (float)((int)((d >> 4) & 3u) - 1));
         float dx, dy, dz;
-        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+        const float r2 = pair_sep(ph, pj, (int)(d & 3u) - 1, (int)((d >> 2) & 3u) - 1, (int)((d >> 4) & 3u) - 1,
+                                  dx, dy, dz);
+        if (!pair_in_range(r2)) continue;
         const uint32_t hj = __float_as_uint(pj.w);
         const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
         float2 pp = pair[pk];
@@ -391,7 +540,6 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
     const uint32_t *__restrict__ start = a.start;
     const uint32_t nt = w.n_types;
     const uint32_t ti = min(__float_as_uint(ph.w) >> 28, nt - 1u);
-    const float min2 = min_dist_sqr_f();
     const float PRUNE = 1.0001f;
     const float2 *cp = w.spatial ? (const float2 *)a.cellpair + w.cellpair_base : nullptr;
     const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
@@ -420,7 +568,7 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
                     const float4 pj = pos[j];
                     float dx, dy, dz;
                     const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-                    if (r2 < 1.0f && r2 >= min2) {
+                    if (r2 < R2_PREFILTER) {
                         if (n == cap) {
                             list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo,
                                           th_hi, scale, F, cp, hc, a.cellg, w.cell_base);
@@ -589,57 +737,41 @@ int launch_begin32(const KArgs &a, cudaStream_t s)
     return 1;
 }
 
-// Set up the brick kernel for a brick shape: opt in to the shared memory it needs and
-// return its persistent grid (resident blocks x SMs) and dynamic shared-memory bytes.
-uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair)
+// Largest staged-bead capacity of a brick for a force variant: what leaves room for two
+// blocks per SM (variants 8 and 9), within the 16-bit staged indices of the list entries.
+uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair, uint32_t home_max)
 {
-    // Variants 0 and 3 keep the neighbour direction in 5 of a list entry's 16 bits (11-bit
-    // staged index); 6 and 7 stay within the same bound, which their bricks do not reach.
-    if (variant != 8) return 2047u;
-    // Variant 8: the entry is the staged index alone; the capacity is what leaves room for
-    // two 512-thread blocks per SM.
+    if (variant != 8 && variant != 9) return 2047u;  // variant 6: its bricks stay far below
     int dev = 0, smem_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
         return 2047u;
-    const BrickLayout L = brick_layout(hc_max, 0, npair, 1, 0, BRICK_THREADS_WIDE);
+    const uint32_t hm = variant == 9 ? home_max : 0u;
+    const BrickLayout L = brick_layout(hc_max, 0, npair, brick_variant_threads(variant), hm);
+    // per staged bead: position and velocity (32 B), and for the half shell its home index
+    const int per_bead = variant == 9 ? 34 : 32;
     const int budget = smem_sm / 2 - 1024 - (int)L.bytes - 64;
-    return (uint32_t)std::max(64, std::min(65535, budget / 32));
+    return (uint32_t)std::max(64, std::min(65535, budget / per_bead));
 }
 
-int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
-                uint32_t *smem_bytes)
+// Set up the brick kernel for a brick shape: opt in to the shared memory it needs and
+// return its persistent grid (resident blocks x SMs) and dynamic shared-memory bytes.
+int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, uint32_t home_max,
+                int *grid, uint32_t *smem_bytes)
 {
     int nb = 0;
-    if (variant == 5) {
-        const CellLayout C = cell_layout(hc_max, maxb, npair);
-        cudaError_t e = cudaFuncSetAttribute(k_force32_cells<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_force32_cells<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C.bytes);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force32_cells<0>, BRICK_THREADS, C.bytes);
-        if (e != cudaSuccess) return (int)e;
-        if (nb < 1) return (int)cudaErrorInvalidConfiguration;
-        *grid = nb * sm_count;
-        *smem_bytes = C.bytes;
-        return 0;
-    }
-    const BrickLayout L = brick_layout(hc_max, maxb, npair, brick_variant_has_list(variant),
-                                       brick_variant_balanced(variant), brick_variant_threads(variant));
+    const uint32_t hm = variant == 9 ? home_max : 0u;
+    const BrickLayout L = brick_layout(hc_max, maxb, npair, brick_variant_threads(variant), hm);
     const int bytes = (int)L.bytes;
     void (*k0)(KArgs, BrickLayout) = nullptr;
     void (*k1)(KArgs, BrickLayout) = nullptr;
     switch (variant) {
-    case 0: k0 = k_force32_brick<0, 1, 0>; k1 = k_force32_brick<1, 1, 0>; break;
-    case 2: k0 = k_force32_brick<0, 0, 0>; k1 = k_force32_brick<1, 0, 0>; break;
-    case 3: k0 = k_force32_brick<0, 1, 1>; k1 = k_force32_brick<1, 1, 1>; break;
-    case 6: k0 = k_force32_brick<0, 1, 2>; k1 = k_force32_brick<1, 1, 2>; break;
-    case 7: k0 = k_force32_brick<0, 1, 3>; k1 = k_force32_brick<1, 1, 3>; break;
+    case 9: k0 = k_force32_half<0>; k1 = k_force32_half<1>; break;
     case 8:
-        k0 = k_force32_brick<0, 1, 2, BRICK_THREADS_WIDE>;
-        k1 = k_force32_brick<1, 1, 2, BRICK_THREADS_WIDE>;
+        k0 = k_force32_brick<0, BRICK_THREADS_WIDE>;
+        k1 = k_force32_brick<1, BRICK_THREADS_WIDE>;
         break;
-    default: k0 = k_force32_brick<0, 0, 1>; k1 = k_force32_brick<1, 0, 1>; break;
+    default: k0 = k_force32_brick<0, BRICK_THREADS>; k1 = k_force32_brick<1, BRICK_THREADS>; break;
     }
     cudaError_t e = cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -666,31 +798,18 @@ int launch_force32(const KArgs &a, int final_step, cudaStream_t s)
 
 static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
 {
-    if (a.force_kernel == 5 && a.n_bricks > 0) {
-        const CellLayout C = cell_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair);
-        const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
-        if (final_step)
-            k_force32_cells<1><<<grid, BRICK_THREADS, C.bytes, s>>>(a, C);
-        else
-            k_force32_cells<0><<<grid, BRICK_THREADS, C.bytes, s>>>(a, C);
-        return 1;
-    }
     if (a.force_kernel != 1 && a.n_bricks > 0) {
         const int v = a.force_kernel;
-        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair, brick_variant_has_list(v),
-                                           brick_variant_balanced(v), brick_variant_threads(v));
+        const BrickLayout L = brick_layout(a.brick_hc_max, a.brick_maxb, a.brick_npair, brick_variant_threads(v),
+                                           v == 9 ? a.brick_home_max : 0u);
         const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((uint32_t)a.brick_grid, a.n_bricks));
         void (*k)(KArgs, BrickLayout);
         switch (v) {
-        case 0: k = final_step ? k_force32_brick<1, 1, 0> : k_force32_brick<0, 1, 0>; break;
-        case 2: k = final_step ? k_force32_brick<1, 0, 0> : k_force32_brick<0, 0, 0>; break;
-        case 3: k = final_step ? k_force32_brick<1, 1, 1> : k_force32_brick<0, 1, 1>; break;
-        case 6: k = final_step ? k_force32_brick<1, 1, 2> : k_force32_brick<0, 1, 2>; break;
-        case 7: k = final_step ? k_force32_brick<1, 1, 3> : k_force32_brick<0, 1, 3>; break;
+        case 9: k = final_step ? k_force32_half<1> : k_force32_half<0>; break;
         case 8:
-            k = final_step ? k_force32_brick<1, 1, 2, BRICK_THREADS_WIDE> : k_force32_brick<0, 1, 2, BRICK_THREADS_WIDE>;
+            k = final_step ? k_force32_brick<1, BRICK_THREADS_WIDE> : k_force32_brick<0, BRICK_THREADS_WIDE>;
             break;
-        default: k = final_step ? k_force32_brick<1, 0, 1> : k_force32_brick<0, 0, 1>; break;
+        default: k = final_step ? k_force32_brick<1, BRICK_THREADS> : k_force32_brick<0, BRICK_THREADS>; break;
         }
         k<<<grid, brick_variant_threads(v), L.bytes, s>>>(a, L);
         return 1;

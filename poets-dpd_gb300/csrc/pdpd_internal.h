@@ -115,15 +115,14 @@ struct KArgs {
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
-    int force_kernel;    // FP32: 6 = brick kernel, neighbour lists, row walk (8: the same with
-                         // 512-thread blocks, the default);
-                         // 0 = as 6 with a cell walk, 2 = brick kernel without lists,
-                         // 3 / 4 = flat walk, 5 = warp per cell, 7 = as 6, balanced lists,
-                         // 8 = as 6 with 512-thread blocks, 1 = thread per bead (global)
+    int force_kernel;    // FP32: 9 = half-shell brick kernel (Newton's third law inside a
+                         // brick), 8 = full-shell brick kernel with 512-thread blocks, 6 = the
+                         // same with 128-thread blocks, 1 = thread per bead (global memory)
     int brick_grid;      // persistent grid size of the brick kernel
     uint32_t brick_hc_max;  // halo cells of the nominal brick shape
     uint32_t brick_maxb;    // staged-bead capacity of one brick
     uint32_t brick_npair;   // staged pair-table entries: the largest n_types^2 of the worlds
+    uint32_t brick_home_max;  // half shell: home-bead capacity of one brick
     uint32_t *brick_next;   // FP32: the brick queue's next free entry beyond the first
                             // gridDim.x (zeroed by the sort, which precedes every force pass)
 };
@@ -153,11 +152,11 @@ int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uin
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
 
 size_t payload_bytes(int fp64);  // bytes of one pos / vel / frc element
-// Largest staged-bead capacity of a brick for force variant `variant` (the list entries'
-// index range, and for variant 8 two blocks per SM of shared memory).
-uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair);
-int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, int *grid,
-                uint32_t *smem_bytes);  // 0 or a cudaError_t
+// Largest staged-bead capacity of a brick for force variant `variant` (two blocks per SM of
+// shared memory for variants 8 and 9, the list entries' range for 6).
+uint32_t brick_maxb_limit(int variant, uint32_t hc_max, uint32_t npair, uint32_t home_max);
+int brick_setup(int sm_count, int variant, uint32_t hc_max, uint32_t maxb, uint32_t npair, uint32_t home_max,
+                int *grid, uint32_t *smem_bytes);  // 0 or a cudaError_t
 uint32_t scan_blocks(uint32_t n_cells);
 
 // Observables of one world (pdpd_observe.cu): per-block FP64 partial sums.

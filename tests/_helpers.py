@@ -65,6 +65,42 @@ def force_rel_err(f, f_ref):
     return float(np.max(np.linalg.norm(f - f_ref, axis=1)) / scale)
 
 
+# Worst-case error of one pair's separation in the FP32 engine after one step: each stored
+# position offset (in [0, 1)) is rounded to FP32 at attach and again by update_pos, <= 2^-25
+# each per axis, and the separation is rounded once (<= 2^-24 of a value below 1), so per axis
+# <= 3 * 2^-24 and over three axes <= sqrt(3) * 3 * 2^-24 < 2^-21.
+FP32_SEP_ERR = 2.0 ** -21
+
+
+def fp32_force_check(world, x, v, f, f_ref, tol=1e-5, r_close=0.01, slack=10.0):
+    """One-step FP32 forces against FP64 ones: every bead within tol * rms|f_ref|, except a
+    bead with a pair closer than r_close, whose unit vector the FP32 storage of positions
+    alone turns by up to FP32_SEP_ERR / r.  Such a bead may reach slack * tol * rms|f_ref|,
+    and no more than the storage error carried through its close pairs: the sum over them of
+    F_max (4 / r + 2) FP32_SEP_ERR, where F_max = a_max + gamma_max (|v_i - v_j| + 1) +
+    sqrt(gamma_max) sqrt(24 / dt) / 2 bounds the pair force and its r-derivative / 2.  Such
+    beads must also be rare: at most 1e-5 of the beads + 2.  x, v: the positions the forces
+    were evaluated at and the velocities (FP64 run).  Returns (max error / rms, beads above
+    tol)."""
+    scale = np.sqrt(np.mean(np.sum(f_ref * f_ref, axis=1)))
+    err = np.linalg.norm(f - f_ref, axis=1)
+    bad = np.nonzero(err > tol * scale)[0]
+    assert len(bad) <= 1e-5 * len(err) + 2, f"{len(bad)} beads above {tol:g} of rms|f|"
+    a_max, g_max = float(world.conservative.max()), float(world.dissipative.max())
+    rand = np.sqrt(g_max) * np.sqrt(24.0 / world.dt) / 2
+    L = np.asarray(world.box, float)
+    for i in bad:
+        d = x - x[i]
+        d -= L * np.round(d / L)
+        r = np.linalg.norm(d, axis=1)
+        m = (r < r_close) & (r > 0.0)
+        assert m.any(), (int(i), float(err[i] / scale), "no pair closer than", r_close)
+        f_max = a_max + g_max * (np.linalg.norm(v[m] - v[i], axis=1) + 1.0) + rand
+        bound = min(slack * tol * scale, np.sum(f_max * (4.0 / r[m] + 2.0)) * FP32_SEP_ERR)
+        assert err[i] <= bound, (int(i), float(err[i]), float(bound), float(r[m].min()))
+    return float(err.max() / scale) if err.size else 0.0, len(bad)
+
+
 def load_testbase():
     """The reference's TestBase suite as replayable segments (tests/golden/testbase_suite.npz):
     a list of (name, world, [(todo, t_in, state_in (n,9), t_out, state_out (n,9)), ...]) where a

@@ -17,7 +17,7 @@ import pytest
 import oracle as O
 import pdpd_engine as E
 import pdpd_world as W
-from _helpers import (force_rel_err, load_hash_kat, load_world_fixture, periodic_dx,
+from _helpers import (force_rel_err, fp32_force_check, load_hash_kat, load_world_fixture, periodic_dx,
                       world_fixture_names)
 
 pytestmark = pytest.mark.gpu
@@ -90,22 +90,53 @@ def test_fp64_bit_exact_vs_oracle_polymer_box(L, steps):
         assert np.array_equal(world.f, ow.f)
 
 
-def test_fp64_bit_exact_large_box_one_step():
-    """128^3 box, 5% chains (6,291,456 beads): one FP64 step equals the oracle's bit for bit."""
+@pytest.fixture(scope="module")
+def large_box_one_step():
+    """The 128^3 polymer box of the HBM-roofline configuration (5% chains, seed 3; 6,291,456
+    beads) and the oracle's state after one FP64 step from it (computed once for the FP64
+    and FP32 tests)."""
     world = W.make_polymer_box(128, chain_fraction=0.05, seed=3)
     ow = O.OracleWorld(world)
+    ow.run(1, nthreads=16)
+    return world, ow
+
+
+def test_fp64_bit_exact_large_box_one_step(large_box_one_step):
+    """128^3 box, 5% chains (6,291,456 beads): one FP64 step equals the oracle's bit for bit."""
+    world0, ow = large_box_one_step
+    world = world0.copy()
     eng = E.GB300DPDEngine("fp64")
     eng.Attach(world)
     eng.Run(1)
-    ow.run(1, nthreads=16)
     assert np.array_equal(world.f, ow.f)
     assert np.array_equal(world.x, ow.x)
     assert np.array_equal(world.v, ow.v)
 
 
+@pytest.mark.parametrize("force_kernel", [8, 9])
+def test_fp32_large_box_one_step_force_error(large_box_one_step, force_kernel):
+    """The HBM-roofline configuration itself (128^3, 6,291,456 beads from uniform random
+    positions): one FP32 step against the oracle's FP64 step, |f_i - f_ref_i| <= 1e-5
+    rms|f_ref| for every bead but the few with a pair closer than 0.01 (on this machine: chain
+    beads i and i + 2 folded back onto each other, r ~ 0.004), whose force the FP32 storage of
+    positions (2^-25 per offset) moves by ~1e-3; those are held to the propagated storage
+    error, at most 10x the tolerance, and must be rare (fp32_force_check).  Positions within
+    1e-6."""
+    world0, ow = large_box_one_step
+    world = world0.copy()
+    eng = E.GB300DPDEngine("fp32")
+    eng.SetConfigEntry("force_kernel", force_kernel)
+    eng.Attach(world)
+    eng.Run(1)
+    err, n_close = fp32_force_check(world0, ow.x, ow.v, world.f, ow.f, FP32_FORCE_TOL)
+    print(f"128^3 one-step FP32 force error {err:.3e} of rms|f|; {n_close} beads above 1e-5 "
+          f"(close pairs)")
+    assert np.max(np.abs(periodic_dx(world.x, ow.x, world.box))) < 1e-6
+
+
 # ---------------------------------------------------------------------------- FP32
 
-@pytest.mark.parametrize("force_kernel", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("force_kernel", [1, 6, 8, 9])
 @pytest.mark.parametrize("name", [n for n in world_fixture_names() if n != "empty_world"])
 def test_fp32_vs_reference(name, force_kernel):
     world, ref = load_world_fixture(name)
@@ -120,7 +151,7 @@ def test_fp32_vs_reference(name, force_kernel):
     assert np.max(np.abs(dx)) < 1e-6
 
 
-@pytest.mark.parametrize("force_kernel", [0, 1, 5, 6, 7, 8])
+@pytest.mark.parametrize("force_kernel", [1, 6, 8, 9])
 def test_fp32_polymer_box_one_and_ten_steps(force_kernel):
     world = W.make_polymer_box(32, chain_fraction=0.1, seed=2)
     ow = O.OracleWorld(world)
@@ -242,27 +273,26 @@ def test_batch_with_an_empty_world(prec):
 
 
 LAUNCH_CONFIGS = {
-    # Every FP32 force kernel (shared-memory brick with or without neighbour lists, any brick
-    # shape; thread per bead from global memory) adds the same pair terms in the same order
-    # with the same roundings, so all of them give bit-identical trajectories.
+    # Every full-shell FP32 force kernel (shared-memory brick, any brick shape; thread per bead
+    # from global memory) adds the same pair terms in the same order with the same roundings,
+    # so all of them give bit-identical trajectories.
     "fp32": ({}, {"use_graphs": 0}, {"grid_blocks": 3}, {"graph_steps": 5},
-             {"force_kernel": 2}, {"force_kernel": 1}, {"force_kernel": 1, "list_capacity": 1},
-             {"list_capacity": 1}, {"list_capacity": 3, "force_kernel": 0},
+             {"force_kernel": 1}, {"force_kernel": 1, "list_capacity": 1},
+             {"list_capacity": 1}, {"list_capacity": 3, "force_kernel": 6},
              {"brick_x": 2, "brick_y": 2, "brick_z": 2}, {"brick_x": 8, "brick_y": 4, "brick_z": 8},
-             {"brick_x": 3, "brick_y": 5, "brick_z": 7, "force_kernel": 2},
-             {"force_kernel": 3}, {"force_kernel": 4}, {"force_kernel": 3, "list_capacity": 2},
-             {"force_kernel": 4, "brick_x": 2, "brick_y": 3, "brick_z": 8},
              {"force_kernel": 6}, {"force_kernel": 6, "list_capacity": 2},
              {"force_kernel": 6, "brick_x": 3, "brick_y": 5, "brick_z": 7},
-             {"force_kernel": 7}, {"force_kernel": 7, "list_capacity": 2},
-             {"force_kernel": 7, "brick_x": 4, "brick_y": 4, "brick_z": 8},
              {"force_kernel": 8}, {"force_kernel": 8, "brick_x": 4, "brick_y": 8, "brick_z": 8},
              {"force_kernel": 8, "list_capacity": 3, "brick_x": 3, "brick_y": 5, "brick_z": 7}),
-    # The warp-per-cell kernel sums each bead's pairs in a different (but data-determined)
-    # order: deterministic and independent of the launch configuration.
-    "fp32_cells": ({"force_kernel": 5}, {"force_kernel": 5, "use_graphs": 0},
-                   {"force_kernel": 5, "grid_blocks": 3},
-                   {"force_kernel": 5, "brick_x": 2, "brick_y": 4, "brick_z": 8}),
+    # The half-shell kernel sums each bead's pair forces in fixed point (integer sums: any
+    # order), so its trajectory is the same whatever its brick shape, grid or graph use.
+    "fp32_half": ({"force_kernel": 9}, {"force_kernel": 9, "grid_blocks": 3},
+                  {"force_kernel": 9, "use_graphs": 0}, {"force_kernel": 9, "graph_steps": 5},
+                  {"force_kernel": 9, "brick_x": 4, "brick_y": 8, "brick_z": 8},
+                  {"force_kernel": 9, "brick_x": 3, "brick_y": 5, "brick_z": 7},
+                  {"force_kernel": 9, "brick_x": 1, "brick_y": 1, "brick_z": 1},
+                  {"force_kernel": 9, "brick_y": 1, "brick_x": 12, "brick_z": 12},
+                  {"force_kernel": 9, "brick_x": 2, "brick_y": 2, "brick_z": 12}),
     "fp64": ({}, {"use_graphs": 0}, {"list_capacity": 1}, {"list_capacity": 5, "grid_blocks": 3},
              {"graph_steps": 5}),
 }
@@ -283,7 +313,7 @@ def test_autotune_and_mid_run_reconfiguration_keep_the_trajectory():
     e2.Run(65)  # the autotuner's warm-up and trials take the first 49 steps
     cfg = {n: v for n, _, v in e2.GetConfigEntries()}
     assert "trials" in cfg["autotune"]
-    e2.SetConfigEntry("force_kernel", 2)
+    e2.SetConfigEntry("force_kernel", 6 if cfg["force_kernel"] != "6" else 8)
     e2.SetConfigEntry("brick_z", 8)
     e2.Run(15)
     assert w.t == ref.t == 80
@@ -301,7 +331,7 @@ def clustered_world():
     return w
 
 
-@pytest.mark.parametrize("force_kernel", [0, 2, 3, 4, 6, 7, 8])
+@pytest.mark.parametrize("force_kernel", [6, 8])
 def test_fp32_brick_overflow_fallback(force_kernel):
     world = clustered_world()
     ref = world.copy()

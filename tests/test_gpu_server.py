@@ -135,7 +135,7 @@ def test_server_failing_job_does_not_disturb_the_others(prec):
 
 def test_server_config_only_when_idle():
     srv = E.GB300DPDServer("fp32")
-    srv.config("force_kernel", 2)
+    srv.config("force_kernel", 6)
     w = W.make_water(8, seed=3, gen_seed=33)
     j = srv.submit(w, 30)
     srv.drain()

@@ -42,7 +42,7 @@ def test_fp64_spatial_bit_exact_vs_oracle_and_close_to_half_merge(name):
 
 
 @pytest.mark.parametrize("name", merge_fixture_names("spatial"))
-@pytest.mark.parametrize("configured", [6, 0])
+@pytest.mark.parametrize("configured", [6, 9])
 def test_fp32_spatial(name, configured):
     """The FP32 engine runs spatial worlds on the thread-per-bead kernel whatever kernel is
     configured; forces within the FP32 tolerance, trajectories identical across configs."""

@@ -47,7 +47,7 @@ def test_fp64_stationary_bit_exact_vs_oracle_and_close_to_half_merge(name):
 
 
 @pytest.mark.parametrize("name", merge_fixture_names("stationary"))
-@pytest.mark.parametrize("force_kernel", [6, 0, 1])
+@pytest.mark.parametrize("force_kernel", [6, 8, 9, 1])
 def test_fp32_stationary(name, force_kernel):
     world, ref = load_world_fixture(name)
     st = np.asarray(world.stationary, bool)[world.bead_type]
