@@ -477,6 +477,12 @@ def kernel_config(eng):
             if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
 
 
+def fixed_kernel(eng, args):
+    """--force-kernel K: run FP32 force kernel K (no autotuning), for profiling a variant."""
+    if args.force_kernel:
+        eng.SetConfigEntry("force_kernel", args.force_kernel)
+
+
 def tune(eng, attach, steps=64):
     """Autotune once (its trials are ordinary steps: the trajectory does not depend on the
     choice), then keep the chosen kernel and brick shape fixed."""
@@ -528,7 +534,9 @@ def measure_grid(args, dev, local, world_size):
     worlds = W.make_batched_grid(GRID_STATES, count=n_states)
     total = sum(w.n_beads for w in worlds)
     eng = E.GB300DPDEngine("fp32", device=local)
-    tuned = tune(eng, lambda: eng.AttachBatch([w.copy() for w in worlds])) if args.autotune else None
+    fixed_kernel(eng, args)
+    tuned = (tune(eng, lambda: eng.AttachBatch([w.copy() for w in worlds]))
+             if args.autotune and not args.force_kernel else None)
     # e2e: AttachBatch (upload) + Run(K) + read-back of every state, host buffers
     eng.AttachBatch([w.copy() for w in worlds])
     eng.Run(args.warmup)
@@ -567,7 +575,10 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
     world = make_world(name, side=side)
     n = world.n_beads
     eng = E.GB300DPDEngine(precision, device=local)
-    tuned = tune(eng, lambda: eng.Attach(world.copy())) if precision == "fp32" and autotune else None
+    if precision == "fp32":
+        fixed_kernel(eng, args)
+    tuned = (tune(eng, lambda: eng.Attach(world.copy()))
+             if precision == "fp32" and autotune and not args.force_kernel else None)
     # e2e: through the C ABI with host buffers (Attach = upload, Run, read-back)
     eng.Attach(world.copy())
     eng.Run(args.warmup)
@@ -698,6 +709,8 @@ def main():
                     help="skip the 128^3 single-box run beside the grid")
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: autotune the FP32 force kernel first (default); 0: default kernel")
+    ap.add_argument("--force-kernel", type=int, default=0,
+                    help="FP32 force kernel variant to run instead of autotuning (1, 6, 8, 9)")
     ap.add_argument("--serving-window", type=float, default=4.0,
                     help="seconds of Poisson arrivals of the serving stream (0 skips it)")
     ap.add_argument("--grid-states", type=int, default=GRID_STATES,
