@@ -83,7 +83,11 @@ typedef struct pdpd_timings {
 typedef struct pdpd_engine pdpd_engine;
 
 /* Interval callback for pdpd_run_intervals: called on the caller's thread after the
- * interval's state has been written to the host arrays.  Return nonzero to continue. */
+ * interval's state has been written to the host arrays.  Return nonzero to continue.  The
+ * state is a snapshot for reading: the next interval is already running on the device from
+ * the state as reported, so edits to the host arrays do not reach the engine (and are
+ * overwritten by the next interval's write).  A caller that changes beads between intervals
+ * stops (returns 0), edits, re-attaches and runs again. */
 typedef int (*pdpd_interval_fn)(void *user, int64_t t);
 
 /* Create/destroy an engine (DPDEngineFactory::create, dpd_engine.hpp:244-252).

@@ -198,6 +198,11 @@ public:
         read_back();
     }
 
+    // The callback sees each interval's state in the beads while the device already runs the
+    // next interval from that state: it must treat the beads as read-only (an edit does not
+    // reach the engine and is overwritten by the next interval's write-back).  The reference's
+    // engines run the callback between intervals, where an edit would take effect; a caller
+    // that edits returns false, edits, and calls Attach and Run again.
     unsigned Run(int interval_count, unsigned interval_size,
                  std::function<bool()> interval_callback) override
     {
