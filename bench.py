@@ -21,8 +21,14 @@ grid's bead payload (~1 GB) is larger than L2, so no flush is needed.
             measured HBM copy bandwidth.
   roofline_run  the 128^3 box (6,291,456 beads, same chain recipe, a_WT = 75, gamma = 4.5):
             value, e2e, roofline and phases of the single large state.
-  serving   the served stream (Poisson arrivals, continuous batching): p50/p99 latency and
-            served bead-steps/s against sequential execution.
+  serving   the served stream (Poisson arrivals at 50 jobs/s for 20 s, continuous batching):
+            p50/p99 latency, served bead-steps/s over the whole run and at steady state (while
+            the stream arrives, after a 2 s ramp; with the fractions of that time the GPU
+            stepped and the host re-packed), served / offered, and against sequential
+            execution.  The offered load exceeds the server's capacity, so a queue builds and
+            the latencies measure it.
+  serving_light  the same job mix at 20 jobs/s for 10 s, below capacity: latency without a
+            standing queue.
   cpu_baseline  the oracle (C restatement of the reference's FP64 half-step engine) on all
             host cores, on a bounded sample of the same workload, with the host's CPU and,
             beside it, the reference's own TBB engine's expected rate: the port's rate times
@@ -303,7 +309,13 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
 
     th = threading.Thread(target=client)
     th.start()
-    th.join()
+    # the server's counters every 0.25 s while the stream arrives (steady_state)
+    samples = []
+    while th.is_alive():
+        s_ = srv.stats()
+        samples.append((time.perf_counter() - t0, s_["bead_steps"] - st0["bead_steps"],
+                        s_["step_s"] - st0["step_s"], s_["repack_s"] - st0["repack_s"]))
+        th.join(0.25)
     srv.drain()
     wall = time.perf_counter() - t0
     st = srv.stats()
@@ -330,13 +342,16 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
         eng.close()
         return bs / secs, count
 
-    seq32, n32 = sequential("fp32", seq_fp32)
-    seq64, n64 = sequential("fp64", seq_fp64)
+    seq32, n32 = sequential("fp32", seq_fp32) if seq_fp32 else (None, 0)
+    seq64, n64 = sequential("fp64", seq_fp64) if seq_fp64 else (None, 0)
+    steady = steady_state(samples, ramp_s=min(2.0, window_s / 4), end_s=window_s)
+    offered = total_bs / window_s
     return {"workload": f"Poisson {rate:g} jobs/s for {window_s:g} s ({len(worlds)} jobs), water "
                         f"sides log-uniform 8..64, n_steps U{{100..2000}}, callback every "
                         f"{interval} steps, {budget / 2**30:g} GiB budget",
-            "jobs": len(worlds), "offered_bead_steps_per_s": total_bs / window_s,
-            "served_bead_steps_per_s": served, "wall_s": wall,
+            "jobs": len(worlds), "offered_bead_steps_per_s": offered,
+            "served_bead_steps_per_s": served, "served_over_offered": served / offered,
+            "steady_state": steady, "wall_s": wall,
             "latency_p50_s": st["latency_p50_s"], "latency_p99_s": st["latency_p99_s"],
             "latency_max_s": st["latency_max_s"], "max_active_jobs": st["max_active"],
             "repacks": st["repacks"] - st0["repacks"],
@@ -346,7 +361,25 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,
-            "served_vs_sequential_fp32": served / seq32, "served_vs_sequential_fp64": served / seq64}
+            "served_vs_sequential_fp32": served / seq32 if seq32 else None,
+            "served_vs_sequential_fp64": served / seq64 if seq64 else None,
+            "steady_vs_sequential_fp32": steady["served_bead_steps_per_s"] / seq32
+            if seq32 and steady else None}
+
+
+def steady_state(samples, ramp_s, end_s):
+    """Served rate while the stream arrives, after the ramp: from the server's counters sampled
+    over time, (t, bead_steps, step_s, repack_s), the slope between the first sample at or
+    after ramp_s and the last at or before end_s, and the fractions of that wall time the GPU
+    spent stepping (device time of the epochs) and the host spent re-packing."""
+    win = [x for x in samples if ramp_s <= x[0] <= end_s]
+    if len(win) < 2 or win[-1][0] <= win[0][0]:
+        return None
+    (t_a, b_a, s_a, r_a), (t_b, b_b, s_b, r_b) = win[0], win[-1]
+    dt = t_b - t_a
+    return {"from_s": t_a, "to_s": t_b, "served_bead_steps_per_s": (b_b - b_a) / dt,
+            "step_frac": (s_b - s_a) / dt, "repack_frac": (r_b - r_a) / dt,
+            "bead_steps_per_step_s": (b_b - b_a) / (s_b - s_a) if s_b > s_a else None}
 
 
 def dist_setup(n_gpus):
@@ -644,9 +677,13 @@ def run_engine_arm(args):
         main = measure_box(args, args.workload, args.side, args.precision, dev, local, world_size,
                            args.autotune)
         side = None
-    serving = None
+    serving = serving_light = None
     if args.serving_window > 0 and world_size == 1:
         serving = serving_metrics(window_s=args.serving_window, device=local)
+    if args.serving_light_rate > 0 and args.serving_window > 0 and world_size == 1:
+        # the same job mix offered below the server's capacity: latency without a standing queue
+        serving_light = serving_metrics(rate=args.serving_light_rate, window_s=args.serving_light_window,
+                                        seed=6, device=local, seq_fp32=0, seq_fp64=0)
     if rank != 0:
         return
     cpu = None
@@ -676,6 +713,7 @@ def run_engine_arm(args):
         "cpu_baseline": cpu,
         "plain_fp64": main.get("plain_fp64"),
         "serving": serving,
+        "serving_light": serving_light,
         "roofline_run": None if side is None else {
             "workload": side["config"]["workload"], "value": side["value"],
             "ms_per_step": side["ms"] / args.steps, "e2e": side["e2e"],
@@ -711,8 +749,12 @@ def main():
                     help="1: autotune the FP32 force kernel first (default); 0: default kernel")
     ap.add_argument("--force-kernel", type=int, default=0,
                     help="FP32 force kernel variant to run instead of autotuning (1, 6, 8, 9)")
-    ap.add_argument("--serving-window", type=float, default=4.0,
+    ap.add_argument("--serving-window", type=float, default=20.0,
                     help="seconds of Poisson arrivals of the serving stream (0 skips it)")
+    ap.add_argument("--serving-light-rate", type=float, default=20.0,
+                    help="jobs/s of a second stream below capacity (0 skips it)")
+    ap.add_argument("--serving-light-window", type=float, default=10.0,
+                    help="seconds of Poisson arrivals of the stream below capacity")
     ap.add_argument("--grid-states", type=int, default=GRID_STATES,
                     help="run the grid's first N states only (profiling on a smaller grid)")
     ap.add_argument("--side", type=int, default=None,

@@ -45,3 +45,16 @@ def test_force_roofline_arithmetic():
 def test_grid_workload_name_names_the_grid():
     assert bench.grid_workload_name(512).startswith("batched512: 512 polymer-solvent states")
     assert "(its first 64)" in bench.grid_workload_name(64)
+
+
+def test_steady_state_slope_of_the_server_counters():
+    # (t, bead_steps, step_s, repack_s): 4e9 bead-steps/s from t = 2 on, the GPU stepping 90%
+    # of the time and re-packing 2%; the ramp before t = 2 is left out
+    samples = [(0.5 * k, (0 if k < 4 else 4e9 * (0.5 * k - 2.0)) + 1e6 * min(k, 4),
+                0.45 * k, 0.01 * k) for k in range(41)]
+    st = bench.steady_state(samples, ramp_s=2.0, end_s=15.0)
+    assert st["from_s"] == 2.0 and st["to_s"] == 15.0
+    assert st["served_bead_steps_per_s"] == pytest.approx(4e9)
+    assert st["step_frac"] == pytest.approx(0.9)
+    assert st["repack_frac"] == pytest.approx(0.02)
+    assert bench.steady_state(samples[:3], ramp_s=2.0, end_s=15.0) is None
