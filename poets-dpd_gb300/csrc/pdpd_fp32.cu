@@ -204,10 +204,15 @@ __device__ __forceinline__ float slab_gap(float o, int d)
 }
 
 // Separation of a neighbour bead pj from a home position already shifted by the neighbour
-// cell's direction (a = o_home - dir), and its square: the neighbour walks' cheap prefilter.
-// A walk keeps a candidate when this r^2 is below R2_PREFILTER; the evaluation decides with
-// the exact test on pair_sep's r^2, which differs from this one by at most a few units in the
-// last place (|dr^2| < 4e-6), so no pair in range is lost.
+// cell's direction (a = o_home - dir), and its square.  The full-shell paths (the brick
+// kernels 6 and 8, their fallback and the thread-per-bead kernel) test and evaluate every pair
+// with this separation and pair_accumulate, with explicit roundings, so they give
+// bit-identical forces.  For a pair close across a face in the -1 direction, o_home + 1 is
+// rounded to 2^-24 (6e-8 absolute), about twice the rounding of the stored offsets themselves.
+// The half shell needs an exactly antisymmetric separation and uses pair_sep; its walk keeps
+// a candidate when this r^2 is below R2_PREFILTER, and the evaluation decides with the exact
+// test on pair_sep's r^2, which differs from this one by at most a few units in the last
+// place (|dr^2| < 4e-6), so no pair in range is lost.
 constexpr float R2_PREFILTER = 1.0f + 0x1p-17f;
 
 __device__ __forceinline__ float pair_r2(float ax, float ay, float az, const float4 pj, float &dx,
@@ -243,7 +248,7 @@ __device__ __forceinline__ void pair_accumulate(float dx, float dy, float dz, fl
 }
 
 // Separation of the pair (i, j), d = cell_j - cell_i, per axis (o_i - [d > 0]) - (o_j - [d < 0]),
-// and its square: the separation every pair force is evaluated with.  When the pair is close
+// and its square: the separation the half shell evaluates a pair with.  When the pair is close
 // across a cell face the offset next to the face is >= 0.5, so its shift by one cell is exact
 // and the separation carries one rounding relative to its own (small) size -- the unit vector
 // keeps FP32 precision however close the beads are (o_i - d - o_j in the other order loses
@@ -436,19 +441,23 @@ __device__ void pair_forces32_seq(const KArgs &a, const WorldDev &w, const float
     const uint32_t nt = w.n_types;
     const uint32_t hi = __float_as_uint(ph.w);
     const uint32_t ti = min(hi >> 28, nt - 1u);
+    const float min2 = min_dist_sqr_f();
     for (int ddx = -1; ddx <= 1; ddx++) {
         const int nx = wrap_index(c[0] + ddx, w.L[0]);
+        const float ax = __fsub_rn(ph.x, (float)ddx);
         for (int ddy = -1; ddy <= 1; ddy++) {
             const int ny = wrap_index(c[1] + ddy, w.L[1]);
+            const float ay = __fsub_rn(ph.y, (float)ddy);
             const uint32_t row = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2];
             for (int ddz = -1; ddz <= 1; ddz++) {
+                const float az = __fsub_rn(ph.z, (float)ddz);
                 const uint32_t nc = row + (uint32_t)wrap_index(c[2] + ddz, w.L[2]);
                 const uint32_t j1 = a.start[nc + 1];
                 for (uint32_t j = a.start[nc]; j < j1; j++) {
                     const float4 pj = pos[j];
                     float dx, dy, dz;
-                    const float r2 = pair_sep(ph, pj, ddx, ddy, ddz, dx, dy, dz);
-                    if (pair_in_range(r2)) {
+                    const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                    if (r2 < 1.0f && r2 >= min2) {
                         const uint32_t hj = __float_as_uint(pj.w);
                         pair_accumulate(dx, dy, dz, r2, vh, vel[j], hi, hj,
                                         pair[ti * nt + min(hj >> 28, nt - 1u)], th_lo, th_hi,
@@ -509,10 +518,11 @@ __device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
         const uint32_t j = s_j[k * TILE_BEADS + threadIdx.x];
         const uint32_t d = s_dir[k * TILE_BEADS + threadIdx.x];
         const float4 pj = pos[j];
+        const float ax = __fsub_rn(ph.x, (float)((int)(d & 3u) - 1));
+        const float ay = __fsub_rn(ph.y, (float)((int)((d >> 2) & 3u) - 1));
+        const float az = __fsub_rn(ph.z, (float)((int)((d >> 4) & 3u) - 1));
         float dx, dy, dz;
-        const float r2 = pair_sep(ph, pj, (int)(d & 3u) - 1, (int)((d >> 2) & 3u) - 1, (int)((d >> 4) & 3u) - 1,
-                                  dx, dy, dz);
-        if (!pair_in_range(r2)) continue;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
         const uint32_t hj = __float_as_uint(pj.w);
         const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
         float2 pp = pair[pk];
@@ -540,6 +550,7 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
     const uint32_t *__restrict__ start = a.start;
     const uint32_t nt = w.n_types;
     const uint32_t ti = min(__float_as_uint(ph.w) >> 28, nt - 1u);
+    const float min2 = min_dist_sqr_f();
     const float PRUNE = 1.0001f;
     const float2 *cp = w.spatial ? (const float2 *)a.cellpair + w.cellpair_base : nullptr;
     const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
@@ -568,7 +579,7 @@ __device__ __forceinline__ void pair_forces32(const KArgs &a, const WorldDev &w,
                     const float4 pj = pos[j];
                     float dx, dy, dz;
                     const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
-                    if (r2 < R2_PREFILTER) {
+                    if (r2 < 1.0f && r2 >= min2) {
                         if (n == cap) {
                             list_forces32(pos, vel, s_j, s_dir, n, ph, vh, ti, nt, pair, th_lo,
                                           th_hi, scale, F, cp, hc, a.cellg, w.cell_base);

@@ -129,8 +129,9 @@ __device__ __forceinline__ int home_row_of(const uint32_t *rows, int nr, uint32_
 }
 
 // Evaluate list entries [0, n) of this thread in order, adding to F (variants 6 and 8): an
-// entry is a staged index, and the neighbour direction is the difference of the two beads'
-// staged halo cells (vi is the home bead's staged velocity).
+// entry is a staged index of an in-range neighbour, and the neighbour direction is the
+// difference of the two beads' staged halo cells (vi is the home bead's staged velocity); the
+// separation is recomputed exactly as the walk computed it.
 template <int T>
 __device__ __forceinline__ void brick_rows_eval(const float4 *__restrict__ spos,
                                                 const float4 *__restrict__ svel,
@@ -148,10 +149,11 @@ __device__ __forceinline__ void brick_rows_eval(const float4 *__restrict__ spos,
         const float4 pj = spos[j];
         const float4 vj = svel[j];
         const uint32_t cj = staged_cell(vj);
+        const float ax = __fsub_rn(pi.x, (float)((int)(cj & 255u) - hx));
+        const float ay = __fsub_rn(pi.y, (float)((int)((cj >> 8) & 255u) - hy));
+        const float az = __fsub_rn(pi.z, (float)((int)(cj >> 16) - hz));
         float dx, dy, dz;
-        const float r2 = pair_sep(pi, pj, (int)(cj & 255u) - hx, (int)((cj >> 8) & 255u) - hy, (int)(cj >> 16) - hz,
-                                  dx, dy, dz);
-        if (!pair_in_range(r2)) continue;
+        const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
         const uint32_t hj = __float_as_uint(pj.w);
         pair_accumulate(dx, dy, dz, r2, vi, vj, hi, hj, pair[ti * nt + min(hj >> 28, nt - 1u)],
                         th_lo, th_hi, scale, F);
@@ -300,7 +302,8 @@ __device__ __forceinline__ void brick_halo_and_stage(const KArgs &a, const World
 // at its ends by the same conservative test as the per-cell loop (and by the far z half of an
 // end cell: a cell's beads with z offset < 0.5 come first, hlo counts them).  The warp pays the
 // longest row of its lanes 9 times instead of the longest cell 27 times.  The in-range
-// candidates go to this thread's list, as staged indices, in the direction order; room for a
+// candidates (the reference's test, update_bead_pair, on the walk's separation) go to this
+// thread's list, as staged indices, in the direction order; room for a
 // whole row is made before the row (the list is evaluated into F first when it could
 // overflow), so the candidate loop has no capacity check and no branch.  Returns the number
 // of entries left in the list.
@@ -316,6 +319,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                                                   float F[3])
 {
     const float PRUNE = 1.0001f;
+    const float min2 = min_dist_sqr_f();
     const float azm = __fsub_rn(pi.z, -1.0f), azp = __fsub_rn(pi.z, 1.0f);
     const float gzm = pi.z, gzp = 1.0f - pi.z;
     // gaps to the far halves of the end cells: the lower half of the cell below (z offsets
@@ -346,7 +350,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
                 list[n * T + threadIdx.x] = (uint16_t)j;
-                n += r2 < R2_PREFILTER ? 1 : 0;
+                n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
             }
         } else {
             for (uint32_t j = j0; j < j1; j++) {
@@ -355,7 +359,7 @@ __device__ __forceinline__ int brick_rows_collect(const float4 *__restrict__ spo
                 float dx, dy, dz;
                 const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
                 list[n * T + threadIdx.x] = (uint16_t)j;
-                n += r2 < R2_PREFILTER ? 1 : 0;
+                n += (r2 < 1.0f && r2 >= min2) ? 1 : 0;
                 if (n == cap) {
                     brick_rows_eval<T>(spos, svel, list, n, pi, vi, pair, nt, th_lo, th_hi, scale, F);
                     n = 0;
