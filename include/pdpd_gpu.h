@@ -205,6 +205,39 @@ int pdpd_observe(pdpd_engine *e, uint32_t world, pdpd_observables *out, uint32_t
 int pdpd_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
                   const uint32_t *b, uint32_t *h_out, float *u_out);
 
+/* Per-pair force log, the counterpart of the reference's ForceLogging (logging.hpp:9-100) as
+ * its half-step engine feeds it from calc_force (dpd_maths_core_half_step.hpp:131-153,
+ * naive_dpd_engine_half_step.hpp:239-263): one record per in-range pair (home, other) whose
+ * home bead was asked for, with the names the reference logs the values under.  The FP64
+ * engine records the very values its force pass uses (bit-identical to the reference's);
+ * the FP32 engine records its own FP32 values, f being the pair's contribution exactly as
+ * its force kernels add it. */
+typedef struct pdpd_pair_terms {
+    int64_t t;                       /* the step's time: the state's t before the step */
+    uint32_t home_id, other_id;      /* bead ids within the world */
+    uint32_t home_hash, other_hash;  /* BeadHash codes (the reference's FileLogger prints
+                                        reduced hashes: hash & 0x0fffffff) */
+    double dx[3];       /* "dx": home - other, periodic image applied, not normalised */
+    double dr;          /* "dr" */
+    double inv_root_dt; /* "dpd-invrootdt": sqrt(24 kT / dt) */
+    double gammap;      /* "dpd-gammap": (sqrt(gamma_ij) (1 - dr))^2 */
+    double rng;         /* "dpd-rng": default_hash of the pair, in [-0.5, 0.5) */
+    double con;         /* "dpd-con" */
+    double diss;        /* "dpd-diss" */
+    double rng_scale;   /* "dpd-rng-scale" */
+    double rand;        /* "dpd-rand" */
+    double f[3];        /* "f_next_dpd": the pair's force on the home bead */
+} pdpd_pair_terms;
+
+/* Advance the attached world(s) by one step, as pdpd_run(e, 1) does, recording the pair
+ * terms of that step for the n_ids beads bead_ids[] (ids within world `world`; duplicates
+ * are ignored).  Records are grouped by bead in ascending id order, each bead's pairs in the
+ * reference's walk order (27 directions, (-1..1)^3 with z fastest, then the cell's beads in
+ * id order).  The first min(total, capacity) records go to out; *n_pairs receives the total.
+ * A debugging aid: it synchronises the device twice and allocates small device buffers. */
+int pdpd_log_pair_terms(pdpd_engine *e, uint32_t world, const uint32_t *bead_ids, uint32_t n_ids,
+                        pdpd_pair_terms *out, uint32_t capacity, uint32_t *n_pairs);
+
 /* Allocation-free stepping -- this entry point has no counterpart in the reference.
  *
  * For callers that must not allocate device memory while they run: a framework that owns

@@ -31,6 +31,12 @@
 //       n^2 dissipative doubles.
 //   ref_harness v2read <in.v2> <out.bin>
 //       read_world_state (dpd_state_io.hpp:481-586) of a v2binary file; dump t, x, v, f.
+//   ref_harness pairlog <engine> <in.pdw1> <out.bin> <steps> <n_ids> <id...>
+//       Attach + Run(steps) with a ForceLogging logger installed (logging.hpp:9-30): every
+//       LogBeadPairProperty call whose home bead is one of the listed bead ids, as the
+//       engine's calc_force makes them (dpd_maths_core_half_step.hpp:131-153), recorded at
+//       full precision: (int64 t, uint32 home hash, uint32 other hash, char name[24],
+//       int32 dims, double value[3]) per call.
 
 #include "dpd/core/dpd_engine.hpp"
 #include "dpd/core/dpd_state_validator.hpp"
@@ -41,6 +47,7 @@
 #include "dpd/engines/naive/naive_dpd_engine_half_step.hpp"
 #include "dpd/engines/naive/naive_dpd_engine_half_merge.hpp"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -100,6 +107,58 @@ int cmd_step(int argc, char **argv)
         dump(out, s);
     }
     fclose(out);
+    return 0;
+}
+
+// A ForceLogging logger that keeps the pair properties of chosen home beads, full precision.
+class PairRecorder : public ForceLogging
+{
+public:
+    std::vector<uint32_t> homes;  // full hashes of the chosen home beads
+    FILE *out = nullptr;
+    long t = 0;
+    void Flush() override {}
+    void SetTime(long tt) override { t = tt; }
+    void SetPrefix(const std::string &) override {}
+    void LogProperty(const char *, int, const double *) override {}
+    void LogBeadProperty(BeadHash, const char *, int, const double *) override {}
+    void LogBeadTripleProperty(BeadHash, BeadHash, BeadHash, const char *, int, const double *) override {}
+    void LogBeadPairProperty(BeadHash b0, BeadHash b1, const char *name, int dims, const double *x) override
+    {
+        if (std::find(homes.begin(), homes.end(), b0.hash) == homes.end()) return;
+        int64_t tt = t;
+        uint32_t h[2] = {b0.hash, b1.hash};
+        char nm[24] = {0};
+        strncpy(nm, name, sizeof nm - 1);
+        int32_t d = dims;
+        double v[3] = {0, 0, 0};
+        for (int i = 0; i < dims && i < 3; i++) v[i] = x[i];
+        fwrite(&tt, sizeof tt, 1, out);
+        fwrite(h, sizeof h, 1, out);
+        fwrite(nm, 1, sizeof nm, out);
+        fwrite(&d, sizeof d, 1, out);
+        fwrite(v, sizeof v, 1, out);
+    }
+};
+
+int cmd_pairlog(int argc, char **argv)
+{
+    if (argc < 7) throw std::runtime_error("usage: pairlog engine in out steps n_ids ids...");
+    WorldState s = read_pdw1(argv[3]);
+    PairRecorder rec;
+    rec.out = fopen(argv[4], "wb");
+    if (!rec.out) throw std::runtime_error("cannot open output");
+    const unsigned steps = atoi(argv[5]), n_ids = atoi(argv[6]);
+    if (argc < 7 + (int)n_ids) throw std::runtime_error("pairlog: missing bead ids");
+    for (unsigned k = 0; k < n_ids; k++) rec.homes.push_back(s.beads.at(atoi(argv[7 + k])).get_hash_code().hash);
+    auto e = make_engine(argv[2]);
+    std::string why = e->CanSupport(&s);
+    if (!why.empty()) throw std::runtime_error("CanSupport: " + why);
+    e->Attach(&s);
+    ForceLogging::set_logger(&rec);
+    e->Run(steps);
+    ForceLogging::set_logger(nullptr);
+    fclose(rec.out);
     return 0;
 }
 
@@ -254,6 +313,7 @@ int main(int argc, char **argv)
         if (cmd == "v2read") return cmd_v2read(argc, argv);
         if (cmd == "stepx") return cmd_stepx(argc, argv);
         if (cmd == "tables") return cmd_tables(argc, argv);
+        if (cmd == "pairlog") return cmd_pairlog(argc, argv);
         throw std::runtime_error("unknown command " + cmd);
     } catch (std::exception &e) {
         fprintf(stderr, "ref_harness: %s\n", e.what());

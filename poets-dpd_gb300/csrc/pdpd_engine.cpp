@@ -67,6 +67,10 @@ template <class F> void parallel_for(size_t n, size_t min_chunk, F fn)
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }  // scratch buffers local to a call are freed on return
     cudaError_t alloc(size_t n)
     {
         if (p && n <= bytes) return cudaSuccess;
@@ -1513,6 +1517,76 @@ int pdpd_observe(pdpd_engine *e, uint32_t world, pdpd_observables *out, uint32_t
         o.virial += p.virial;
     }
     *out = o;
+    return PDPD_OK;
+}
+
+static_assert(sizeof(pdpd_pair_terms) == sizeof(PairLogRec), "pair log record layouts differ");
+
+int pdpd_log_pair_terms(pdpd_engine *e, uint32_t world, const uint32_t *bead_ids, uint32_t n_ids,
+                        pdpd_pair_terms *out, uint32_t capacity, uint32_t *n_pairs)
+{
+    if (n_pairs) *n_pairs = 0;
+    if (!e || (n_ids && !bead_ids) || (capacity && !out)) return PDPD_E_INVALID;
+    if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
+    if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
+    const WorldDev wd = e->worlds[world].dev;
+    std::vector<uint32_t> sel;
+    for (uint32_t k = 0; k < n_ids; k++) {
+        if (bead_ids[k] >= wd.n_beads) return e->fail(PDPD_E_INVALID, "bead id %u out of range", bead_ids[k]);
+        sel.push_back(wd.bead_base + bead_ids[k]);
+    }
+    std::sort(sel.begin(), sel.end());
+    sel.erase(std::unique(sel.begin(), sel.end()), sel.end());
+    cudaSetDevice(e->device);
+    cudaStream_t s = e->stream;
+    const uint32_t ns = (uint32_t)sel.size();
+    DevBuf d_sel, d_counts, d_offs, d_out;
+    cudaError_t ce = d_sel.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, ns));
+    if (ce == cudaSuccess) ce = d_counts.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, ns));
+    if (ce == cudaSuccess) ce = d_offs.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, ns));
+    if (ce != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pair log: device allocation failed");
+    if (ns) ce = cudaMemcpyAsync(d_sel.p, sel.data(), sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "pair log upload");
+    const bool f64 = e->fp64();
+    auto log = [&](const uint32_t *offs, uint32_t *counts, PairLogRec *recs) {
+        return f64 ? launch_pair_log64(e->args, d_sel.as<uint32_t>(), ns, offs, counts, recs, s)
+                   : launch_pair_log32(e->args, d_sel.as<uint32_t>(), ns, offs, counts, recs, s);
+    };
+    // the step up to its force pass (update_pos and the cell lists of t + 1), then the log of
+    // the pairs that force pass will evaluate, then the force pass and the end of the step
+    e->launches += e->enqueue_begin(s);
+    e->launches += log(nullptr, d_counts.as<uint32_t>(), nullptr);
+    std::vector<uint32_t> counts(ns), offs(ns);
+    if (ns) ce = cudaMemcpyAsync(counts.data(), d_counts.p, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost, s);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "pair log count");
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < ns; k++) {
+        offs[k] = (uint32_t)total;
+        total += counts[k];
+    }
+    if (total >= (1ull << 31)) return e->fail(PDPD_E_UNSUPPORTED, "pair log too large");
+    ce = d_out.alloc(sizeof(PairLogRec) * std::max<uint64_t>(1, total));
+    if (ce != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pair log: device allocation failed");
+    if (ns) ce = cudaMemcpyAsync(d_offs.p, offs.data(), sizeof(uint32_t) * ns, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "pair log upload");
+    e->launches += log(d_offs.as<uint32_t>(), nullptr, d_out.as<PairLogRec>());
+    e->launches += e->enqueue_final(s);
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "kernel launch");
+    std::vector<PairLogRec> recs(total);
+    if (total)
+        ce = cudaMemcpyAsync(recs.data(), d_out.p, sizeof(PairLogRec) * total, cudaMemcpyDeviceToHost, s);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "pair log download");
+    int rc = e->check_device_errors();  // synchronises
+    if (rc) return rc;
+    for (PairLogRec &r : recs) {  // world-local ids
+        r.home_id -= wd.bead_base;
+        r.other_id -= wd.bead_base;
+    }
+    const uint32_t n_copy = (uint32_t)std::min<uint64_t>(total, capacity);
+    if (n_copy) memcpy(out, recs.data(), sizeof(PairLogRec) * n_copy);
+    if (n_pairs) *n_pairs = (uint32_t)total;
     return PDPD_OK;
 }
 

@@ -500,6 +500,103 @@ __device__ void pair_forces32_seq_fx(const KArgs &a, const WorldDev &w, const fl
     fx_to_force(q, F);
 }
 
+// Pair log (pdpd_log_pair_terms) of the FP32 engine: for each sorted slot whose bead is in the
+// sorted id list sel, every in-range pair of the 27-direction walk (the full-shell kernels'
+// separation and test), with the terms of its force.  The force kernels fuse the terms
+// (pair_accumulate: con - diss and the random term in two multiply-adds); here con, diss and
+// rand are also formed one by one, and f = e * scaled is the pair's contribution exactly as
+// the kernels add it.  Count pass (out null) and write pass as k_pair_log64.
+__global__ void k_pair_log32(KArgs a, const uint32_t *__restrict__ sel, uint32_t n_sel,
+                             const uint32_t *__restrict__ offs, uint32_t *__restrict__ counts,
+                             PairLogRec *__restrict__ out)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_beads) return;
+    const uint32_t id = a.ids[s];
+    uint32_t lo = 0, hi = n_sel;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (sel[mid] < id) lo = mid + 1; else hi = mid;
+    }
+    if (lo == n_sel || sel[lo] != id) return;
+    const uint32_t k = lo;
+    uint32_t wl = 0, wh = a.n_worlds;
+    while (wh - wl > 1) {
+        const uint32_t mid = (wl + wh) / 2;
+        if (a.worlds[mid].bead_base <= id) wl = mid; else wh = mid;
+    }
+    const WorldDev &w = a.worlds[wl];
+    const float4 *pos = (const float4 *)a.posA, *vel = (const float4 *)a.velA;
+    const float4 ph = pos[s], vh = vel[s];
+    int c[3];
+    decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+    const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+    const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+    const float scale = (float)w.scale_inv_sqrt_dt;
+    const float2 *pair = (const float2 *)a.pair + w.param_base;
+    const float2 *cp = w.spatial ? (const float2 *)a.cellpair + w.cellpair_base : nullptr;
+    const uint32_t hc = ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
+    const uint32_t nt = w.n_types, n2 = nt * nt;
+    const uint32_t hh = __float_as_uint(ph.w), ti = min(hh >> 28, nt - 1u);
+    const float min2 = min_dist_sqr_f();
+    uint32_t n = 0;
+    for (int ddx = -1; ddx <= 1; ddx++)
+        for (int ddy = -1; ddy <= 1; ddy++)
+            for (int ddz = -1; ddz <= 1; ddz++) {
+                const int nx = wrap_index(c[0] + ddx, w.L[0]), ny = wrap_index(c[1] + ddy, w.L[1]),
+                          nz = wrap_index(c[2] + ddz, w.L[2]);
+                const uint32_t nc = w.cell_base + ((uint32_t)nx * (uint32_t)w.L[1] + (uint32_t)ny) * (uint32_t)w.L[2] + (uint32_t)nz;
+                const float ax = __fsub_rn(ph.x, (float)ddx), ay = __fsub_rn(ph.y, (float)ddy),
+                            az = __fsub_rn(ph.z, (float)ddz);
+                for (uint32_t j = a.start[nc]; j < a.start[nc + 1]; j++) {
+                    const float4 pj = pos[j];
+                    float dx, dy, dz;
+                    const float r2 = pair_r2(ax, ay, az, pj, dx, dy, dz);
+                    if (!(r2 < 1.0f && r2 >= min2)) continue;
+                    if (out) {
+                        const float4 vj = vel[j];
+                        const uint32_t hj = __float_as_uint(pj.w);
+                        const uint32_t pk = ti * nt + min(hj >> 28, nt - 1u);
+                        float2 pp = pair[pk];
+                        if (cp) {
+                            const float2 hv = cp[(size_t)hc * n2 + pk], ov = cp[(size_t)(a.cellg[j] - w.cell_base) * n2 + pk];
+                            pp = make_float2(__fmul_rn(__fadd_rn(hv.x, ov.x), 0.5f), __fmul_rn(__fadd_rn(hv.y, ov.y), 0.5f));
+                        }
+                        float F[3] = {0.f, 0.f, 0.f};
+                        pair_accumulate(dx, dy, dz, r2, vh, vj, hh, hj, pp, th_lo, th_hi, scale, F);
+                        const float inv_r = rsqrtf(r2);
+                        const float r = __fmul_rn(r2, inv_r);
+                        const float wr = __fsub_rn(1.0f, r);
+                        const float ex = __fmul_rn(dx, inv_r), ey = __fmul_rn(dy, inv_r), ez = __fmul_rn(dz, inv_r);
+                        const float rdotv = __fmaf_rn(ez, __fsub_rn(vh.z, vj.z),
+                                                      __fmaf_rn(ey, __fsub_rn(vh.y, vj.y), __fmul_rn(ex, __fsub_rn(vh.x, vj.x))));
+                        const float sg = __fmul_rn(pp.y, wr);
+                        const float u = hash_u(th_lo, th_hi, hh, hj);
+                        PairLogRec &rec = out[offs[k] + n];
+                        rec.t = w.t;
+                        rec.home_id = id;
+                        rec.other_id = a.ids[j];
+                        rec.home_hash = hh;
+                        rec.other_hash = hj;
+                        rec.dx[0] = dx;
+                        rec.dx[1] = dy;
+                        rec.dx[2] = dz;
+                        rec.dr = r;
+                        rec.inv_root_dt = scale;
+                        rec.gammap = __fmul_rn(sg, sg);
+                        rec.rng = u;
+                        rec.con = __fmul_rn(pp.x, wr);
+                        rec.diss = __fmul_rn(-__fmul_rn(sg, sg), rdotv);
+                        rec.rng_scale = __fmul_rn(sg, scale);
+                        rec.rand = __fmul_rn(__fmul_rn(sg, scale), u);
+                        for (int d = 0; d < 3; d++) rec.f[d] = F[d];
+                    }
+                    n++;
+                }
+            }
+    if (!out) counts[k] = n;
+}
+
 // Phase 2: the pair forces of the listed neighbours, in list order.
 __device__ __forceinline__ void list_forces32(const float4 *__restrict__ pos,
                                               const float4 *__restrict__ vel,
@@ -829,6 +926,14 @@ static int launch_pair_forces32(const KArgs &a, int final_step, cudaStream_t s)
         k_force32<1><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     else
         k_force32<0><<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
+    return 1;
+}
+
+int launch_pair_log32(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const uint32_t *offs,
+                      uint32_t *counts, PairLogRec *out, cudaStream_t s)
+{
+    if (a.n_beads == 0 || n_sel == 0) return 0;
+    k_pair_log32<<<(a.n_beads + 127) / 128, 128, 0, s>>>(a, sel, n_sel, offs, counts, out);
     return 1;
 }
 

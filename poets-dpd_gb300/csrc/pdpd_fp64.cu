@@ -196,6 +196,39 @@ __device__ __forceinline__ uint32_t neighbour64(const WorldDev &w, const int c[3
            (uint32_t)op[2];
 }
 
+// calc_force's terms of one in-range pair (dpd_maths_core_half_step.hpp:69-157, kappa = 0,
+// r0 = 0.5), each operation in the reference's order: the force pass adds e * scaled, and the
+// pair log (k_pair_log64) records the terms the reference's ForceLogging logs.
+struct PairTerms64 {
+    double e[3], wr, sqrt_gammap, u, con, diss, rand_scale, rand, scaled;
+};
+
+__device__ __forceinline__ PairTerms64 pair_terms64(double dx0, double dx1, double dx2, double dr,
+                                                    const Vec2d pp, const Vec4d &vh, const Vec4d &vj,
+                                                    uint32_t hh, uint32_t hj, uint32_t th_lo,
+                                                    uint32_t th_hi, double scale_inv_sqrt_dt)
+{
+    PairTerms64 q;
+    const double kappa = 0.0, r0 = 0.5;
+    const double inv_dr = 1.0 / dr;
+    const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
+    q.wr = 1.0 - dr;
+    q.con = pp.x * q.wr;
+    q.e[0] = dx0 * inv_dr;
+    q.e[1] = dx1 * inv_dr;
+    q.e[2] = dx2 * inv_dr;
+    const double rdotv = q.e[0] * dv0 + q.e[1] * dv1 + q.e[2] * dv2;
+    q.sqrt_gammap = pp.y * q.wr;
+    q.diss = -q.sqrt_gammap * q.sqrt_gammap * rdotv;
+    q.u = (double)hash_u(th_lo, th_hi, hh, hj);
+    q.rand_scale = q.sqrt_gammap * scale_inv_sqrt_dt;
+    q.rand = q.rand_scale * q.u;
+    const double dr0 = r0 - dr;
+    const double hookean_force = kappa * dr0;
+    q.scaled = q.con + q.diss + q.rand + hookean_force;
+    return q;
+}
+
 // Phase 2: the reference's pair filter and calc_force (dpd_maths_core_half_step.hpp:69-157,
 // kappa = 0, r0 = 0.5) for the listed candidates, in list order, each operation in the
 // reference's order.  The list holds every neighbour that can be in range (the walk's
@@ -237,24 +270,10 @@ __device__ __forceinline__ void list_forces64(const Vec4d *__restrict__ pos,
             pp.x = (h.x + o.x) * 0.5;
             pp.y = (h.y + o.y) * 0.5;
         }
-        const double kappa = 0.0, r0 = 0.5;
-        const double inv_dr = 1.0 / dr;
-        const double dv0 = vh.x - vj.x, dv1 = vh.y - vj.y, dv2 = vh.z - vj.z;
-        const double wr = 1.0 - dr;
-        const double con_force = pp.x * wr;
-        const double e0 = dx0 * inv_dr, e1 = dx1 * inv_dr, e2 = dx2 * inv_dr;
-        const double rdotv = e0 * dv0 + e1 * dv1 + e2 * dv2;
-        const double sqrt_gammap = pp.y * wr;
-        const double diss_force = -sqrt_gammap * sqrt_gammap * rdotv;
-        const double u = (double)hash_u(th_lo, th_hi, hh, hj);
-        const double rand_scale = sqrt_gammap * scale_inv_sqrt_dt;
-        const double rand_force = rand_scale * u;
-        const double dr0 = r0 - dr;
-        const double hookean_force = kappa * dr0;
-        const double scaled = con_force + diss_force + rand_force + hookean_force;
-        F[0] = F[0] + e0 * scaled;
-        F[1] = F[1] + e1 * scaled;
-        F[2] = F[2] + e2 * scaled;
+        const PairTerms64 q = pair_terms64(dx0, dx1, dx2, dr, pp, vh, vj, hh, hj, th_lo, th_hi, scale_inv_sqrt_dt);
+        F[0] = F[0] + q.e[0] * q.scaled;
+        F[1] = F[1] + q.e[1] * q.scaled;
+        F[2] = F[2] + q.e[2] * q.scaled;
     }
 }
 
@@ -352,6 +371,92 @@ __device__ __forceinline__ int walk64(const KArgs &a, const WorldDev &w, const V
         }
     }
     return n;
+}
+
+// Pair log (pdpd_log_pair_terms): for each sorted slot whose bead is in the sorted id list
+// sel, every in-range pair of the 27-direction walk in the reference's order
+// (naive_dpd_engine_half_step.hpp:300-424), with calc_force's terms as the reference's
+// ForceLogging records them (dpd_maths_core_half_step.hpp:131-153).  Count pass (out null):
+// counts[k] = pairs of sel[k]; write pass: the records of sel[k] at out + offs[k].
+__global__ void k_pair_log64(KArgs a, const uint32_t *__restrict__ sel, uint32_t n_sel,
+                             const uint32_t *__restrict__ offs, uint32_t *__restrict__ counts,
+                             PairLogRec *__restrict__ out)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.n_beads) return;
+    const uint32_t id = a.ids[s];
+    uint32_t lo = 0, hi = n_sel;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (sel[mid] < id) lo = mid + 1; else hi = mid;
+    }
+    if (lo == n_sel || sel[lo] != id) return;
+    const uint32_t k = lo;
+    uint32_t wl = 0, wh = a.n_worlds;
+    while (wh - wl > 1) {
+        const uint32_t mid = (wl + wh) / 2;
+        if (a.worlds[mid].bead_base <= id) wl = mid; else wh = mid;
+    }
+    const WorldDev &w = a.worlds[wl];
+    const Home64 h = home64(a, w, s);
+    const uint64_t th = t_hash((uint32_t)w.t, w.seed);
+    const uint32_t th_lo = (uint32_t)th, th_hi = (uint32_t)(th >> 32);
+    const double Ld[3] = {(double)w.L[0], (double)w.L[1], (double)w.L[2]};
+    const Vec2d *pair = (const Vec2d *)a.pair + w.param_base;
+    const Vec2d *cp = w.spatial ? (const Vec2d *)a.cellpair + w.cellpair_base : nullptr;
+    const Vec4d *pos = (const Vec4d *)a.posA, *vel = (const Vec4d *)a.velA;
+    const uint32_t nt = w.n_types, n2 = nt * nt;
+    const double min2 = (double)min_dist_sqr_f();
+    uint32_t n = 0;
+    int dir[3];
+    for (dir[0] = -1; dir[0] <= 1; dir[0]++)
+        for (dir[1] = -1; dir[1] <= 1; dir[1]++)
+            for (dir[2] = -1; dir[2] <= 1; dir[2]++) {
+                double delta[3];
+                const uint32_t nc = neighbour64(w, h.c, dir, Ld, delta);
+                for (uint32_t j = a.start[nc]; j < a.start[nc + 1]; j++) {
+                    const Vec4d pj = pos[j];
+                    const double obx = pj.x + delta[0], oby = pj.y + delta[1], obz = pj.z + delta[2];
+                    const double dx0 = h.x[0] - obx, dx1 = h.x[1] - oby, dx2 = h.x[2] - obz;
+                    const double dr2 = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+                    if (dr2 >= 1 || dr2 < min2) continue;
+                    if (out) {
+                        const Vec4d vj = vel[j];
+                        const double dr = sqrt(dr2);
+                        const uint32_t hj = hash_of(pj);
+                        const uint32_t pk = h.ti * nt + min(hj >> 28, nt - 1u);
+                        Vec2d pp = pair[pk];
+                        if (cp) {
+                            const Vec2d hv = cp[(size_t)h.hc * n2 + pk], ov = cp[(size_t)(a.cellg[j] - w.cell_base) * n2 + pk];
+                            pp.x = (hv.x + ov.x) * 0.5;
+                            pp.y = (hv.y + ov.y) * 0.5;
+                        }
+                        const PairTerms64 q =
+                            pair_terms64(dx0, dx1, dx2, dr, pp, h.v, vj, h.hash, hj, th_lo, th_hi, w.scale_inv_sqrt_dt);
+                        PairLogRec &r = out[offs[k] + n];
+                        r.t = w.t;
+                        r.home_id = id;
+                        r.other_id = a.ids[j];
+                        r.home_hash = h.hash;
+                        r.other_hash = hj;
+                        r.dx[0] = dx0;
+                        r.dx[1] = dx1;
+                        r.dx[2] = dx2;
+                        r.dr = dr;
+                        r.inv_root_dt = w.scale_inv_sqrt_dt;
+                        r.gammap = q.sqrt_gammap * q.sqrt_gammap;
+                        r.rng = q.u;
+                        r.con = q.con;
+                        r.diss = q.diss;
+                        r.rng_scale = q.rand_scale;
+                        r.rand = q.rand;
+                        const double dpd_force = q.con + q.diss + q.rand;
+                        for (int d = 0; d < 3; d++) r.f[d] = q.e[d] * dpd_force;
+                    }
+                    n++;
+                }
+            }
+    if (!out) counts[k] = n;
 }
 
 // Lists of a tile, re-dealt to threads by length (see k_force64).
@@ -606,6 +711,14 @@ int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
 int launch_begin64(const KArgs &a, cudaStream_t s)
 {
     k_begin64<<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
+    return 1;
+}
+
+int launch_pair_log64(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const uint32_t *offs,
+                      uint32_t *counts, PairLogRec *out, cudaStream_t s)
+{
+    if (a.n_beads == 0 || n_sel == 0) return 0;
+    k_pair_log64<<<(a.n_beads + 127) / 128, 128, 0, s>>>(a, sel, n_sel, offs, counts, out);
     return 1;
 }
 

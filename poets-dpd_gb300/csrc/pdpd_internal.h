@@ -147,6 +147,21 @@ int launch_finish64(const KArgs &a, cudaStream_t s);
 int launch_unsort64(const KArgs &a, cudaStream_t s, uint32_t first, uint32_t count);  // sorted slots [first, first + count)
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s);
 
+// One record of the pair log (pdpd_log_pair_terms; the C ABI's pdpd_pair_terms has this
+// layout, with world-local ids): bead ids are global here.
+struct PairLogRec {
+    int64_t t;
+    uint32_t home_id, other_id;
+    uint32_t home_hash, other_hash;
+    double dx[3], dr, inv_root_dt, gammap, rng, con, diss, rng_scale, rand, f[3];
+};
+// Pair log of the beads whose global ids are in sel (sorted, n_sel of them): with out null,
+// counts[k] = in-range pairs of sel[k]; else the records of sel[k] from out + offs[k].
+int launch_pair_log32(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const uint32_t *offs,
+                      uint32_t *counts, PairLogRec *out, cudaStream_t s);
+int launch_pair_log64(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const uint32_t *offs,
+                      uint32_t *counts, PairLogRec *out, cudaStream_t s);
+
 // Device RNG on arrays (device pointers), for known-answer tests.
 int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);

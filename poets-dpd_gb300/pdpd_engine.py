@@ -40,7 +40,7 @@ EXPORTED = ["pdpd_create", "pdpd_destroy", "pdpd_last_error", "pdpd_can_support"
             "pdpd_run_async", "pdpd_sync", "pdpd_stream", "pdpd_read_state", "pdpd_read_states",
             "pdpd_run_intervals", "pdpd_get_timings", "pdpd_get_config", "pdpd_set_config",
             "pdpd_kernel_launches", "pdpd_rng_eval", "pdpd_profile_run", "pdpd_step_noalloc",
-            "pdpd_observe", "pdpd_v2binary_prepare", "pdpd_v2binary_encode",
+            "pdpd_observe", "pdpd_log_pair_terms", "pdpd_v2binary_prepare", "pdpd_v2binary_encode",
             "pdpd_v2binary_decode", "pdpd_server_create", "pdpd_server_submit", "pdpd_server_drain",
             "pdpd_server_config", "pdpd_server_stats_get", "pdpd_server_engine",
             "pdpd_server_destroy"]
@@ -72,6 +72,44 @@ class PdpdTimings(C.Structure):
 class PdpdPhaseTimes(C.Structure):
     _fields_ = [("force_ms", C.c_double), ("sort_ms", C.c_double), ("other_ms", C.c_double),
                 ("force_launches", C.c_uint32), ("sort_launches", C.c_uint32)]
+
+
+# pdpd_pair_terms (include/pdpd_gpu.h): one pair of the per-pair force log.
+PAIR_TERMS_DTYPE = np.dtype([("t", "<i8"), ("home_id", "<u4"), ("other_id", "<u4"),
+                             ("home_hash", "<u4"), ("other_hash", "<u4"), ("dx", "<f8", 3),
+                             ("dr", "<f8"), ("inv_root_dt", "<f8"), ("gammap", "<f8"), ("rng", "<f8"),
+                             ("con", "<f8"), ("diss", "<f8"), ("rng_scale", "<f8"), ("rand", "<f8"),
+                             ("f", "<f8", 3)])
+
+# The names the reference's calc_force logs a pair's terms under
+# (dpd_maths_core_half_step.hpp:134-148), with the record fields that hold them.
+PAIR_LOG_PROPERTIES = [("dx", "dx"), ("dr", "dr"), ("dpd-invrootdt", "inv_root_dt"),
+                       ("dpd-gammap", "gammap"), ("dpd-rng", "rng"), ("dpd-con", "con"),
+                       ("dpd-diss", "diss"), ("dpd-rng-scale", "rng_scale"), ("dpd-rand", "rand"),
+                       ("f_next_dpd", "f")]
+
+
+def _log_value(v):
+    """A value as the reference's FileLogger prints it (logging_impl.hpp:27-34): an integer in
+    [0, 2^32) as an integer, anything else as an ostream prints a double (%g, 6 digits)."""
+    v = float(v)
+    if v == round(v) and 0 <= v < 2.0 ** 32:
+        return str(int(v))
+    return "%g" % v
+
+
+def force_log_lines(records, prefix=""):
+    """The pair records in the reference's FileLogger text format (logging_impl.hpp:75-86):
+    'Prop,t,home,other,,name,v0,v1,v2' with reduced hashes (hash & 0x0fffffff), one line per
+    property, in the reference's property order -- to diff against a reference log."""
+    lines = []
+    for r in records:
+        h0, h1 = int(r["home_hash"]) & 0x0FFFFFFF, int(r["other_hash"]) & 0x0FFFFFFF
+        for name, field in PAIR_LOG_PROPERTIES:
+            vals = np.atleast_1d(r[field])
+            cells = [_log_value(x) for x in vals] + [""] * (3 - vals.size)
+            lines.append(f"{prefix}Prop,{int(r['t'])},{h0},{h1},,{name}," + ",".join(cells))
+    return lines
 
 
 class PdpdObservables(C.Structure):
@@ -129,6 +167,7 @@ def lib():
         "pdpd_profile_run": (i32, [vp, u32, C.POINTER(PdpdPhaseTimes)]),
         "pdpd_step_noalloc": (i32, [C.POINTER(PdpdWorld), vp, vp, vp, vp, u32, vp]),
         "pdpd_observe": (i32, [vp, u32, C.POINTER(PdpdObservables), u32, vp, u32, vp]),
+        "pdpd_log_pair_terms": (i32, [vp, u32, vp, u32, vp, u32, C.POINTER(u32)]),
         "pdpd_v2binary_prepare": (i32, [vp, u32, u32, vp, vp, vp, vp, C.POINTER(C.c_size_t)]),
         "pdpd_v2binary_encode": (i32, [vp, u32, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
         "pdpd_v2binary_decode": (i32, [vp, u32, vp, C.c_size_t]),
@@ -365,6 +404,23 @@ class GB300DPDEngine:
                                        n_bond_bins, _p(bh)), "observe")
         return {"ke2": o.ke2, "virial": o.virial, "momentum": np.array(o.momentum[:]),
                 "rdf": rdf.reshape(nt, nt, n_bins), "bond_hist": bh}
+
+    def log_pair_terms(self, bead_ids, world_index=0, per_bead_capacity=256):
+        """Advance one step (as Run(1)) and return the pair terms of that step for the given
+        beads of world ``world_index``: a structured array (PAIR_TERMS_DTYPE, the C ABI's
+        pdpd_pair_terms) grouped by bead in ascending id order, each bead's pairs in the
+        reference's walk order -- what the reference's ForceLogging logs from calc_force.
+        Room is made for per_bead_capacity pairs per bead (density 3 gives ~13); a step with
+        more raises, and its records are lost (the step itself has run)."""
+        ids = np.ascontiguousarray(np.unique(np.asarray(bead_ids, np.int64)).astype(np.uint32))
+        cap = max(1, per_bead_capacity * ids.size)
+        out = np.zeros(cap, PAIR_TERMS_DTYPE)
+        n = C.c_uint32(0)
+        self._check(lib().pdpd_log_pair_terms(self._h, world_index, _p(ids), ids.size, _p(out), cap,
+                                              C.byref(n)), "log_pair_terms")
+        if n.value > cap:
+            raise RuntimeError(f"log_pair_terms: {n.value} pairs, room for {cap}")
+        return out[:n.value]
 
     def kernel_launches(self):
         return int(lib().pdpd_kernel_launches(self._h))

@@ -17,7 +17,7 @@ def world_fixture_names():
     bit)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                   if not p.endswith(("hash_kat.npz", "testbase_suite.npz"))
-                  and not os.path.basename(p).startswith(("merge_", "v2_")))
+                  and not os.path.basename(p).startswith(("merge_", "v2_", "pair_log_")))
 
 
 def merge_fixture_names(kind=""):

@@ -365,9 +365,49 @@ def testbase_fixture(max_segments=4, keep_every_multiple=1):
     print(f"testbase_suite: {len(names)} of {n} cases, {len(todos)} segments")
 
 
+PAIR_LOG_NAMES = ["dx", "dr", "dpd-invrootdt", "dpd-gammap", "dpd-rng", "dpd-con", "dpd-diss",
+                  "dpd-rng-scale", "dpd-rand", "f_next_dpd"]
+
+
+def pair_log_fixture(name="pair_log_polymer10", steps=2, ids=(0, 3, 5, 700, 2999)):
+    """The reference's per-pair force log (ForceLogging, logging.hpp:9-100, as calc_force makes
+    it: dpd_maths_core_half_step.hpp:131-153) of the half-step engine over `steps` steps of
+    the 10^3 polymer box, for the listed home beads, at full precision (ref_harness pairlog)."""
+    world = W.make_polymer_box(10, chain_fraction=0.1, seed=2)
+    tmp_in, tmp_out = os.path.join(HERE, "_in.pdw1"), os.path.join(HERE, "_out.bin")
+    W.write_pdw1(world, tmp_in)
+    subprocess.run([HARNESS, "pairlog", ENGINE, tmp_in, tmp_out, str(steps), str(len(ids))]
+                   + [str(i) for i in ids], check=True)
+    data = open(tmp_out, "rb").read()
+    os.remove(tmp_in)
+    os.remove(tmp_out)
+    rec = np.dtype([("t", "<i8"), ("h", "<u4", 2), ("name", "S24"), ("dims", "<i4"), ("v", "<f8", 3)])
+    raw = np.frombuffer(data, rec)
+    k = len(PAIR_LOG_NAMES)
+    assert raw.size % k == 0, raw.size
+    names = [n.decode() for n in raw["name"][:k]]
+    assert names == PAIR_LOG_NAMES, names
+    g = raw.reshape(-1, k)
+    assert all((g["name"][:, i] == PAIR_LOG_NAMES[i].encode()).all() for i in range(k))
+    out = {"t": g["t"][:, 0], "home_hash": g["h"][:, 0, 0], "other_hash": g["h"][:, 0, 1],
+           "dx": g["v"][:, 0], "f": g["v"][:, 9]}
+    for i, key in enumerate(["dr", "inv_root_dt", "gammap", "rng", "con", "diss", "rng_scale", "rand"], 1):
+        out[key] = g["v"][:, i, 0]
+    buf = io.BytesIO()
+    W.write_pdw1(world, buf)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), world=np.frombuffer(buf.getvalue(), np.uint8),
+                        ids=np.array(ids, np.uint32), steps=np.array(steps), engine=np.array(ENGINE),
+                        **out)
+    print(f"{name}: {g.shape[0]} pair records of {len(ids)} beads over {steps} steps")
+
+
 def main():
     if not os.path.exists(HARNESS):
         raise SystemExit("build the reference harness first: make -C oracle/ref")
+    if "--only" in sys.argv:  # e.g. --only pair_log: regenerate one fixture
+        globals()[sys.argv[sys.argv.index("--only") + 1] + "_fixture"]()
+        return
+    pair_log_fixture()
     hash_fixture()
     testbase_fixture()
     save_world_fixture("water8_seed1", W.make_water(8, seed=1), [1, 10, 100, 1000],
