@@ -314,7 +314,8 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
     while th.is_alive():
         s_ = srv.stats()
         samples.append((time.perf_counter() - t0, s_["bead_steps"] - st0["bead_steps"],
-                        s_["step_s"] - st0["step_s"], s_["repack_s"] - st0["repack_s"]))
+                        s_["step_s"] - st0["step_s"], s_["repack_s"] - st0["repack_s"],
+                        s_["host_gap_s"] - st0["host_gap_s"]))
         th.join(0.25)
     srv.drain()
     wall = time.perf_counter() - t0
@@ -358,6 +359,8 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "repack_s": st["repack_s"] - st0["repack_s"],
             "wasted_bead_steps": st["wasted_bead_steps"] - st0["wasted_bead_steps"],
             "step_s": st["step_s"] - st0["step_s"],
+            "host_gap_s": st["host_gap_s"] - st0["host_gap_s"],
+            "callback_s": st["callback_s"] - st0["callback_s"],
             "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,
@@ -369,17 +372,21 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
 
 def steady_state(samples, ramp_s, end_s):
     """Served rate while the stream arrives, after the ramp: from the server's counters sampled
-    over time, (t, bead_steps, step_s, repack_s), the slope between the first sample at or
-    after ramp_s and the last at or before end_s, and the fractions of that wall time the GPU
-    spent stepping (device time of the epochs) and the host spent re-packing."""
+    over time, (t, bead_steps, step_s, repack_s[, host_gap_s]), the slope between the first
+    sample at or after ramp_s and the last at or before end_s, and the fractions of that wall
+    time the GPU spent stepping (device time of the epochs), the host spent re-packing, and
+    the GPU waited for the host between epochs (re-packs included)."""
     win = [x for x in samples if ramp_s <= x[0] <= end_s]
     if len(win) < 2 or win[-1][0] <= win[0][0]:
         return None
-    (t_a, b_a, s_a, r_a), (t_b, b_b, s_b, r_b) = win[0], win[-1]
-    dt = t_b - t_a
-    return {"from_s": t_a, "to_s": t_b, "served_bead_steps_per_s": (b_b - b_a) / dt,
-            "step_frac": (s_b - s_a) / dt, "repack_frac": (r_b - r_a) / dt,
-            "bead_steps_per_step_s": (b_b - b_a) / (s_b - s_a) if s_b > s_a else None}
+    a, b = win[0], win[-1]
+    dt = b[0] - a[0]
+    out = {"from_s": a[0], "to_s": b[0], "served_bead_steps_per_s": (b[1] - a[1]) / dt,
+           "step_frac": (b[2] - a[2]) / dt, "repack_frac": (b[3] - a[3]) / dt,
+           "bead_steps_per_step_s": (b[1] - a[1]) / (b[2] - a[2]) if b[2] > a[2] else None}
+    if len(a) > 4:
+        out["host_gap_frac"] = (b[4] - a[4]) / dt
+    return out
 
 
 def dist_setup(n_gpus):

@@ -233,6 +233,7 @@ typedef struct pdpd_pair_terms {
  * terms of that step for the n_ids beads bead_ids[] (ids within world `world`; duplicates
  * are ignored).  Records are grouped by bead in ascending id order, each bead's pairs in the
  * reference's walk order (27 directions, (-1..1)^3 with z fastest, then the cell's beads in
+ * id order; in the FP32 engine a cell holds its beads with z offset < 0.5 first, each half in
  * id order).  The first min(total, capacity) records go to out; *n_pairs receives the total.
  * A debugging aid: it synchronises the device twice and allocates small device buffers. */
 int pdpd_log_pair_terms(pdpd_engine *e, uint32_t world, const uint32_t *bead_ids, uint32_t n_ids,
@@ -342,6 +343,9 @@ typedef struct pdpd_server_stats {
     double step_s;         /* device time of the epochs' steps (CUDA events on the engine's
                               stream); wall_s minus it is time the GPU spent on re-packs,
                               snapshots or waiting for the host */
+    double host_gap_s;     /* wall time from the host seeing an epoch finish to its launch of
+                              the next (re-packs included): the GPU waits for the host */
+    double callback_s;     /* wall time in job callbacks (they overlap the running epoch) */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.

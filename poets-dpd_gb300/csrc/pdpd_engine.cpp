@@ -11,6 +11,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <condition_variable>
+#include <mutex>
+#include <unistd.h>
 #include <memory>
 #include <string>
 #include <thread>
@@ -42,22 +46,105 @@ double now_s()
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Host worker threads for parallel_for, started once per process and kept: a batch attach or
+// read-back runs a few dozen parallel loops, and starting 16 threads for each cost more than
+// some of the loops.  One loop at a time uses the pool (a loop that finds it busy, e.g. on a
+// second engine's thread, starts its own threads as before); a process that forked after the
+// pool was started builds a new one.
+class HostPool {
+public:
+    static HostPool &get()
+    {
+        static std::mutex init;
+        static HostPool *pool = nullptr;
+        std::lock_guard<std::mutex> lk(init);
+        if (!pool || pool->pid_ != getpid()) pool = new HostPool();  // (kept until exit)
+        return *pool;
+    }
+    size_t threads() const { return workers_ + 1; }
+    // Run task(k) for k in [0, n_tasks) on the pool and the calling thread; false if the pool
+    // is busy with another loop.
+    bool run(size_t n_tasks, const std::function<void(size_t)> &task)
+    {
+        std::unique_lock<std::mutex> use(use_, std::try_to_lock);
+        if (!use.owns_lock()) return false;
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            task_ = &task;
+            n_ = n_tasks;
+            next_ = 0;
+            done_ = 0;
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(m_);
+        done_cv_.wait(lk, [&] { return done_ == n_; });
+        task_ = nullptr;
+        return true;
+    }
+
+private:
+    HostPool() : pid_(getpid())
+    {
+        workers_ = std::min<size_t>(15, std::max(1u, std::thread::hardware_concurrency()) - 1);
+        for (size_t k = 0; k < workers_; k++)
+            std::thread([this] {
+                uint64_t seen = 0;
+                for (;;) {
+                    {
+                        std::unique_lock<std::mutex> lk(m_);
+                        cv_.wait(lk, [&] { return gen_ != seen; });
+                        seen = gen_;
+                    }
+                    work();
+                }
+            }).detach();
+    }
+    void work()
+    {
+        for (;;) {
+            size_t k;
+            const std::function<void(size_t)> *t;
+            {
+                std::lock_guard<std::mutex> lk(m_);
+                if (!task_ || next_ >= n_) return;
+                k = next_++;
+                t = task_;
+            }
+            (*t)(k);
+            std::lock_guard<std::mutex> lk(m_);
+            if (++done_ == n_) done_cv_.notify_all();
+        }
+    }
+    pid_t pid_;
+    size_t workers_ = 0;
+    std::mutex use_, m_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t)> *task_ = nullptr;
+    size_t n_ = 0, next_ = 0, done_ = 0;
+    uint64_t gen_ = 0;
+};
+
 // fn(begin, end) over [0, n) on up to 16 host threads (chunks of at least min_chunk items):
 // the per-bead host packing and unpacking of large worlds.
 template <class F> void parallel_for(size_t n, size_t min_chunk, F fn)
 {
-    size_t nt = std::min<size_t>(16, std::max(1u, std::thread::hardware_concurrency()));
+    HostPool &pool = HostPool::get();
+    size_t nt = std::min<size_t>(16, pool.threads());
     nt = std::min(nt, std::max<size_t>(1, n / std::max<size_t>(1, min_chunk)));
     if (nt <= 1) {
         fn((size_t)0, n);
         return;
     }
-    std::vector<std::thread> th;
     const size_t per = (n + nt - 1) / nt;
-    for (size_t k = 0; k < nt; k++) {
+    const std::function<void(size_t)> task = [&](size_t k) {
         const size_t b = std::min(n, k * per), e = std::min(n, b + per);
-        if (b < e) th.emplace_back([=] { fn(b, e); });
-    }
+        if (b < e) fn(b, e);
+    };
+    if (pool.run(nt, task)) return;
+    std::vector<std::thread> th;
+    for (size_t k = 0; k < nt; k++) th.emplace_back([&task, k] { task(k); });
     for (auto &t : th) t.join();
 }
 
@@ -205,6 +292,7 @@ struct pdpd_engine {
     DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo, d_brick_next, d_hash_old;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
+    HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
     HostPinned h_err;
     DevBuf d_v2err;
     cudaEvent_t ev_snap[2] = {nullptr, nullptr};
@@ -550,11 +638,24 @@ struct pdpd_engine {
 
     int check_device_errors()
     {
+        int rc = fetch_device_errors();
+        if (rc) return rc;
+        cudaError_t e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_fail(e, "device error check");
+        return eval_device_errors();
+    }
+    // The worlds' flags and t copied to h_err on the stream (for eval_device_errors once the
+    // copy has completed).
+    int fetch_device_errors()
+    {
         size_t nb = sizeof(WorldDev) * worlds.size();
         if (h_err.alloc(nb) != cudaSuccess) return fail(PDPD_E_NOMEM, "pinned allocation failed");
         cudaError_t e = cudaMemcpyAsync(h_err.p, d_worlds.p, nb, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) return cuda_fail(e, "device error check");
+        return PDPD_OK;
+    }
+    int eval_device_errors()
+    {
         const WorldDev *wd = (const WorldDev *)h_err.p;
         for (size_t i = 0; i < worlds.size(); i++) {
             worlds[i].dev.t = wd[i].t;
@@ -631,6 +732,12 @@ static const double *vec_at(const double *base, size_t stride_bytes, uint32_t i)
 {
     size_t s = stride_bytes ? stride_bytes : 3 * sizeof(double);
     return (const double *)((const char *)base + s * (size_t)i);
+}
+
+static double *vec_at_mut(double *base, size_t stride_bytes, size_t i)
+{
+    size_t s = stride_bytes ? stride_bytes : 3 * sizeof(double);
+    return (double *)((char *)base + s * i);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -762,10 +869,22 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     e->reset();
     char reason[256];
     uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
+    {  // the worlds' checks (each scans its beads), in parallel; the first failure is reported
+        std::vector<int> wrc(n_worlds, PDPD_OK);
+        std::vector<std::string> why(n_worlds);
+        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; i++) {
+                char r[256];
+                const bool kept = keep_old && keep_old[i] >= 0;
+                wrc[i] = check_world(&ws[i], r, sizeof r, !kept);
+                if (wrc[i]) why[i] = r;
+            }
+        });
+        for (uint32_t i = 0; i < n_worlds; i++)
+            if (wrc[i]) return e->fail(wrc[i], "world %u: %s", i, why[i].c_str());
+    }
+    (void)reason;
     for (uint32_t i = 0; i < n_worlds; i++) {
-        const bool kept = keep_old && keep_old[i] >= 0;
-        int rc = check_world(&ws[i], reason, sizeof reason, !kept);
-        if (rc) return e->fail(rc, "world %u: %s", i, reason);
         nb += ws[i].n_beads;
         nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
         n_pair += (uint64_t)ws[i].n_bead_types * ws[i].n_bead_types;
@@ -849,12 +968,26 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
     // the flat list order.
     // (no bond terms at all, e.g. pure water: the rows are all zero and are set on the device)
-    std::vector<uint32_t> row(n_terms ? nb + 1 : 0, 0);
-    for (uint32_t i = 0; n_terms && i < n_worlds; i++) {
-        const pdpd_world &w = ws[i];
-        uint32_t bb = wdev[i].bead_base;
-        for (uint32_t k = 0; k < 2 * w.n_bonds; k++) row[bb + w.bond_beads[k] + 1]++;
-        for (uint32_t k = 0; k < 3 * w.n_angles; k++) row[bb + w.angle_beads[k] + 1]++;
+    // Rows and terms are built in pinned memory (uploaded from there, asynchronously); a
+    // world's terms name only its own beads, so the worlds' rows are counted in parallel.
+    uint32_t *row = nullptr;
+    BondTerm *terms = nullptr;
+    if (n_terms) {
+        const size_t row_bytes = (sizeof(uint32_t) * (nb + 1) + 15) & ~size_t(15);
+        if (e->h_meta.alloc(row_bytes + sizeof(BondTerm) * n_terms) != cudaSuccess)
+            return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
+        row = (uint32_t *)e->h_meta.p;
+        terms = (BondTerm *)((char *)e->h_meta.p + row_bytes);
+        row[0] = 0;
+        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; i++) {
+                const pdpd_world &w = ws[i];
+                const uint32_t bb = wdev[i].bead_base;
+                memset(row + bb + 1, 0, sizeof(uint32_t) * w.n_beads);
+                for (uint32_t k = 0; k < 2 * w.n_bonds; k++) row[bb + w.bond_beads[k] + 1]++;
+                for (uint32_t k = 0; k < 3 * w.n_angles; k++) row[bb + w.angle_beads[k] + 1]++;
+            }
+        });
     }
     if (n_terms) {  // inclusive prefix of row[1..nb] in parallel chunks: chunk sums, then offsets
         const size_t n = nb, chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
@@ -875,11 +1008,10 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             }
         });
     }
-    std::vector<BondTerm> terms(n_terms);
-    std::vector<uint32_t> fill(n_terms ? nb : 0);
+    std::unique_ptr<uint32_t[]> fill(n_terms ? new uint32_t[nb] : nullptr);  // per-bead cursors
     if (n_terms)
         parallel_for(nb, 1 << 18, [&](size_t i0, size_t i1) {
-            memcpy(fill.data() + i0, row.data() + i0, sizeof(uint32_t) * (i1 - i0));
+            memcpy(fill.get() + i0, row + i0, sizeof(uint32_t) * (i1 - i0));
         });
     // Parameters: every world's Hookean bonds in order, then every world's angle bonds.  The
     // worlds' terms fill disjoint CSR rows, so the worlds are filled in parallel.
@@ -1009,44 +1141,64 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // --- stage and upload
     double *hs = (double *)e->h_staging[0].p;
     uint32_t *hh = (uint32_t *)(hs + 9 * h_rows);
-    // One pass over the whole batch's beads (global slot g of world i = bead_base_i + k),
-    // split across host threads whatever the worlds' sizes.
-    parallel_for(nb, 1 << 16, [&](size_t g0, size_t g1) {
-        uint32_t i = (uint32_t)(std::upper_bound(wdev.begin(), wdev.end(), (uint32_t)g0,
-                                                 [](uint32_t g, const WorldDev &d) { return g < d.bead_base; }) -
-                                wdev.begin()) - 1;
-        for (size_t g = g0; g < g1;) {
-            while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
-            const pdpd_world &w = ws[i];
-            const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, w.n_beads);
-            const bool kept = keep_old && keep_old[i] >= 0;  // state and hashes from the old arena (below)
-            const size_t ho = hoff[i];
-            for (size_t k = g - bb; k < k1 && !kept; k++) {
-                const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
-                const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
-                const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
-                double *o = hs + 9 * (ho + k);
-                for (int d = 0; d < 3; d++) {
-                    o[d] = x[d];
-                    o[3 + d] = v[d];
-                    o[6 + d] = f[d];
+    // Global slots [r0, r1) of the batch (slot g of world i = bead_base_i + k) into the pinned
+    // rows, split across host threads whatever the worlds' sizes.
+    auto stage = [&](size_t r0, size_t r1) {
+        parallel_for(r1 - r0, 1 << 16, [&](size_t a0, size_t a1) {
+            const size_t g0 = r0 + a0, g1 = r0 + a1;
+            uint32_t i = (uint32_t)(std::upper_bound(wdev.begin(), wdev.end(), (uint32_t)g0,
+                                                     [](uint32_t g, const WorldDev &d) { return g < d.bead_base; }) -
+                                    wdev.begin()) - 1;
+            for (size_t g = g0; g < g1;) {
+                while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
+                const pdpd_world &w = ws[i];
+                const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, w.n_beads);
+                const bool kept = keep_old && keep_old[i] >= 0;  // state and hashes from the old arena (below)
+                const size_t ho = hoff[i];
+                for (size_t k = g - bb; k < k1 && !kept; k++) {
+                    const double *x = vec_at(w.x, w.bead_stride_bytes, (uint32_t)k);
+                    const double *v = vec_at(w.v, w.bead_stride_bytes, (uint32_t)k);
+                    const double *f = vec_at(w.f, w.bead_stride_bytes, (uint32_t)k);
+                    double *o = hs + 9 * (ho + k);
+                    for (int d = 0; d < 3; d++) {
+                        o[d] = x[d];
+                        o[3 + d] = v[d];
+                        o[6 + d] = f[d];
+                    }
+                    hh[ho + k] = w.hash[k];
                 }
-                hh[ho + k] = w.hash[k];
+                g = bb + k1;
             }
-            g = bb + k1;
-        }
-    });
+        });
+    };
     cudaStream_t s = e->stream;
+    if (!any_kept) {
+        // a whole batch from its descriptors: chunks of 2^20 beads, each uploaded while the
+        // next is staged
+        const size_t CH = size_t(1) << 20;
+        for (size_t r0 = 0; r0 < nb; r0 += CH) {
+            const size_t r1 = std::min<size_t>(nb, r0 + CH);
+            stage(r0, r1);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * r0, hs + 9 * r0, sizeof(double) * 9 * (r1 - r0),
+                                     cudaMemcpyHostToDevice, s);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(e->d_hash.as<uint32_t>() + r0, hh + r0, sizeof(uint32_t) * (r1 - r0),
+                                     cudaMemcpyHostToDevice, s);
+        }
+    } else {
+        stage(0, nb);
+    }
     auto H2D = [&](DevBuf &b, const void *src, size_t n) {
         if (ce == cudaSuccess && n) ce = cudaMemcpyAsync(b.p, src, n, cudaMemcpyHostToDevice, s);
     };
     H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
     H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
     if (n_terms)
-        H2D(e->d_bond_row, row.data(), sizeof(uint32_t) * (nb + 1));
+        H2D(e->d_bond_row, row, sizeof(uint32_t) * (nb + 1));
     else if (ce == cudaSuccess)
         ce = cudaMemsetAsync(e->d_bond_row.p, 0, sizeof(uint32_t) * (nb + 1), s);
-    H2D(e->d_bond_terms, terms.data(), sizeof(BondTerm) * n_terms);
+    H2D(e->d_bond_terms, terms, sizeof(BondTerm) * n_terms);
     if (f64) {
         H2D(e->d_bond_params, bp64.data(), sizeof(double) * bp64.size());
         H2D(e->d_pair, pair64.data(), sizeof(double) * pair64.size());
@@ -1056,9 +1208,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
         H2D(e->d_cellpair, cp32.data(), sizeof(float) * cp32.size());
     }
-    if (!any_kept) {
-        H2D(e->d_staging[0], hs, sizeof(double) * 9 * nb);
-    } else {  // only the rows of the worlds that come from their descriptors
+    if (any_kept) {  // only the rows of the worlds that come from their descriptors
         for (uint32_t i = 0; i < n_worlds; i++)
             if (keep_old[i] < 0 && ws[i].n_beads && ce == cudaSuccess)
                 ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
@@ -1071,9 +1221,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
                              snap + 9 * (size_t)old_base[keep_old[i]],
                              sizeof(double) * 9 * ws[i].n_beads, cudaMemcpyDeviceToDevice, s);
     }
-    if (!any_kept) {
-        H2D(e->d_hash, hh, sizeof(uint32_t) * nb);
-    } else {
+    if (any_kept) {
         for (uint32_t i = 0; i < n_worlds && ce == cudaSuccess; i++) {
             if (ws[i].n_beads == 0) continue;
             uint32_t *dst = e->d_hash.as<uint32_t>() + wdev[i].bead_base;
@@ -1252,6 +1400,49 @@ static void scatter(const double *src, uint32_t n, double *x, double *v, double 
     });
 }
 
+// Rows [r_begin, r_end) of device staging buffer 0 (9 doubles per bead, unsorted by the
+// kernels already on the stream) to pinned host staging and on to the caller: the worlds'
+// error flags are fetched first, then the rows go in chunks, each handed to scatter(r0, r1)
+// as soon as it has arrived, so the host scatter of one chunk overlaps the copy of the next.
+static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
+                     const std::function<void(const double *, size_t, size_t)> &scatter)
+{
+    const size_t n = r_end - r_begin;
+    if (e->h_staging[0].alloc(sizeof(double) * 9 * std::max<size_t>(1, n)) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    int rc = e->fetch_device_errors();
+    if (rc) return rc;
+    cudaEvent_t ev_err;
+    cudaEventCreateWithFlags(&ev_err, cudaEventDisableTiming);
+    cudaEventRecord(ev_err, e->stream);
+    const size_t CH = size_t(1) << 20;
+    const size_t nch = (n + CH - 1) / CH;
+    std::vector<cudaEvent_t> ev(nch);
+    double *dst = (double *)e->h_staging[0].p;
+    cudaError_t ce = cudaSuccess;
+    for (size_t k = 0; k < nch; k++) {
+        const size_t r0 = k * CH, r1 = std::min(n, r0 + CH);
+        cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(dst + 9 * r0, e->d_staging[0].as<double>() + 9 * (r_begin + r0),
+                                 sizeof(double) * 9 * (r1 - r0), cudaMemcpyDeviceToHost, e->stream);
+        cudaEventRecord(ev[k], e->stream);
+    }
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(ev_err);
+    rc = ce != cudaSuccess ? e->cuda_fail(ce, "download") : e->eval_device_errors();
+    for (size_t k = 0; k < nch; k++) {
+        if (rc == PDPD_OK) {
+            ce = cudaEventSynchronize(ev[k]);
+            if (ce != cudaSuccess) rc = e->cuda_fail(ce, "download");
+        }
+        if (rc == PDPD_OK) scatter(dst, k * CH, std::min(n, (k + 1) * CH));
+    }
+    if (rc != PDPD_OK) cudaStreamSynchronize(e->stream);
+    for (cudaEvent_t x : ev) cudaEventDestroy(x);
+    cudaEventDestroy(ev_err);
+    return rc;
+}
+
 int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
                     size_t stride, int64_t *t)
 {
@@ -1262,17 +1453,13 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     int rc = download_world(e, 0, world, e->stream);
     if (rc) return rc;
     const WorldDev &wd = e->worlds[world].dev;
-    size_t nbytes = sizeof(double) * 9 * (size_t)wd.n_beads;
-    if (e->h_staging[0].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
-        return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
-    if (nbytes) {
-        cudaError_t ce = cudaMemcpyAsync(e->h_staging[0].p, e->d_staging[0].as<double>() + 9 * (size_t)wd.bead_base,
-                                         nbytes, cudaMemcpyDeviceToHost, e->stream);
-        if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
-    }
-    rc = e->check_device_errors();  // synchronises
+    rc = read_rows(e, wd.bead_base, (size_t)wd.bead_base + wd.n_beads,
+                   [&](const double *src, size_t r0, size_t r1) {
+                       scatter(src + 9 * r0, (uint32_t)(r1 - r0), x ? vec_at_mut(x, stride, r0) : nullptr,
+                               v ? vec_at_mut(v, stride, r0) : nullptr, f ? vec_at_mut(f, stride, r0) : nullptr,
+                               stride);
+                   });
     if (rc) return rc;
-    scatter((const double *)e->h_staging[0].p, wd.n_beads, x, v, f, stride);
     if (t) *t = e->worlds[world].dev.t;
     return PDPD_OK;
 }
@@ -1287,32 +1474,26 @@ int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *o
     cudaSetDevice(e->device);
     int rc = download(e, 0, e->stream);
     if (rc) return rc;
-    const size_t nbytes = sizeof(double) * 9 * (size_t)e->n_beads;
-    if (e->h_staging[0].alloc(nbytes) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
-    if (nbytes) {
-        cudaError_t ce = cudaMemcpyAsync(e->h_staging[0].p, e->d_staging[0].p, nbytes, cudaMemcpyDeviceToHost,
-                                         e->stream);
-        if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
-    }
-    rc = e->check_device_errors();  // synchronises
-    if (rc) return rc;
-    // one pass over the batch's beads, split across host threads whatever the worlds' sizes
+    // each chunk of the batch's beads, split across host threads whatever the worlds' sizes
     const size_t sb = stride ? stride : 3 * sizeof(double);
-    const double *src = (const double *)e->h_staging[0].p;
     std::vector<uint32_t> base(n_worlds + 1);
     for (uint32_t i = 0; i < n_worlds; i++) base[i] = e->worlds[i].dev.bead_base;
     base[n_worlds] = e->n_beads;
-    parallel_for(e->n_beads, 1 << 16, [&](size_t g0, size_t g1) {
-        uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
-        for (size_t g = g0; g < g1; g++) {
-            while (g >= base[i + 1]) i++;
-            const size_t k = g - base[i];
-            const double *r = src + 9 * g;
-            if (out[i].x) memcpy((char *)out[i].x + sb * k, r, 3 * sizeof(double));
-            if (out[i].v) memcpy((char *)out[i].v + sb * k, r + 3, 3 * sizeof(double));
-            if (out[i].f) memcpy((char *)out[i].f + sb * k, r + 6, 3 * sizeof(double));
-        }
+    rc = read_rows(e, 0, e->n_beads, [&](const double *src, size_t c0, size_t c1) {
+        parallel_for(c1 - c0, 1 << 16, [&](size_t a0, size_t a1) {
+            const size_t g0 = c0 + a0, g1 = c0 + a1;
+            uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
+            for (size_t g = g0; g < g1; g++) {
+                while (g >= base[i + 1]) i++;
+                const size_t k = g - base[i];
+                const double *r = src + 9 * g;
+                if (out[i].x) memcpy((char *)out[i].x + sb * k, r, 3 * sizeof(double));
+                if (out[i].v) memcpy((char *)out[i].v + sb * k, r + 3, 3 * sizeof(double));
+                if (out[i].f) memcpy((char *)out[i].f + sb * k, r + 6, 3 * sizeof(double));
+            }
+        });
     });
+    if (rc) return rc;
     for (uint32_t i = 0; i < n_worlds; i++)
         if (out[i].t) *out[i].t = e->worlds[i].dev.t;
     return PDPD_OK;
@@ -2065,10 +2246,14 @@ void pdpd_server::run()
 {
     cudaSetDevice(eng->device);
     int b = 0;  // host snapshot buffer of the current epoch
+    double t_sync_end = -1;  // when the host saw the last epoch finish
     while (true) {
+        double waited = 0;  // time idle for want of jobs (not host overhead)
         {
             std::unique_lock<std::mutex> lk(mu);
+            const double t_w0 = now_s();
             cv.wait(lk, [&] { return stop || !pending.empty() || !active.empty() || !owed.empty(); });
+            waited = now_s() - t_w0;
             if (stop && pending.empty() && active.empty() && owed.empty()) break;
             // Membership changes only where every running job is at one of its interval
             // boundaries: the jobs' intervals stay in phase, epochs are whole intervals (a job
@@ -2099,7 +2284,9 @@ void pdpd_server::run()
             busy = true;
             st.max_active = std::max<uint32_t>(st.max_active, (uint32_t)active.size());
         }
-        if (changed) deliver();  // the re-pack needs the snapshot buffers and the old arena
+        // (the callbacks still owed read the pinned snapshot buffer of the previous epoch,
+        // which neither the re-pack nor the next epoch touches: they run below, while the next
+        // epoch computes; the re-pack itself waits for the snapshot copies out of the arena)
         int rc = repack();
         if (rc != PDPD_OK) {
             std::vector<ServerJob *> all;
@@ -2115,6 +2302,10 @@ void pdpd_server::run()
         if (epoch == UINT32_MAX) epoch = 0;  // only ended jobs: they leave at the next iteration
         const double t_epoch0 = now_s();
         if (epoch > 0) {
+            if (t_sync_end > 0) {  // host time between the previous epoch's end and this launch
+                std::lock_guard<std::mutex> lk(mu);
+                st.host_gap_s += std::max(0.0, t_epoch0 - t_sync_end - waited);
+            }
             cudaEventRecord(ev_step0, eng->stream);
             rc = pdpd_run_async(eng, epoch);
             cudaEventRecord(ev_step1, eng->stream);
@@ -2154,9 +2345,15 @@ void pdpd_server::run()
                 }
             }
         }
-        deliver();  // host callbacks of the previous epoch while this one computes
+        {
+            const double t_cb0 = now_s();
+            deliver();  // host callbacks of the previous epoch while this one computes
+            std::lock_guard<std::mutex> lk(mu);
+            st.callback_s += now_s() - t_cb0;
+        }
         if (epoch > 0) {
             if (rc == PDPD_OK) rc = pdpd_sync(eng);
+            t_sync_end = now_s();
             if (rc == PDPD_E_BOND_SNAPPED || rc == PDPD_E_BEAD_LOST) {
                 // worlds are independent: fail the ones that raised an error flag, keep the rest
                 const WorldDev *wd = (const WorldDev *)eng->h_err.p;

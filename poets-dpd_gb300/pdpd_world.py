@@ -55,6 +55,23 @@ class PolymerType:
     bond_pairs: list = field(default_factory=list)   # (head_bond, tail_bond, kappa, theta0)
 
 
+# The bead and polymer topology of a World: fixed once the World is built, as the reference
+# keeps a WorldState's types and polymers fixed while it is attached (dpd_engine.hpp:171-176).
+# These arrays are stored read-only (an assignment replaces one), so the arrays derived from
+# them -- the bead hashes and the flat bond lists, which every attach needs -- are computed
+# once and shared by the World's copies.
+_TOPOLOGY = ("poly_type", "poly_start", "poly_beads", "polymer_id", "polymer_offset", "bead_type",
+             "polymer_type_of_bead", "is_monomer")
+
+
+def _read_only(a):
+    if isinstance(a, np.ndarray) and not a.flags.writeable:
+        return a
+    v = np.asarray(a).view()
+    v.flags.writeable = False
+    return v
+
+
 @dataclass
 class World:
     box: np.ndarray                 # (3,) int32 box sides
@@ -90,26 +107,56 @@ class World:
     def n_types(self) -> int:
         return int(self.conservative.shape[0])
 
+    def __post_init__(self):
+        # the bead hashes and bond lists of a new topology, once (its copies share them)
+        self.hashes()
+        self.flat_bonds()
+
+    def __setattr__(self, name, value):
+        if name in _TOPOLOGY and value is not None:
+            value = _read_only(value)
+        object.__setattr__(self, name, value)
+
+    def _derived(self, what, fields, extra, make):
+        """make(), cached while the named topology arrays are the same objects (they are
+        read-only) and `extra` compares equal."""
+        cache = self.__dict__.setdefault("_cache", {})
+        arrays = tuple(getattr(self, k) for k in fields)
+        hit = cache.get(what)
+        if hit is not None and hit[1] == extra and all(a is b for a, b in zip(hit[0], arrays)):
+            return hit[2]
+        value = make()
+        value = tuple(_read_only(v) for v in value) if isinstance(value, tuple) else _read_only(value)
+        cache[what] = (arrays, extra, value)
+        return value
+
     def hashes(self) -> np.ndarray:
-        return bead_hash(self.bead_type, self.is_monomer, self.polymer_id, self.polymer_offset)
+        """BeadHash of every bead (read-only; computed once per topology)."""
+        return self._derived("hash", ("bead_type", "is_monomer", "polymer_id", "polymer_offset"), None,
+                             lambda: bead_hash(self.bead_type, self.is_monomer, self.polymer_id,
+                                               self.polymer_offset))
 
     def copy(self) -> "World":
-        return World(
+        """A copy with its own state (x, v, f, t, parameters); the read-only topology arrays
+        and what is derived from them are shared."""
+        w = World(
             box=self.box.copy(), dt=self.dt, lam=self.lam, seed=self.seed, t=self.t,
             conservative=self.conservative.copy(), dissipative=self.dissipative.copy(),
             stationary=self.stationary.copy(),
             polymer_types=[PolymerType(list(p.bead_types), list(p.bonds), list(p.bond_pairs))
                            for p in self.polymer_types],
-            poly_type=self.poly_type.copy(), poly_start=self.poly_start.copy(),
-            poly_beads=self.poly_beads.copy(), polymer_id=self.polymer_id.copy(),
-            polymer_offset=self.polymer_offset.copy(), bead_type=self.bead_type.copy(),
-            polymer_type_of_bead=self.polymer_type_of_bead.copy(),
-            is_monomer=self.is_monomer.copy(), x=self.x.copy(), v=self.v.copy(), f=self.f.copy(),
+            poly_type=self.poly_type, poly_start=self.poly_start, poly_beads=self.poly_beads,
+            polymer_id=self.polymer_id, polymer_offset=self.polymer_offset, bead_type=self.bead_type,
+            polymer_type_of_bead=self.polymer_type_of_bead, is_monomer=self.is_monomer,
+            x=self.x.copy(), v=self.v.copy(), f=self.f.copy(),
             cell_conservative=None if self.cell_conservative is None else self.cell_conservative.copy(),
             cell_dissipative=None if self.cell_dissipative is None else self.cell_dissipative.copy())
+        w.__dict__["_cache"] = dict(self.__dict__.get("_cache", {}))
+        return w
 
     def flat_bonds(self):
-        """Expand the polymer templates into flat bond and angle lists.
+        """Expand the polymer templates into flat bond and angle lists (read-only; computed
+        once per topology and polymer types).
 
         Returns ``(bond_beads (nb,2) uint32, bond_kappa, bond_r0, angle_beads (na,3) uint32,
         angle_kappa, angle_theta0)``.  Order: polymers in id order; within a polymer, bonds in
@@ -117,6 +164,11 @@ class World:
         to one polymer, so each bead sees its bond terms in the same order as the reference's
         per-polymer loop (naive_dpd_engine_half_step.hpp:321-329).
         """
+        types = tuple((tuple(p.bead_types), tuple(map(tuple, p.bonds)), tuple(map(tuple, p.bond_pairs)))
+                      for p in self.polymer_types)
+        return self._derived("bonds", ("poly_type", "poly_start", "poly_beads"), types, self._expand_bonds)
+
+    def _expand_bonds(self):
         bonds = {"beads": [], "kappa": [], "r0": [], "poly": []}
         angles = {"beads": [], "kappa": [], "theta0": [], "poly": []}
         with_terms = [i for i, pt in enumerate(self.polymer_types) if pt.bonds or pt.bond_pairs]

@@ -62,8 +62,9 @@ def test_can_support_rejections():
     assert "bead types" in E.can_support(b.build())
     # a bond to a bead that does not exist
     w = W.make_polymer_box(6, chain_fraction=0.1)
-    w.poly_beads = w.poly_beads.copy()
-    w.poly_beads[1] = w.n_beads + 5
+    pb = w.poly_beads.copy()  # the topology arrays are read-only: replace one
+    pb[1] = w.n_beads + 5
+    w.poly_beads = pb
     assert "does not exist" in E.can_support(w)
 
 

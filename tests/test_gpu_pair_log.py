@@ -86,13 +86,16 @@ def test_fp32_pair_log_within_fp32_precision():
     assert mine.keys() == ref.keys()
     fscale = np.sqrt(np.mean(np.sum(g["f"] ** 2, axis=1)))
     for key, ks in mine.items():
-        kr = ref[key]
+        # the FP32 cell lists hold a cell's lower-z-half beads first (then id order), so the
+        # pairs of one direction may come in another order: match them by partner
+        kr = [ref[key][i] for i in np.argsort(g["other_hash"][ref[key]], kind="stable")]
+        ks = [ks[i] for i in np.argsort(r["other_hash"][ks], kind="stable")]
         assert np.array_equal(r["other_hash"][ks], g["other_hash"][kr]), key
         assert np.array_equal(r["rng"][ks], g["rng"][kr])  # the RNG is bit-exact in FP32 too
         assert np.allclose(r["dr"][ks], g["dr"][kr], rtol=0, atol=1e-6)
         assert np.allclose(r["dx"][ks], g["dx"][kr], rtol=0, atol=1e-6)
         for name in ("con", "diss", "rand", "rng_scale", "gammap"):
-            assert np.allclose(r[name][ks], g[name][kr], rtol=1e-5, atol=1e-4 * fscale * 1e-2), (key, name)
+            assert np.allclose(r[name][ks], g[name][kr], rtol=1e-5, atol=1e-6 * fscale), (key, name)
         assert np.max(np.abs(r["f"][ks] - g["f"][kr])) <= 1e-5 * fscale, key
 
 
