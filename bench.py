@@ -361,6 +361,8 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "step_s": st["step_s"] - st0["step_s"],
             "host_gap_s": st["host_gap_s"] - st0["host_gap_s"],
             "callback_s": st["callback_s"] - st0["callback_s"],
+            "epochs": st["epochs"] - st0["epochs"],
+            "between_epochs_s": st["between_s"] - st0["between_s"],
             "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,

@@ -346,6 +346,9 @@ typedef struct pdpd_server_stats {
     double host_gap_s;     /* wall time from the host seeing an epoch finish to its launch of
                               the next (re-packs included): the GPU waits for the host */
     double callback_s;     /* wall time in job callbacks (they overlap the running epoch) */
+    uint64_t epochs;       /* batch runs between interval boundaries / job ends */
+    double between_s;      /* device time from one epoch's end to the next one's start
+                              (snapshot unsorts, re-packs, waits for the host), while busy */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.

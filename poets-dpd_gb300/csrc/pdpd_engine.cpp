@@ -2135,7 +2135,9 @@ struct pdpd_server {
     double repack_est_s = 0.005;  // recent re-pack time
     HostPinned snap[2];
     cudaEvent_t ev_unsorted = nullptr, ev_copied[2] = {nullptr, nullptr};
-    cudaEvent_t ev_step0 = nullptr, ev_step1 = nullptr;  // around an epoch's steps
+    cudaEvent_t ev_step0 = nullptr, ev_step1[2] = {nullptr, nullptr};  // around an epoch's steps
+    int end_k = 0;           // ev_step1[end_k]: the last epoch's end
+    bool have_end = false;
     std::thread worker;
 
     void run();
@@ -2308,7 +2310,7 @@ void pdpd_server::run()
             }
             cudaEventRecord(ev_step0, eng->stream);
             rc = pdpd_run_async(eng, epoch);
-            cudaEventRecord(ev_step1, eng->stream);
+            cudaEventRecord(ev_step1[end_k ^ 1], eng->stream);
             std::vector<size_t> at_boundary;
             for (size_t i = 0; i < active.size(); i++) {
                 ServerJob &j = *active[i];
@@ -2376,10 +2378,18 @@ void pdpd_server::run()
             }
             uint64_t stepped = 0, live_phase = 0;
             float step_ms = 0.f;
-            if (rc == PDPD_OK && cudaEventElapsedTime(&step_ms, ev_step0, ev_step1) != cudaSuccess) step_ms = 0.f;
+            float between_ms = 0.f;
+            if (rc == PDPD_OK && cudaEventElapsedTime(&step_ms, ev_step0, ev_step1[end_k ^ 1]) != cudaSuccess) step_ms = 0.f;
+            if (rc == PDPD_OK && have_end &&
+                cudaEventElapsedTime(&between_ms, ev_step1[end_k], ev_step0) != cudaSuccess)
+                between_ms = 0.f;
+            end_k ^= 1;
+            have_end = rc == PDPD_OK;
             {
                 std::lock_guard<std::mutex> lk(mu);
                 st.step_s += 1e-3 * step_ms;
+                st.between_s += 1e-3 * between_ms;
+                st.epochs++;
                 for (auto &j : active) {
                     stepped += (uint64_t)j->desc.n_beads * epoch;
                     if (!j->ended) st.bead_steps += (uint64_t)j->desc.n_beads * epoch;
@@ -2406,6 +2416,7 @@ void pdpd_server::run()
             b ^= 1;
         }
         if (active.empty() && owed.empty()) {
+            have_end = false;  // idle: the next epoch's distance from the last is not overhead
             repack();  // releases the arena
             std::lock_guard<std::mutex> lk(mu);
             if (busy) st.busy_s += now_s() - t_busy_from;
@@ -2439,7 +2450,8 @@ int pdpd_server_create(int precision, int device, size_t memory_budget_bytes, ui
     cudaEventCreateWithFlags(&s->ev_copied[0], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&s->ev_copied[1], cudaEventDisableTiming);
     cudaEventCreate(&s->ev_step0);
-    cudaEventCreate(&s->ev_step1);
+    cudaEventCreate(&s->ev_step1[0]);
+    cudaEventCreate(&s->ev_step1[1]);
     s->worker = std::thread([s] { s->run(); });
     *out = s;
     return PDPD_OK;
@@ -2591,7 +2603,8 @@ void pdpd_server_destroy(pdpd_server *s)
     cudaStreamSynchronize(s->eng->side);
     if (s->ev_unsorted) cudaEventDestroy(s->ev_unsorted);
     if (s->ev_step0) cudaEventDestroy(s->ev_step0);
-    if (s->ev_step1) cudaEventDestroy(s->ev_step1);
+    for (cudaEvent_t ev : s->ev_step1)
+        if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : s->ev_copied)
         if (ev) cudaEventDestroy(ev);
     s->snap[0].release();

@@ -123,7 +123,8 @@ class PdpdServerStats(C.Structure):
                 ("wall_s", C.c_double), ("latency_p50_s", C.c_double),
                 ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double),
                 ("repack_s", C.c_double), ("wasted_bead_steps", C.c_uint64),
-                ("step_s", C.c_double), ("host_gap_s", C.c_double), ("callback_s", C.c_double)]
+                ("step_s", C.c_double), ("host_gap_s", C.c_double), ("callback_s", C.c_double),
+                ("epochs", C.c_uint64), ("between_s", C.c_double)]
 
 
 INTERVAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)
