@@ -2320,17 +2320,21 @@ void pdpd_server::run()
                 if (j.done % interval == 0 || j.done == j.n_steps) at_boundary.push_back(i);
             }
             if (rc == PDPD_OK && !at_boundary.empty()) {
-                cudaEventSynchronize(ev_copied[b]);  // the buffer's last copy (normally long done)
+                // Snapshot b: the arena (or its worlds at a boundary) unsorted into device staging
+                // buffer b and copied from there to pinned buffer b on the side stream.  The last
+                // copy that read either buffer b is the one of two snapshots ago: once it is
+                // done, the unsort needs no wait on the copy still running out of the other pair
+                // (a job ending a few steps after an interval boundary would otherwise hold the
+                // GPU until the whole interval snapshot had crossed to the host).
+                cudaEventSynchronize(ev_copied[b]);  // (normally long done)
                 if (snap[b].alloc(sizeof(double) * 9 * (size_t)eng->n_beads) != cudaSuccess)
                     rc = eng->fail(PDPD_E_NOMEM, "pinned snapshot allocation failed");
-                // the previous copy out of the device staging rows must be done before the unsort
-                if (rc == PDPD_OK) cudaStreamWaitEvent(eng->stream, ev_copied[b ^ 1], 0);
                 // unsort the arena, or only the worlds at a boundary when they are few (a job
                 // ending mid-interval splits an epoch for its own snapshot)
-                if (rc == PDPD_OK && at_boundary.size() * 4 >= active.size()) rc = download(eng, 1, eng->stream);
+                if (rc == PDPD_OK && at_boundary.size() * 4 >= active.size()) rc = download(eng, b, eng->stream);
                 else
                     for (size_t i : at_boundary)
-                        if (rc == PDPD_OK) rc = download_world(eng, 1, active[i]->slot, eng->stream);
+                        if (rc == PDPD_OK) rc = download_world(eng, b, active[i]->slot, eng->stream);
                 if (rc == PDPD_OK) {
                     cudaEventRecord(ev_unsorted, eng->stream);
                     cudaStreamWaitEvent(eng->side, ev_unsorted, 0);
@@ -2339,7 +2343,7 @@ void pdpd_server::run()
                         const WorldDev &wd = eng->worlds[j.slot].dev;
                         const size_t row = 9 * (size_t)wd.bead_base;
                         if (wd.n_beads)
-                            cudaMemcpyAsync((double *)snap[b].p + row, eng->d_staging[1].as<double>() + row,
+                            cudaMemcpyAsync((double *)snap[b].p + row, eng->d_staging[b].as<double>() + row,
                                             sizeof(double) * 9 * wd.n_beads, cudaMemcpyDeviceToHost, eng->side);
                         next.push_back({&j, row, wd.n_beads, j.t, j.done == j.n_steps ? 1 : 0});
                     }

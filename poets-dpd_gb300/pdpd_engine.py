@@ -193,6 +193,18 @@ def _p(a):
     return a.ctypes.data if a is not None and a.size else None
 
 
+def _dest(world, name, n):
+    """Where a read-back of a World's x, v or f goes: its own array when that is a writable,
+    C-contiguous float64 (n, 3) array -- written in place, as the reference's engines write
+    the WorldState's beads (its pages are already mapped, unlike a new array's) -- else a new
+    array."""
+    a = getattr(world, name, None) if world is not None else None
+    if (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.shape == (n, 3)
+            and a.flags.c_contiguous and a.flags.writeable):
+        return a
+    return np.empty((n, 3))
+
+
 class _Flat:
     """Contiguous arrays of one World in the C ABI's layout, kept alive with the struct."""
 
@@ -464,8 +476,8 @@ class GB300DPDEngine:
         """Every attached world's x, v, f, t at once (one device unsort and copy); returns a
         list of (x, v, f, t), and writes them into the given Worlds when ``into`` is given."""
         n = len(self._worlds)
-        arrs = [(np.empty((w.n_beads, 3)), np.empty((w.n_beads, 3)), np.empty((w.n_beads, 3)))
-                for w in self._worlds]
+        dst = into if into is not None else [None] * n
+        arrs = [tuple(_dest(d, k, w.n_beads) for k in ("x", "v", "f")) for w, d in zip(self._worlds, dst)]
         ts = (C.c_int64 * max(1, n))()
         views = (PdpdStateView * max(1, n))()
         for i, (x, v, f) in enumerate(arrs):
@@ -481,9 +493,7 @@ class GB300DPDEngine:
     def read_state(self, world_index=0, into=None):
         """Copy world ``world_index``'s x, v, f, t to numpy (into a World when given)."""
         n = (self._worlds[world_index].n_beads if self._worlds else 0)
-        x = np.empty((n, 3))
-        v = np.empty((n, 3))
-        f = np.empty((n, 3))
+        x, v, f = (_dest(into, k, n) for k in ("x", "v", "f"))
         t = C.c_int64(0)
         self._check(lib().pdpd_read_state(self._h, world_index, _p(x), _p(v), _p(f), 24,
                                           C.byref(t)), "read_state")
