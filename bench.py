@@ -363,6 +363,10 @@ def serving_metrics(rate=50.0, window_s=4.0, budget=40 << 30, interval=100, seed
             "callback_s": st["callback_s"] - st0["callback_s"],
             "epochs": st["epochs"] - st0["epochs"],
             "between_epochs_s": st["between_s"] - st0["between_s"],
+            "copy_wait_s": st["copy_wait_s"] - st0["copy_wait_s"],
+            "sync_wait_s": st["sync_wait_s"] - st0["sync_wait_s"],
+            "snap_alloc_s": st["snap_alloc_s"] - st0["snap_alloc_s"],
+            "post_launch_s": st["post_launch_s"] - st0["post_launch_s"],
             "gpu_launches": launches,
             "sequential_fp32_bead_steps_per_s": seq32, "sequential_fp32_sample_jobs": n32,
             "sequential_fp64_bead_steps_per_s": seq64, "sequential_fp64_sample_jobs": n64,

@@ -349,11 +349,18 @@ typedef struct pdpd_server_stats {
     uint64_t epochs;       /* batch runs between interval boundaries / job ends */
     double between_s;      /* device time from one epoch's end to the next one's start
                               (snapshot unsorts, re-packs, waits for the host), while busy */
+    double copy_wait_s;    /* host wall time waiting for a snapshot buffer's last copy */
+    double sync_wait_s;    /* host wall time waiting for epochs to finish (the GPU is busy) */
+    double snap_alloc_s;   /* host wall time growing the pinned snapshot buffers */
+    double post_launch_s;  /* host wall time from an epoch's launch to its snapshot enqueued */
 } pdpd_server_stats;
 
 /* Create a server with its own engine (precision, device as pdpd_create) and worker thread.
  * memory_budget_bytes bounds the summed footprint estimate of the admitted jobs (a job larger
- * than the budget still runs, alone); interval_steps >= 1 is the snapshot interval. */
+ * than the budget still runs, alone); interval_steps >= 1 is the snapshot interval.  The
+ * server reserves two pinned host buffers for the snapshots of a batch that fills the budget
+ * (72 bytes per bead, at most 16 GiB each): creation takes a moment, later batches do not
+ * wait for host memory to be pinned. */
 int pdpd_server_create(int precision, int device, size_t memory_budget_bytes,
                        uint32_t interval_steps, pdpd_server **out);
 /* Queue a job: the world (copied; the caller's arrays may be reused at once) advanced by

@@ -185,10 +185,10 @@ struct DevBuf {
 struct HostPinned {
     void *p = nullptr;
     size_t bytes = 0;
-    cudaError_t alloc(size_t n)
+    cudaError_t alloc(size_t n, bool exact = false)
     {
         if (n <= bytes) return cudaSuccess;
-        if (p) n += n / 2;  // pinning is slow: grow by half again
+        if (p && !exact) n += n / 2;  // pinning is slow: grow by half again
         release();
         cudaError_t e = cudaMallocHost(&p, n);
         if (e != cudaSuccess) {
@@ -2326,9 +2326,22 @@ void pdpd_server::run()
                 // done, the unsort needs no wait on the copy still running out of the other pair
                 // (a job ending a few steps after an interval boundary would otherwise hold the
                 // GPU until the whole interval snapshot had crossed to the host).
-                cudaEventSynchronize(ev_copied[b]);  // (normally long done)
-                if (snap[b].alloc(sizeof(double) * 9 * (size_t)eng->n_beads) != cudaSuccess)
-                    rc = eng->fail(PDPD_E_NOMEM, "pinned snapshot allocation failed");
+                {
+                    const double t_c0 = now_s();
+                    cudaEventSynchronize(ev_copied[b]);  // (normally long done)
+                    std::lock_guard<std::mutex> lk(mu);
+                    st.copy_wait_s += now_s() - t_c0;
+                }
+                {
+                    // (reserved at creation for a batch that fills the budget; a job larger
+                    // than the budget, which runs alone, may need more)
+                    const double t_a0 = now_s();
+                    const size_t need = sizeof(double) * 9 * (size_t)eng->n_beads;
+                    if (need > snap[b].bytes && snap[b].alloc(need, true) != cudaSuccess)
+                        rc = eng->fail(PDPD_E_NOMEM, "pinned snapshot allocation failed");
+                    std::lock_guard<std::mutex> lk(mu);
+                    st.snap_alloc_s += now_s() - t_a0;
+                }
                 // unsort the arena, or only the worlds at a boundary when they are few (a job
                 // ending mid-interval splits an epoch for its own snapshot)
                 if (rc == PDPD_OK && at_boundary.size() * 4 >= active.size()) rc = download(eng, b, eng->stream);
@@ -2351,6 +2364,10 @@ void pdpd_server::run()
                 }
             }
         }
+        if (epoch > 0) {
+            std::lock_guard<std::mutex> lk(mu);
+            st.post_launch_s += now_s() - t_epoch0;
+        }
         {
             const double t_cb0 = now_s();
             deliver();  // host callbacks of the previous epoch while this one computes
@@ -2358,8 +2375,13 @@ void pdpd_server::run()
             st.callback_s += now_s() - t_cb0;
         }
         if (epoch > 0) {
+            const double t_s0 = now_s();
             if (rc == PDPD_OK) rc = pdpd_sync(eng);
             t_sync_end = now_s();
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                st.sync_wait_s += t_sync_end - t_s0;
+            }
             if (rc == PDPD_E_BOND_SNAPPED || rc == PDPD_E_BEAD_LOST) {
                 // worlds are independent: fail the ones that raised an error flag, keep the rest
                 const WorldDev *wd = (const WorldDev *)eng->h_err.p;
@@ -2456,6 +2478,23 @@ int pdpd_server_create(int precision, int device, size_t memory_budget_bytes, ui
     cudaEventCreate(&s->ev_step0);
     cudaEventCreate(&s->ev_step1[0]);
     cudaEventCreate(&s->ev_step1[1]);
+    // The two pinned snapshot buffers, reserved for the rows (x, v, f as doubles) of a batch
+    // that fills the budget, at most 16 GiB each.  Pinning host memory is slow: in a 20 s
+    // stream whose batch grew to the budget, buffers re-pinned as they grew (by half, then by
+    // 4x) held the GPU idle for 7%, then 4.5% of the wall time.
+    const size_t per_bead = precision == PDPD_FP64 ? 424 : 296;  // as job_bytes
+    const size_t full = std::min<size_t>(sizeof(double) * 9 * (memory_budget_bytes / per_bead), size_t(16) << 30);
+    for (HostPinned &h : s->snap)
+        if (h.alloc(std::max<size_t>(full, 4096), true) != cudaSuccess) {
+            g_last_error = "pinned snapshot buffers: allocation failed";
+            for (cudaEvent_t ev : {s->ev_unsorted, s->ev_copied[0], s->ev_copied[1], s->ev_step0, s->ev_step1[0],
+                                   s->ev_step1[1]})
+                cudaEventDestroy(ev);
+            for (HostPinned &x : s->snap) x.release();
+            pdpd_destroy(e);
+            delete s;
+            return PDPD_E_NOMEM;
+        }
     s->worker = std::thread([s] { s->run(); });
     *out = s;
     return PDPD_OK;

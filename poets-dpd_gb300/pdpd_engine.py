@@ -124,7 +124,9 @@ class PdpdServerStats(C.Structure):
                 ("latency_p99_s", C.c_double), ("latency_max_s", C.c_double),
                 ("repack_s", C.c_double), ("wasted_bead_steps", C.c_uint64),
                 ("step_s", C.c_double), ("host_gap_s", C.c_double), ("callback_s", C.c_double),
-                ("epochs", C.c_uint64), ("between_s", C.c_double)]
+                ("epochs", C.c_uint64), ("between_s", C.c_double), ("copy_wait_s", C.c_double),
+                ("sync_wait_s", C.c_double), ("snap_alloc_s", C.c_double),
+                ("post_launch_s", C.c_double)]
 
 
 INTERVAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)
