@@ -496,24 +496,39 @@ def upload_bytes(worlds):
     return total
 
 
+ISSUE_SLOTS_PER_S = 152 * 4 * 2.07e9  # warp-instruction issue slots per second of a GB300
+
+
 def force_roofline(phases, beads, precision, traffic_key=None):
     """Roofline of the force pass from profile_run's per-phase CUDA-event times; traffic from
     the ncu capture summarised in profiles/force_kernel_traffic.json (per bead-step)."""
     force_ms = phases["force_ms"] / max(1, phases["force_launches"])
     peak, peak_kind = measured_peaks()
     achieved = ALGO_BYTES[precision] * beads / (force_ms / 1e3) / 1e9
-    traffic = None
+    traffic = instr = None
     tpath = os.path.join(ROOT, "profiles", "force_kernel_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
             tj = json.load(fh)
-        key = f"{traffic_key or precision}_bytes_per_bead_step"
-        if key in tj:
-            traffic = tj[key] * beads
+        key = traffic_key or precision
+        if f"{key}_bytes_per_bead_step" in tj:
+            traffic = tj[f"{key}_bytes_per_bead_step"] * beads
+        if f"{key}_warp_instructions_per_bead_step" in tj:
+            instr = tj[f"{key}_warp_instructions_per_bead_step"]
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "kernel": "force", "kernel_ms": force_ms,
             "algo_bytes_per_bead_step": ALGO_BYTES[precision], "peak_source": peak_kind,
             "compulsory_frac": COMPULSORY_BYTES * beads / (force_ms / 1e3) / 1e9 / peak}
+    if traffic is not None:
+        # what the kernel really moves: its ncu DRAM bytes over the same time
+        roof["dram_gbs"] = traffic / (force_ms / 1e3) / 1e9
+        roof["dram_frac"] = roof["dram_gbs"] / peak
+    if instr is not None:
+        # the bound that applies: one warp instruction per SMSP per clock
+        # (GB300: 152 SMs x 4 SMSPs x 2.07 GHz), the kernel's ncu instructions per bead
+        cap = ISSUE_SLOTS_PER_S
+        roof["issue"] = {"warp_instructions_per_bead_step": instr, "slots_per_s": cap,
+                         "frac": instr * beads / (force_ms / 1e3) / cap}
     ph = {"force": force_ms, "sort": phases["sort_ms"] / max(1, phases["sort_launches"])}
     return roof, ph
 

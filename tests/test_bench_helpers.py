@@ -40,6 +40,11 @@ def test_force_roofline_arithmetic():
     assert roof["achieved"] == pytest.approx(1180.0 * 1e6 / 2e-3 / 1e9)
     assert roof["frac"] == pytest.approx(roof["achieved"] / roof["peak"])
     assert roof["bound"] == "hbm" and roof["unit"] == "GB/s"
+    # beside the model: the kernel's ncu DRAM bytes and instructions per bead over the same time
+    assert roof["dram_gbs"] == pytest.approx(roof["traffic"] / 2e-3 / 1e9)
+    issue = roof["issue"]
+    assert issue["frac"] == pytest.approx(issue["warp_instructions_per_bead_step"] * 1e6 / 2e-3 /
+                                          bench.ISSUE_SLOTS_PER_S)
 
 
 def test_grid_workload_name_names_the_grid():
