@@ -238,6 +238,33 @@ def oracle_rate_multi(worlds, max_seconds=12.0, max_steps=200, threads=None):
     return sum(w.n_beads for w in worlds) * steps / dt, threads, steps, dt
 
 
+def batched_fp64_metrics(worlds, steps=10, device=0):
+    """All states on one FP64 engine (the bit-exact precision, batched): the like-for-like
+    counterpart of the FP32 headline, CUDA events around the run on the engine's stream."""
+    import torch
+
+    import pdpd_engine as E
+
+    dev = torch.device("cuda", device)
+    total = sum(w.n_beads for w in worlds)
+    e64 = E.GB300DPDEngine("fp64", device=device)
+    s64 = torch.cuda.ExternalStream(e64.stream(), device=dev)
+    e64.AttachBatch([w.copy() for w in worlds])
+    e64.run_async(3)
+    e64.sync()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s64)
+    e64.run_async(steps)
+    b.record(s64)
+    e64.sync()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    e64.close()
+    return {"value": total * steps / (ms / 1e3), "unit": "bead-steps/s", "steps": steps,
+            "note": "every state attached to one FP64 engine (bit-exact with the reference), "
+                    "stepped together"}
+
+
 def plain_fp64_metrics(worlds, plain_steps=10, device=0):
     """The plain FP64 engine run one state at a time (Attach excluded from the time, as the
     reference's bpsExec), `plain_steps` steps per state, CUDA events around each Run."""
@@ -621,6 +648,8 @@ def measure_grid(args, dev, local, world_size):
     value = aggregate_rate(total * args.steps, ms, world_size)
     if plain:
         plain["batched_vs_plain"] = value / world_size / plain["value"]
+        plain["batched_fp64"] = batched_fp64_metrics(worlds, device=local)
+        plain["batched_fp64_vs_plain"] = plain["batched_fp64"]["value"] / plain["value"]
     return {"value": value, "ms": ms, "beads": total, "e2e": e2e, "launches": launches,
             "clocks": clocks, "roofline": roof, "phases": ph, "tuned": tuned, "plain_fp64": plain,
             "config": {"workload": grid_workload_name(n_states), "states": n_states,
