@@ -719,8 +719,13 @@ static int check_world(const pdpd_world *w, char *reason, size_t n, bool fresh =
     if (w->n_angles && (!w->angle_beads || !w->angle_kappa || !w->angle_theta0))
         return say(PDPD_E_INVALID, "Missing angle-bond arrays.");
     if (!fresh) return PDPD_OK;
-    for (uint32_t i = 0; i < w->n_beads; i++)
-        if ((w->hash[i] >> 28) >= w->n_bead_types) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
+    bool bad_type = false;  // (a large world's beads checked in parallel chunks)
+    parallel_for(w->n_beads, 1 << 18, [&](size_t i0, size_t i1) {
+        bool bad = false;
+        for (size_t i = i0; i < i1; i++) bad |= (w->hash[i] >> 28) >= w->n_bead_types;
+        if (bad) __atomic_store_n(&bad_type, true, __ATOMIC_RELAXED);
+    });
+    if (bad_type) return say(PDPD_E_INVALID, "Bead hash has a bead type out of range.");
     for (uint32_t k = 0; k < 2 * w->n_bonds; k++)
         if (w->bond_beads[k] >= w->n_beads) return say(PDPD_E_INVALID, "Bond refers to a bead that does not exist.");
     for (uint32_t k = 0; k < 3 * w->n_angles; k++)
@@ -968,28 +973,57 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
     // the flat list order.
     // (no bond terms at all, e.g. pure water: the rows are all zero and are set on the device)
-    // Rows and terms are built in pinned memory (uploaded from there, asynchronously); a
-    // world's terms name only its own beads, so the worlds' rows are counted in parallel.
+    // Rows and terms are built in pinned memory (uploaded from there, asynchronously), in
+    // passes over all the batch's bond and angle terms split across host threads whatever the
+    // worlds' sizes (one large world as fast as many small ones): counts by atomic increments,
+    // a prefix, terms placed through atomic per-bead cursors, then each bead's few terms put
+    // in flat-list order.
+    // Parameters: every world's Hookean bonds in order, then every world's angle bonds.
+    std::vector<uint32_t> bond_off(n_worlds + 1, 0), angle_off(n_worlds + 1, 0);
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        bond_off[i + 1] = bond_off[i] + ws[i].n_bonds;
+        angle_off[i + 1] = angle_off[i] + ws[i].n_angles;
+    }
+    const uint32_t n_bond_par = bond_off[n_worlds], n_angle_par = angle_off[n_worlds];
+    // fn(world, k) for the global terms [g0, g1) of a per-world list with offsets off
+    auto over_terms = [&](const std::vector<uint32_t> &off, size_t n, auto fn) {
+        parallel_for(n, 1 << 14, [&](size_t g0, size_t g1) {
+            uint32_t i = (uint32_t)(std::upper_bound(off.begin(), off.end(), (uint32_t)g0) - off.begin()) - 1;
+            for (size_t g = g0; g < g1; g++) {
+                while (g >= off[i + 1]) i++;
+                fn(i, (uint32_t)(g - off[i]), (uint32_t)g);
+            }
+        });
+    };
     uint32_t *row = nullptr;
     BondTerm *terms = nullptr;
+    std::unique_ptr<uint32_t[]> fill(n_terms ? new uint32_t[nb] : nullptr);  // per-bead cursors
+    std::vector<double> bp64(f64 ? 4 * (size_t)n_bparams : 0);
+    std::vector<float> bp32(f64 ? 0 : 4 * (size_t)n_bparams);
+    auto put = [&](uint32_t pidx, const double p[4]) {
+        for (int q = 0; q < 4; q++) {
+            if (f64) bp64[4 * (size_t)pidx + q] = p[q];
+            else bp32[4 * (size_t)pidx + q] = (float)p[q];
+        }
+    };
     if (n_terms) {
         const size_t row_bytes = (sizeof(uint32_t) * (nb + 1) + 15) & ~size_t(15);
         if (e->h_meta.alloc(row_bytes + sizeof(BondTerm) * n_terms) != cudaSuccess)
             return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
         row = (uint32_t *)e->h_meta.p;
         terms = (BondTerm *)((char *)e->h_meta.p + row_bytes);
-        row[0] = 0;
-        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
-            for (size_t i = i0; i < i1; i++) {
-                const pdpd_world &w = ws[i];
-                const uint32_t bb = wdev[i].bead_base;
-                memset(row + bb + 1, 0, sizeof(uint32_t) * w.n_beads);
-                for (uint32_t k = 0; k < 2 * w.n_bonds; k++) row[bb + w.bond_beads[k] + 1]++;
-                for (uint32_t k = 0; k < 3 * w.n_angles; k++) row[bb + w.angle_beads[k] + 1]++;
-            }
+        parallel_for(nb + 1, 1 << 18, [&](size_t i0, size_t i1) { memset(row + i0, 0, sizeof(uint32_t) * (i1 - i0)); });
+        auto bump = [&](uint32_t g) { __atomic_fetch_add(row + g + 1, 1u, __ATOMIC_RELAXED); };
+        over_terms(bond_off, n_bond_par, [&](uint32_t i, uint32_t k, uint32_t) {
+            const uint32_t bb = wdev[i].bead_base;
+            bump(bb + ws[i].bond_beads[2 * k]);
+            bump(bb + ws[i].bond_beads[2 * k + 1]);
         });
-    }
-    if (n_terms) {  // inclusive prefix of row[1..nb] in parallel chunks: chunk sums, then offsets
+        over_terms(angle_off, n_angle_par, [&](uint32_t i, uint32_t k, uint32_t) {
+            const uint32_t bb = wdev[i].bead_base;
+            for (int q = 0; q < 3; q++) bump(bb + ws[i].angle_beads[3 * k + q]);
+        });
+        // inclusive prefix of row[1..nb] in parallel chunks: chunk sums, then offsets
         const size_t n = nb, chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
         const size_t per = (n + chunks - 1) / chunks;
         std::vector<uint32_t> part(chunks + 1, 0);
@@ -1007,54 +1041,47 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
                 for (size_t i = c * per; i < std::min(n, (c + 1) * per); i++) row[i + 1] = acc += row[i + 1];
             }
         });
-    }
-    std::unique_ptr<uint32_t[]> fill(n_terms ? new uint32_t[nb] : nullptr);  // per-bead cursors
-    if (n_terms)
         parallel_for(nb, 1 << 18, [&](size_t i0, size_t i1) {
             memcpy(fill.get() + i0, row + i0, sizeof(uint32_t) * (i1 - i0));
         });
-    // Parameters: every world's Hookean bonds in order, then every world's angle bonds.  The
-    // worlds' terms fill disjoint CSR rows, so the worlds are filled in parallel.
-    std::vector<uint32_t> bond_off(n_worlds + 1, 0), angle_off(n_worlds + 1, 0);
-    for (uint32_t i = 0; i < n_worlds; i++) {
-        bond_off[i + 1] = bond_off[i] + ws[i].n_bonds;
-        angle_off[i + 1] = angle_off[i] + ws[i].n_angles;
-    }
-    const uint32_t n_bond_par = bond_off[n_worlds];
-    std::vector<double> bp64(f64 ? 4 * (size_t)n_bparams : 0);
-    std::vector<float> bp32(f64 ? 0 : 4 * (size_t)n_bparams);
-    auto put = [&](uint32_t pidx, const double p[4]) {
-        for (int q = 0; q < 4; q++) {
-            if (f64) bp64[4 * (size_t)pidx + q] = p[q];
-            else bp32[4 * (size_t)pidx + q] = (float)p[q];
-        }
-    };
-    if (n_terms)
-        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
-            for (size_t i = i0; i < i1; i++) {
-                const pdpd_world &w = ws[i];
-                const uint32_t bb = wdev[i].bead_base;
-                for (uint32_t k = 0; k < w.n_bonds; k++) {
-                    const uint32_t pidx = bond_off[i] + k;
-                    uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
-                    terms[fill[h]++] = {0u | (0u << 8), t, t, pidx};
-                    terms[fill[t]++] = {0u | (1u << 8), h, h, pidx};
-                    const double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
-                    put(pidx, p);
-                }
-                for (uint32_t k = 0; k < w.n_angles; k++) {
-                    const uint32_t pidx = n_bond_par + angle_off[i] + k;
-                    uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
-                             t = bb + w.angle_beads[3 * k + 2];
-                    terms[fill[h]++] = {1u | (0u << 8), m, t, pidx};
-                    terms[fill[m]++] = {1u | (1u << 8), h, t, pidx};
-                    terms[fill[t]++] = {1u | (2u << 8), h, m, pidx};
-                    const double th = w.angle_theta0[k];
-                    const double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
-                    put(pidx, p);
+        auto slot = [&](uint32_t g) { return __atomic_fetch_add(fill.get() + g, 1u, __ATOMIC_RELAXED); };
+        over_terms(bond_off, n_bond_par, [&](uint32_t i, uint32_t k, uint32_t pidx) {
+            const pdpd_world &w = ws[i];
+            const uint32_t bb = wdev[i].bead_base;
+            const uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
+            terms[slot(h)] = {0u | (0u << 8), t, t, pidx};
+            terms[slot(t)] = {0u | (1u << 8), h, h, pidx};
+            const double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
+            put(pidx, p);
+        });
+        over_terms(angle_off, n_angle_par, [&](uint32_t i, uint32_t k, uint32_t g) {
+            const pdpd_world &w = ws[i];
+            const uint32_t bb = wdev[i].bead_base;
+            const uint32_t pidx = n_bond_par + g;
+            const uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
+                           t = bb + w.angle_beads[3 * k + 2];
+            terms[slot(h)] = {1u | (0u << 8), m, t, pidx};
+            terms[slot(m)] = {1u | (1u << 8), h, t, pidx};
+            terms[slot(t)] = {1u | (2u << 8), h, m, pidx};
+            const double th = w.angle_theta0[k];
+            const double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
+            put(pidx, p);
+        });
+        // each bead's terms in flat-list order (parameter index, then role): the order the
+        // threads placed them in is arbitrary, a bead has only a few
+        parallel_for(nb, 1 << 16, [&](size_t b0, size_t b1) {
+            for (size_t bd = b0; bd < b1; bd++) {
+                BondTerm *t0 = terms + row[bd], *t1 = terms + row[bd + 1];
+                for (BondTerm *x = t0 + 1; x < t1; x++) {
+                    const BondTerm v = *x;
+                    BondTerm *y = x;
+                    for (; y > t0 && (y[-1].param > v.param || (y[-1].param == v.param && y[-1].meta > v.meta)); y--)
+                        *y = y[-1];
+                    *y = v;
                 }
             }
         });
+    }
     // The per-bead order is this bead's Hookean terms in flat order, then its angle terms in
     // flat order: each bead belongs to one world, whose bonds are filled before its angles.
 
