@@ -739,12 +739,6 @@ static const double *vec_at(const double *base, size_t stride_bytes, uint32_t i)
     return (const double *)((const char *)base + s * (size_t)i);
 }
 
-static double *vec_at_mut(double *base, size_t stride_bytes, size_t i)
-{
-    size_t s = stride_bytes ? stride_bytes : 3 * sizeof(double);
-    return (double *)((char *)base + s * i);
-}
-
 // ------------------------------------------------------------------------------------------
 // C ABI
 
@@ -836,7 +830,7 @@ int pdpd_attach(pdpd_engine *e, const pdpd_world *w)
     return pdpd_attach_batch(e, w, 1);
 }
 
-static int download(pdpd_engine *e, int buf, cudaStream_t s);
+static int download(pdpd_engine *e, int buf, cudaStream_t s, bool fields);
 
 // Attach a batch.  keep_old (optional, one entry per world): index of a world of the
 // currently attached batch whose bead state (x, v, f) the new world takes over on the device
@@ -860,7 +854,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         for (uint32_t i = 0; i < n_worlds; i++)
             if (keep_old[i] >= (int32_t)e->worlds.size())
                 return e->fail(PDPD_E_INVALID, "re-pack refers to a world that is not attached");
-        int rc = download(e, 1, e->stream);
+        int rc = download(e, 1, e->stream, false);
         if (rc) return rc;
         snap = e->d_staging[1].as<double>();
         for (const WorldHost &wh : e->worlds) old_base.push_back(wh.dev.bead_base);
@@ -1385,21 +1379,27 @@ void *pdpd_stream(pdpd_engine *e)
     return e ? (void *)e->stream : nullptr;
 }
 
-static int download(pdpd_engine *e, int buf, cudaStream_t s)
+// fields: write the staging buffer field-major (the x of every bead, then every v, then
+// every f) instead of in rows of 9 doubles.
+static int download(pdpd_engine *e, int buf, cudaStream_t s, bool fields = false)
 {
     KArgs a = e->args;
     if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
         return e->fail(PDPD_E_NOMEM, "staging allocation failed");
     a.staging = e->d_staging[buf].as<double>();
+    a.staging_fields = fields ? 1u : 0u;
+    a.staging_n = e->n_beads;
     e->launches += e->fp64() ? launch_unsort64(a, s, 0, e->n_beads) : launch_unsort32(a, s);
     return PDPD_OK;
 }
 
 // Unsort one world only (its own work tiles) into device staging buffer `buf`: the rows
 // of its beads, so reading every world of a batch in turn costs one pass over the arena.
-static int download_world(pdpd_engine *e, int buf, uint32_t world, cudaStream_t s)
+static int download_world(pdpd_engine *e, int buf, uint32_t world, cudaStream_t s, bool fields = false)
 {
     KArgs a = e->args;
+    a.staging_fields = fields ? 1u : 0u;
+    a.staging_n = e->n_beads;
     if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
         return e->fail(PDPD_E_NOMEM, "staging allocation failed");
     uint32_t first = 0;
@@ -1427,14 +1427,16 @@ static void scatter(const double *src, uint32_t n, double *x, double *v, double 
     });
 }
 
-// Rows [r_begin, r_end) of device staging buffer 0 (9 doubles per bead, unsorted by the
-// kernels already on the stream) to pinned host staging and on to the caller: the worlds'
-// error flags are fetched first, then the rows go in chunks, each handed to scatter(r0, r1)
-// as soon as it has arrived, so the host scatter of one chunk overlaps the copy of the next.
+// Beads [r_begin, r_end) of device staging buffer 0, written field-major by the unsort
+// kernels already on the stream (download(..., true)), to pinned host staging (field-major
+// too: n x's, n v's, n f's, n = r_end - r_begin) and on to the caller: the worlds' error
+// flags are fetched first, then the beads go in chunks, each handed to scatter(host, n, r0,
+// r1) as soon as its x, v and f have arrived, so the host copies of one chunk overlap the
+// transfer of the next.
 static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
-                     const std::function<void(const double *, size_t, size_t)> &scatter)
+                     const std::function<void(const double *, size_t, size_t, size_t)> &scatter)
 {
-    const size_t n = r_end - r_begin;
+    const size_t n = r_end - r_begin, nd = e->n_beads;
     if (e->h_staging[0].alloc(sizeof(double) * 9 * std::max<size_t>(1, n)) != cudaSuccess)
         return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
     int rc = e->fetch_device_errors();
@@ -1446,13 +1448,14 @@ static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
     const size_t nch = (n + CH - 1) / CH;
     std::vector<cudaEvent_t> ev(nch);
     double *dst = (double *)e->h_staging[0].p;
+    const double *src = e->d_staging[0].as<double>();
     cudaError_t ce = cudaSuccess;
     for (size_t k = 0; k < nch; k++) {
         const size_t r0 = k * CH, r1 = std::min(n, r0 + CH);
         cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
-        if (ce == cudaSuccess)
-            ce = cudaMemcpyAsync(dst + 9 * r0, e->d_staging[0].as<double>() + 9 * (r_begin + r0),
-                                 sizeof(double) * 9 * (r1 - r0), cudaMemcpyDeviceToHost, e->stream);
+        for (int q = 0; q < 3 && ce == cudaSuccess; q++)  // x, v, f of the chunk's beads
+            ce = cudaMemcpyAsync(dst + 3 * (q * n + r0), src + 3 * (q * nd + r_begin + r0),
+                                 sizeof(double) * 3 * (r1 - r0), cudaMemcpyDeviceToHost, e->stream);
         cudaEventRecord(ev[k], e->stream);
     }
     if (ce == cudaSuccess) ce = cudaEventSynchronize(ev_err);
@@ -1462,12 +1465,30 @@ static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
             ce = cudaEventSynchronize(ev[k]);
             if (ce != cudaSuccess) rc = e->cuda_fail(ce, "download");
         }
-        if (rc == PDPD_OK) scatter(dst, k * CH, std::min(n, (k + 1) * CH));
+        if (rc == PDPD_OK) scatter(dst, n, k * CH, std::min(n, (k + 1) * CH));
     }
     if (rc != PDPD_OK) cudaStreamSynchronize(e->stream);
     for (cudaEvent_t x : ev) cudaEventDestroy(x);
     cudaEventDestroy(ev_err);
     return rc;
+}
+
+// Beads [k0, k1) of one world from field-major host staging (x block at hx, v at hv, f at
+// hf, indexed by the world's bead index) into the caller's vectors of byte stride sb (24:
+// packed, copied as one block per vector).
+static void copy_out(const double *hx, const double *hv, const double *hf, size_t k0, size_t k1, double *x,
+                     double *v, double *f, size_t sb)
+{
+    const double *src[3] = {hx, hv, hf};
+    double *out[3] = {x, v, f};
+    for (int q = 0; q < 3; q++) {
+        if (!out[q]) continue;
+        if (sb == 3 * sizeof(double)) {
+            memcpy(out[q] + 3 * k0, src[q] + 3 * k0, sizeof(double) * 3 * (k1 - k0));
+        } else {
+            for (size_t k = k0; k < k1; k++) memcpy((char *)out[q] + sb * k, src[q] + 3 * k, 3 * sizeof(double));
+        }
+    }
 }
 
 int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
@@ -1477,14 +1498,15 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
     if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
     cudaSetDevice(e->device);
-    int rc = download_world(e, 0, world, e->stream);
+    int rc = download_world(e, 0, world, e->stream, true);
     if (rc) return rc;
     const WorldDev &wd = e->worlds[world].dev;
+    const size_t sb = stride ? stride : 3 * sizeof(double);
     rc = read_rows(e, wd.bead_base, (size_t)wd.bead_base + wd.n_beads,
-                   [&](const double *src, size_t r0, size_t r1) {
-                       scatter(src + 9 * r0, (uint32_t)(r1 - r0), x ? vec_at_mut(x, stride, r0) : nullptr,
-                               v ? vec_at_mut(v, stride, r0) : nullptr, f ? vec_at_mut(f, stride, r0) : nullptr,
-                               stride);
+                   [&](const double *h, size_t n, size_t r0, size_t r1) {
+                       parallel_for(r1 - r0, 1 << 15, [&](size_t a0, size_t a1) {
+                           copy_out(h, h + 3 * n, h + 6 * n, r0 + a0, r0 + a1, x, v, f, sb);
+                       });
                    });
     if (rc) return rc;
     if (t) *t = e->worlds[world].dev.t;
@@ -1499,24 +1521,23 @@ int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *o
     if (n_worlds != e->worlds.size())
         return e->fail(PDPD_E_INVALID, "%u views for a batch of %zu worlds", n_worlds, e->worlds.size());
     cudaSetDevice(e->device);
-    int rc = download(e, 0, e->stream);
+    int rc = download(e, 0, e->stream, true);
     if (rc) return rc;
     // each chunk of the batch's beads, split across host threads whatever the worlds' sizes
     const size_t sb = stride ? stride : 3 * sizeof(double);
     std::vector<uint32_t> base(n_worlds + 1);
     for (uint32_t i = 0; i < n_worlds; i++) base[i] = e->worlds[i].dev.bead_base;
     base[n_worlds] = e->n_beads;
-    rc = read_rows(e, 0, e->n_beads, [&](const double *src, size_t c0, size_t c1) {
-        parallel_for(c1 - c0, 1 << 16, [&](size_t a0, size_t a1) {
+    rc = read_rows(e, 0, e->n_beads, [&](const double *h, size_t n, size_t c0, size_t c1) {
+        parallel_for(c1 - c0, 1 << 15, [&](size_t a0, size_t a1) {
             const size_t g0 = c0 + a0, g1 = c0 + a1;
             uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
-            for (size_t g = g0; g < g1; g++) {
+            for (size_t g = g0; g < g1;) {
                 while (g >= base[i + 1]) i++;
-                const size_t k = g - base[i];
-                const double *r = src + 9 * g;
-                if (out[i].x) memcpy((char *)out[i].x + sb * k, r, 3 * sizeof(double));
-                if (out[i].v) memcpy((char *)out[i].v + sb * k, r + 3, 3 * sizeof(double));
-                if (out[i].f) memcpy((char *)out[i].f + sb * k, r + 6, 3 * sizeof(double));
+                const size_t b = base[i], e1 = std::min<size_t>(g1, base[i + 1]);
+                copy_out(h + 3 * b, h + 3 * (n + b), h + 3 * (2 * n + b), g - b, e1 - b, out[i].x, out[i].v,
+                         out[i].f, sb);
+                g = e1;
             }
         });
     });

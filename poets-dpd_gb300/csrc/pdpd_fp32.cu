@@ -815,16 +815,19 @@ __global__ void __launch_bounds__(TILE_BEADS) k_unsort32(KArgs a)
         const float4 f = ((const float4 *)a.frc)[s];
         int c[3];
         decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-        double *st = a.staging + 9 * (size_t)a.ids[s];
+        // rows of 9 doubles, or field-major blocks (x, v, f) of staging_n beads each
+        const size_t id = a.ids[s];
+        const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
+        double *st = a.staging + stride * id;
         st[0] = (double)c[0] + (double)p.x;
         st[1] = (double)c[1] + (double)p.y;
         st[2] = (double)c[2] + (double)p.z;
-        st[3] = v.x;
-        st[4] = v.y;
-        st[5] = v.z;
-        st[6] = f.x;
-        st[7] = f.y;
-        st[8] = f.z;
+        st[field + 0] = v.x;
+        st[field + 1] = v.y;
+        st[field + 2] = v.z;
+        st[2 * field + 0] = f.x;
+        st[2 * field + 1] = f.y;
+        st[2 * field + 2] = f.z;
     }
 }
 

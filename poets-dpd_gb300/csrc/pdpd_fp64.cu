@@ -687,16 +687,19 @@ __global__ void k_unsort64(KArgs a, uint32_t first, uint32_t count)
     const Vec4d p = ((const Vec4d *)a.posA)[s];
     const Vec4d v = ((const Vec4d *)a.velA)[s];
     const Vec4d f = ((const Vec4d *)a.frc)[s];
-    double *st = a.staging + 9 * (size_t)a.ids[s];
+    const size_t id = a.ids[s];
+    // rows of 9 doubles, or field-major blocks (x, v, f) of staging_n beads each
+    const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
+    double *st = a.staging + stride * id;
     st[0] = p.x;
     st[1] = p.y;
     st[2] = p.z;
-    st[3] = v.x;
-    st[4] = v.y;
-    st[5] = v.z;
-    st[6] = f.x;
-    st[7] = f.y;
-    st[8] = f.z;
+    st[field + 0] = v.x;
+    st[field + 1] = v.y;
+    st[field + 2] = v.z;
+    st[2 * field + 0] = f.x;
+    st[2 * field + 1] = f.y;
+    st[2 * field + 2] = f.z;
 }
 
 }  // namespace

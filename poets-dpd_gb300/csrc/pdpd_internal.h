@@ -110,8 +110,12 @@ struct KArgs {
     float4 *posf;                // FP64: (x - floor(x), hash) in FP32, by sorted slot: the
                                  // neighbour walk's distance prefilter
     void *bterm;                 // FP64: each bond term's force (Vec4d), by CSR row
-    // id-ordered staging for upload / download: 9 doubles per bead (x, v, f)
+    // id-ordered staging for upload / download: 9 doubles per bead (x, v, f), or, for the
+    // read-backs with staging_fields set, field-major: the x of every bead (3 doubles each),
+    // then every v, then every f (staging_n beads per field)
     double *staging;
+    uint32_t staging_fields;
+    uint32_t staging_n;
     int block_threads;
     int grid_blocks;     // persistent grid size for the tile kernels
     int list_capacity;   // neighbour-list capacity per bead (0 = the kernel's default)
