@@ -208,41 +208,56 @@ def _dest(world, name, n):
 
 
 class _Flat:
-    """Contiguous arrays of one World in the C ABI's layout, kept alive with the struct."""
+    """Contiguous arrays of one World in the C ABI's layout, kept alive with the struct.  The
+    topology part (bead hashes, flat bond lists: read-only arrays a World computes once) is
+    laid into a struct template kept with the World and shared by its copies; each call fills
+    in the state and parameters."""
 
     def __init__(self, world):
+        tmpl, self.topo = _topology_struct(world)
         self.cons = np.ascontiguousarray(world.conservative, np.float64)
         self.diss = np.ascontiguousarray(world.dissipative, np.float64)
         self.stat = np.ascontiguousarray(world.stationary, np.uint8)
-        self.hash = np.ascontiguousarray(world.hashes(), np.uint32)
         self.x = np.ascontiguousarray(world.x, np.float64)
         self.v = np.ascontiguousarray(world.v, np.float64)
         self.f = np.ascontiguousarray(world.f, np.float64)
-        bb, bk, br, ab, ak, at = world.flat_bonds()
-        self.bb = np.ascontiguousarray(bb, np.uint32)
-        self.bk, self.br = np.ascontiguousarray(bk), np.ascontiguousarray(br)
-        self.ab = np.ascontiguousarray(ab, np.uint32)
-        self.ak, self.at = np.ascontiguousarray(ak), np.ascontiguousarray(at)
-        s = PdpdWorld()
-        for i in range(3):
-            s.box[i] = int(world.box[i])
+        s = PdpdWorld.from_buffer_copy(tmpl)
+        s.box[0], s.box[1], s.box[2] = int(world.box[0]), int(world.box[1]), int(world.box[2])
         s.dt, s.lam = float(world.dt), float(world.lam)
         s.seed, s.t = int(world.seed) & 0xFFFFFFFFFFFFFFFF, int(world.t)
         s.n_bead_types = self.cons.shape[0]
         s.conservative, s.dissipative, s.stationary = _p(self.cons), _p(self.diss), _p(self.stat)
         s.n_beads = self.x.shape[0]
-        s.hash, s.x, s.v, s.f = _p(self.hash), _p(self.x), _p(self.v), _p(self.f)
-        s.bead_stride_bytes = 24
-        s.n_bonds, s.bond_beads, s.bond_kappa, s.bond_r0 = (self.bb.shape[0], _p(self.bb),
-                                                            _p(self.bk), _p(self.br))
-        s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (self.ab.shape[0], _p(self.ab),
-                                                                    _p(self.ak), _p(self.at))
+        s.x, s.v, s.f = _p(self.x), _p(self.v), _p(self.f)
         cc, cd = getattr(world, "cell_conservative", None), getattr(world, "cell_dissipative", None)
         self.cell_a = None if cc is None else np.ascontiguousarray(cc, np.float64)
         self.cell_g = None if cd is None else np.ascontiguousarray(cd, np.float64)
         s.cell_conservative = None if self.cell_a is None else self.cell_a.ctypes.data
         s.cell_dissipative = None if self.cell_g is None else self.cell_g.ctypes.data
         self.struct = s
+
+
+def _topology_struct(world):
+    """A PdpdWorld with the hash and bond fields of the World's topology set (and the arrays
+    they point to), cached with the World while those arrays are the same objects."""
+    hash_ = world.hashes()
+    bonds = world.flat_bonds()
+    cache = world.__dict__.setdefault("_cache", {})
+    hit = cache.get("abi")
+    if hit is not None and hit[0] is hash_ and hit[1] is bonds:
+        return hit[2], hit[3]
+    h = np.ascontiguousarray(hash_, np.uint32)
+    bb, bk, br, ab, ak, at = bonds
+    arrs = (h, np.ascontiguousarray(bb, np.uint32), np.ascontiguousarray(bk), np.ascontiguousarray(br),
+            np.ascontiguousarray(ab, np.uint32), np.ascontiguousarray(ak), np.ascontiguousarray(at))
+    s = PdpdWorld()
+    s.hash = _p(arrs[0])
+    s.bead_stride_bytes = 24
+    s.n_bonds, s.bond_beads, s.bond_kappa, s.bond_r0 = arrs[1].shape[0], _p(arrs[1]), _p(arrs[2]), _p(arrs[3])
+    s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (arrs[4].shape[0], _p(arrs[4]), _p(arrs[5]),
+                                                                _p(arrs[6]))
+    cache["abi"] = (hash_, bonds, s, arrs)
+    return s, arrs
 
 
 def can_support(world) -> str:
