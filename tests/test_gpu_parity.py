@@ -464,16 +464,19 @@ def test_full_size_momentum_and_determinism():
 
 # ---------------------------------------------------------------------------- reference test suite
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_reference_testbase_suite_replay(prec):
+@pytest.mark.parametrize("prec,force_kernel", [("fp64", None), ("fp32", None), ("fp32", 9)])
+def test_reference_testbase_suite_replay(prec, force_kernel):
     """The reference's own 225-case engine test suite (TestBase families of test_engine.cpp),
     replayed segment by segment from the reference engine's recorded input states: the FP64
     engine reproduces every output bit for bit (so every property the suite checks on the
-    reference engine holds for it); the FP32 engine stays within the FP32 tolerances on the
-    short segments and finishes every segment."""
+    reference engine holds for it); the FP32 engine -- its default kernels, and the half-shell
+    kernel -- stays within the FP32 tolerances on the short segments and finishes every
+    segment."""
     from _helpers import load_testbase, world_at
     cases = load_testbase()
     eng = E.GB300DPDEngine(prec)
+    if force_kernel:
+        eng.SetConfigEntry("force_kernel", force_kernel)
     checked = 0
     for name, world, segs in cases:
         for todo, t_in, s_in, t_out, s_out in segs:
