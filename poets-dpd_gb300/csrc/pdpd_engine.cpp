@@ -251,6 +251,11 @@ const ConfigEntry kConfig[] = {
     {"brick_z", "Brick extent in cells along z (FP32 brick kernel)."},
     {"autotune", "FP32: time the force-kernel variants and brick shapes on the first steps of "
                  "the next run and keep the fastest (results do not depend on the choice)."},
+    {"host_direct", "Attach's upload and the read-backs by a kernel that reads and writes the "
+                    "caller's host arrays directly (1, default; used where the device reaches "
+                    "pageable host memory through the host's page tables, as Grace-Blackwell does "
+                    "over NVLink-C2C, and the arrays are 8-byte aligned), or through pinned "
+                    "staging buffers and DMA (0).  The results are the same."},
 };
 
 }  // namespace
@@ -273,6 +278,8 @@ struct pdpd_engine {
     int cfg_force_kernel = 8;
     int cfg_brick[3] = {BRICK_X, BRICK_Y, BRICK_Z};
     int cfg_autotune = 0;
+    int cfg_host_direct = 1;
+    bool host_access = false;  // the device reaches pageable host memory through the host's page tables
     bool kernel_user = false;  // force_kernel set through the config
     bool brick_user = false;   // a brick_* entry set through the config
     bool tuning = false;       // the autotuner is trying candidates
@@ -295,6 +302,7 @@ struct pdpd_engine {
     HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
     HostPinned h_err;
     DevBuf d_v2err;
+    DevBuf d_hostio;  // segment and chunk tables of the direct host copies
     cudaEvent_t ev_snap[2] = {nullptr, nullptr};
     cudaEvent_t ev_copied[2] = {nullptr, nullptr};
 
@@ -344,7 +352,8 @@ struct pdpd_engine {
                           &d_frc, &d_posB, &d_velB, &d_frcB, &d_ids, &d_cellg, &d_slot_of_id,
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
-                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next, &d_hash_old};
+                          &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next, &d_hash_old,
+                          &d_hostio};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -646,6 +655,25 @@ struct pdpd_engine {
     }
     // The worlds' flags and t copied to h_err on the stream (for eval_device_errors once the
     // copy has completed).
+    bool host_direct() const { return host_access && cfg_host_direct; }
+    // Run a host copy plan (pdpd_hostio.cu) on the stream: its tables go to the device first.
+    int host_copy(const std::vector<HostCopySeg> &segs, const std::vector<HostCopyChunk> &chunks)
+    {
+        if (chunks.empty()) return PDPD_OK;
+        const size_t sb = (sizeof(HostCopySeg) * segs.size() + 15) & ~size_t(15);
+        const size_t cb = sizeof(HostCopyChunk) * chunks.size();
+        if (d_hostio.alloc(sb + cb) != cudaSuccess) return fail(PDPD_E_NOMEM, "device allocation failed");
+        cudaError_t ce = cudaMemcpyAsync(d_hostio.p, segs.data(), sizeof(HostCopySeg) * segs.size(),
+                                         cudaMemcpyHostToDevice, stream);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync((char *)d_hostio.p + sb, chunks.data(), cb, cudaMemcpyHostToDevice, stream);
+        if (ce != cudaSuccess) return cuda_fail(ce, "host copy tables");
+        launches += launch_host_copy((const HostCopySeg *)d_hostio.p,
+                                     (const HostCopyChunk *)((const char *)d_hostio.p + sb),
+                                     (uint32_t)chunks.size(), sm_count, stream);
+        ce = cudaGetLastError();
+        return ce == cudaSuccess ? PDPD_OK : cuda_fail(ce, "host copy");
+    }
     int fetch_device_errors()
     {
         size_t nb = sizeof(WorldDev) * worlds.size();
@@ -739,6 +767,34 @@ static const double *vec_at(const double *base, size_t stride_bytes, uint32_t i)
     return (const double *)((const char *)base + s * (size_t)i);
 }
 
+// A plan of direct host copies: segments cut into chunks of at most HOSTCOPY_CHUNK units.
+struct HostCopyPlan {
+    std::vector<HostCopySeg> segs;
+    std::vector<HostCopyChunk> chunks;
+    void add(uint32_t kind, const void *src, void *dst, uint64_t n, uint32_t src_stride = 0, uint32_t dst_stride = 0)
+    {
+        if (n == 0) return;
+        const uint32_t si = (uint32_t)segs.size();
+        segs.push_back({src, dst, n, kind, src_stride, dst_stride, 0});
+        for (uint64_t k = 0; k < n; k += HOSTCOPY_CHUNK)
+            chunks.push_back({si, (uint32_t)std::min<uint64_t>(HOSTCOPY_CHUNK, n - k), k});
+    }
+    // n beads' vectors (3 doubles each): a packed array (stride 24) as one run of words, a
+    // strided one bead by bead; the device side is always packed.
+    void vectors(const double *src, size_t src_stride, double *dst, size_t dst_stride, uint64_t n)
+    {
+        if (src_stride == 24 && dst_stride == 24) add(HOSTCOPY_WORDS8, src, dst, 3 * n);
+        else add(HOSTCOPY_TRIPLES, src, dst, n, (uint32_t)src_stride, (uint32_t)dst_stride);
+    }
+};
+
+// Host arrays the copy kernel may access: 8-byte aligned vectors at a stride that is a
+// multiple of 8 (4-byte aligned hashes); anything else goes through the staged copies.
+static bool vec_ok(const void *p, size_t stride)
+{
+    return p == nullptr || (((uintptr_t)p & 7u) == 0 && (stride & 7u) == 0);
+}
+
 // ------------------------------------------------------------------------------------------
 // C ABI
 
@@ -766,6 +822,15 @@ int pdpd_create(int precision, int device, pdpd_engine **out)
     eng->precision = precision;
     eng->device = dev;
     eng->sm_count = sms;
+    {  // direct host copies need coherent access to pageable memory through the host's page tables
+        int pageable = 0, host_tables = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            pageable = host_tables = 0;
+        }
+        eng->host_access = pageable == 1 && host_tables == 1;
+    }
     e = cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->side, cudaStreamNonBlocking);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
@@ -1147,6 +1212,15 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // Host staging rows of the worlds that come from their descriptors: the whole batch in
     // slot order, or in a re-pack only the new worlds, packed (the kept worlds' rows stay on
     // the device, and the pinned buffer stays the size of what a re-pack brings in).
+    // With direct host copies (a whole batch from its descriptors, arrays the copy kernel may
+    // access) the beads go field-major into device staging 0 by the kernel, and the host stages
+    // nothing.
+    bool direct = !any_kept && e->host_direct();
+    for (uint32_t i = 0; direct && i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
+        direct = vec_ok(w.x, sb) && vec_ok(w.v, sb) && vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
+    }
     std::vector<size_t> hoff(n_worlds);
     size_t h_rows = 0;
     for (uint32_t i = 0; i < n_worlds; i++) {
@@ -1154,14 +1228,15 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         if (!any_kept || keep_old[i] < 0) h_rows += ws[i].n_beads;
     }
     if (!any_kept) h_rows = nb;
-    if (e->h_staging[0].alloc(sizeof(double) * 9 * h_rows + sizeof(uint32_t) * h_rows) != cudaSuccess) {
+    if (direct) h_rows = 0;
+    if (!direct && e->h_staging[0].alloc(sizeof(double) * 9 * h_rows + sizeof(uint32_t) * h_rows) != cudaSuccess) {
         e->release();
         return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
     }
 
     // --- stage and upload
-    double *hs = (double *)e->h_staging[0].p;
-    uint32_t *hh = (uint32_t *)(hs + 9 * h_rows);
+    double *hs = direct ? nullptr : (double *)e->h_staging[0].p;
+    uint32_t *hh = direct ? nullptr : (uint32_t *)(hs + 9 * h_rows);
     // Global slots [r0, r1) of the batch (slot g of world i = bead_base_i + k) into the pinned
     // rows, split across host threads whatever the worlds' sizes.
     auto stage = [&](size_t r0, size_t r1) {
@@ -1193,7 +1268,27 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         });
     };
     cudaStream_t s = e->stream;
-    if (!any_kept) {
+    if (direct) {
+        HostCopyPlan plan;
+        double *ds = e->d_staging[0].as<double>();
+        uint32_t *dh = e->d_hash.as<uint32_t>();
+        for (uint32_t i = 0; i < n_worlds; i++) {
+            const pdpd_world &w = ws[i];
+            const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
+            const size_t bb = wdev[i].bead_base;
+            plan.vectors(w.x, sb, ds + 3 * bb, 24, w.n_beads);
+            plan.vectors(w.v, sb, ds + 3 * (nb + bb), 24, w.n_beads);
+            plan.vectors(w.f, sb, ds + 3 * (2 * nb + bb), 24, w.n_beads);
+            plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
+        }
+        int rc = e->host_copy(plan.segs, plan.chunks);
+        if (rc) {
+            std::string m = e->err;
+            e->release();
+            e->err = m;
+            return rc;
+        }
+    } else if (!any_kept) {
         // a whole batch from its descriptors: chunks of 2^20 beads, each uploaded while the
         // next is staged
         const size_t CH = size_t(1) << 20;
@@ -1317,7 +1412,12 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
 
     // --- bin + sort into the rest state
     const uint32_t *hash_in = e->d_hash.as<uint32_t>();
-    e->launches += f64 ? launch_bin64(a, hash_in, s) : launch_bin32(a, hash_in, s);
+    {
+        KArgs ab = a;  // the direct copies left the staging field-major
+        ab.staging_fields = direct ? 1u : 0u;
+        ab.staging_n = (uint32_t)nb;
+        e->launches += f64 ? launch_bin64(ab, hash_in, s) : launch_bin32(ab, hash_in, s);
+    }
     e->launches += launch_sort(a, f64, 0, 1, s);
     ce = cudaGetLastError();
     if (ce != cudaSuccess) {
@@ -1473,6 +1573,25 @@ static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
     return rc;
 }
 
+// The read-back by the copy kernel, for a download already on the stream (field-major device
+// staging 0): the worlds' error flags first (the callers' arrays are not written when a world
+// has failed), then `fill` plans the copies into the callers' arrays, and they run.
+static int read_direct(pdpd_engine *e, const std::function<void(HostCopyPlan &)> &fill)
+{
+    int rc = e->fetch_device_errors();
+    if (rc) return rc;
+    cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
+    rc = e->eval_device_errors();
+    if (rc) return rc;
+    HostCopyPlan plan;
+    fill(plan);
+    rc = e->host_copy(plan.segs, plan.chunks);
+    ce = cudaStreamSynchronize(e->stream);
+    if (rc) return rc;
+    return ce == cudaSuccess ? PDPD_OK : e->cuda_fail(ce, "download");
+}
+
 // Beads [k0, k1) of one world from field-major host staging (x block at hx, v at hv, f at
 // hf, indexed by the world's bead index) into the caller's vectors of byte stride sb (24:
 // packed, copied as one block per vector).
@@ -1502,6 +1621,18 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     if (rc) return rc;
     const WorldDev &wd = e->worlds[world].dev;
     const size_t sb = stride ? stride : 3 * sizeof(double);
+    if (e->host_direct() && vec_ok(x, sb) && vec_ok(v, sb) && vec_ok(f, sb)) {
+        const double *ds = e->d_staging[0].as<double>();
+        const size_t nd = e->n_beads;
+        rc = read_direct(e, [&](HostCopyPlan &p) {
+            double *out[3] = {x, v, f};
+            for (int q = 0; q < 3; q++)
+                if (out[q]) p.vectors(ds + 3 * (q * nd + wd.bead_base), 24, out[q], sb, wd.n_beads);
+        });
+        if (rc) return rc;
+        if (t) *t = e->worlds[world].dev.t;
+        return PDPD_OK;
+    }
     rc = read_rows(e, wd.bead_base, (size_t)wd.bead_base + wd.n_beads,
                    [&](const double *h, size_t n, size_t r0, size_t r1) {
                        parallel_for(r1 - r0, 1 << 15, [&](size_t a0, size_t a1) {
@@ -1528,19 +1659,34 @@ int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *o
     std::vector<uint32_t> base(n_worlds + 1);
     for (uint32_t i = 0; i < n_worlds; i++) base[i] = e->worlds[i].dev.bead_base;
     base[n_worlds] = e->n_beads;
-    rc = read_rows(e, 0, e->n_beads, [&](const double *h, size_t n, size_t c0, size_t c1) {
-        parallel_for(c1 - c0, 1 << 15, [&](size_t a0, size_t a1) {
-            const size_t g0 = c0 + a0, g1 = c0 + a1;
-            uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
-            for (size_t g = g0; g < g1;) {
-                while (g >= base[i + 1]) i++;
-                const size_t b = base[i], e1 = std::min<size_t>(g1, base[i + 1]);
-                copy_out(h + 3 * b, h + 3 * (n + b), h + 3 * (2 * n + b), g - b, e1 - b, out[i].x, out[i].v,
-                         out[i].f, sb);
-                g = e1;
+    bool direct = e->host_direct();
+    for (uint32_t i = 0; direct && i < n_worlds; i++)
+        direct = vec_ok(out[i].x, sb) && vec_ok(out[i].v, sb) && vec_ok(out[i].f, sb);
+    if (direct) {
+        const double *ds = e->d_staging[0].as<double>();
+        const size_t nd = e->n_beads;
+        rc = read_direct(e, [&](HostCopyPlan &p) {
+            for (uint32_t i = 0; i < n_worlds; i++) {
+                double *o[3] = {out[i].x, out[i].v, out[i].f};
+                for (int q = 0; q < 3; q++)
+                    if (o[q]) p.vectors(ds + 3 * (q * nd + base[i]), 24, o[q], sb, base[i + 1] - base[i]);
             }
         });
-    });
+    } else {
+        rc = read_rows(e, 0, e->n_beads, [&](const double *h, size_t n, size_t c0, size_t c1) {
+            parallel_for(c1 - c0, 1 << 15, [&](size_t a0, size_t a1) {
+                const size_t g0 = c0 + a0, g1 = c0 + a1;
+                uint32_t i = (uint32_t)(std::upper_bound(base.begin(), base.end() - 1, (uint32_t)g0) - base.begin()) - 1;
+                for (size_t g = g0; g < g1;) {
+                    while (g >= base[i + 1]) i++;
+                    const size_t b = base[i], e1 = std::min<size_t>(g1, base[i + 1]);
+                    copy_out(h + 3 * b, h + 3 * (n + b), h + 3 * (2 * n + b), g - b, e1 - b, out[i].x, out[i].v,
+                             out[i].f, sb);
+                    g = e1;
+                }
+            });
+        });
+    }
     if (rc) return rc;
     for (uint32_t i = 0; i < n_worlds; i++)
         if (out[i].t) *out[i].t = e->worlds[i].dev.t;
@@ -1646,12 +1792,15 @@ int pdpd_get_config(pdpd_engine *e, uint32_t index, char *name, size_t name_len,
     if (index >= sizeof(kConfig) / sizeof(kConfig[0])) return PDPD_E_INVALID;
     int vals[] = {e->cfg_list_capacity, e->cfg_grid_blocks, e->cfg_graph_steps, e->cfg_use_graphs,
                   e->cfg_force_kernel, e->cfg_brick[0], e->cfg_brick[1], e->cfg_brick[2],
-                  e->cfg_autotune};
+                  e->cfg_autotune, e->cfg_host_direct};
+    static_assert(sizeof(vals) / sizeof(vals[0]) == sizeof(kConfig) / sizeof(kConfig[0]), "config values");
     if (name && name_len) snprintf(name, name_len, "%s", kConfig[index].name);
     if (desc && desc_len) snprintf(desc, desc_len, "%s", kConfig[index].desc);
     if (value && value_len) {
         if (std::string(kConfig[index].name) == "autotune" && e->tuned)
             snprintf(value, value_len, "%d (trials %s)", vals[index], e->tune_log.c_str());
+        else if (std::string(kConfig[index].name) == "host_direct" && vals[index] && !e->host_access)
+            snprintf(value, value_len, "%d (staged: this device does not reach pageable host memory)", vals[index]);
         else
             snprintf(value, value_len, "%d", vals[index]);
     }
@@ -1685,6 +1834,9 @@ int pdpd_set_config(pdpd_engine *e, const char *key, const char *value)
     } else if (k == "autotune") {
         e->cfg_autotune = v ? 1 : 0;
         e->tuned = false;
+    } else if (k == "host_direct") {
+        e->cfg_host_direct = v ? 1 : 0;
+        return PDPD_OK;  // no bearing on the captured graphs or the kernels
     }
     else return e->fail(PDPD_E_INVALID, "Unknown engine config name '%s'", key);
     e->drop_graph();  // graphs are captured again at the next run

@@ -755,7 +755,8 @@ __global__ void __launch_bounds__(TILE_BEADS) k_begin32(KArgs a)
     }
 }
 
-// Attach: id-ordered FP64 staging (x, v, f) -> B in slot = id order, with cell counts.
+// Attach: id-ordered FP64 staging (x, v, f: rows of 9 doubles, or field-major blocks of
+// staging_n beads each) -> B in slot = id order, with cell counts.
 __global__ void k_bin32(KArgs a, const uint32_t *__restrict__ hash_in)
 {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -767,7 +768,8 @@ __global__ void k_bin32(KArgs a, const uint32_t *__restrict__ hash_in)
         if (a.worlds[mid].bead_base <= g) lo = mid; else hi = mid;
     }
     const WorldDev &w = a.worlds[lo];
-    const double *st = a.staging + 9 * (size_t)g;
+    const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
+    const double *st = a.staging + stride * g;
     int c[3];
     float o[3];
     uint32_t err = 0;
@@ -788,8 +790,8 @@ __global__ void k_bin32(KArgs a, const uint32_t *__restrict__ hash_in)
     const uint32_t key = w.cell_base + ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
     const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
     ((float4 *)a.posB)[g] = make_float4(o[0], o[1], o[2], __uint_as_float(hash_in[g]));
-    ((float4 *)a.velB)[g] = make_float4((float)st[3], (float)st[4], (float)st[5], 0.f);
-    ((float4 *)a.frcB)[g] = make_float4((float)st[6], (float)st[7], (float)st[8], 0.f);
+    ((float4 *)a.velB)[g] = make_float4((float)st[field], (float)st[field + 1], (float)st[field + 2], 0.f);
+    ((float4 *)a.frcB)[g] = make_float4((float)st[2 * field], (float)st[2 * field + 1], (float)st[2 * field + 2], 0.f);
     a.ids[g] = g;
     a.keyrank[g] = make_uint2(key, zhalf_rank(rank, o[2]));
 }

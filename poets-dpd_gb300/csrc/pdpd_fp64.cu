@@ -644,7 +644,9 @@ __global__ void k_bin64(KArgs a, const uint32_t *__restrict__ hash_in)
         if (a.worlds[mid].bead_base <= g) lo = mid; else hi = mid;
     }
     const WorldDev &w = a.worlds[lo];
-    const double *st = a.staging + 9 * (size_t)g;
+    // rows of 9 doubles, or field-major blocks (x, v, f) of staging_n beads each
+    const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
+    const double *st = a.staging + stride * g;
     int c[3];
     double x[3];
     uint32_t err = 0;
@@ -662,8 +664,8 @@ __global__ void k_bin64(KArgs a, const uint32_t *__restrict__ hash_in)
     const uint32_t key = w.cell_base + ((uint32_t)c[0] * (uint32_t)w.L[1] + (uint32_t)c[1]) * (uint32_t)w.L[2] + (uint32_t)c[2];
     const uint32_t rank = atomicAdd(&a.cnt[key], 1u);
     Vec4d po = {x[0], x[1], x[2], __longlong_as_double((long long)hash_in[g])};
-    Vec4d vo = {st[3], st[4], st[5], 0.0};
-    Vec4d fo = {st[6], st[7], st[8], 0.0};
+    Vec4d vo = {st[field], st[field + 1], st[field + 2], 0.0};
+    Vec4d fo = {st[2 * field], st[2 * field + 1], st[2 * field + 2], 0.0};
     ((Vec4d *)a.posB)[g] = po;
     ((Vec4d *)a.velB)[g] = vo;
     ((Vec4d *)a.frcB)[g] = fo;

@@ -166,6 +166,30 @@ int launch_pair_log32(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const
 int launch_pair_log64(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const uint32_t *offs,
                       uint32_t *counts, PairLogRec *out, cudaStream_t s);
 
+// Copies between device memory and the caller's host arrays done by a kernel (pdpd_hostio.cu),
+// on devices that access pageable host memory coherently through the host's page tables
+// (Grace-Blackwell: NVLink-C2C with address translation).  A segment is one contiguous run
+// of 8-byte words (n words), of 4-byte words (n words), or n triples of doubles at byte
+// strides src_stride / dst_stride (the beads of a strided bead array).  Chunks split the
+// segments into pieces of at most HOSTCOPY_CHUNK units, the unit of work of a block.
+enum HostCopyKind : uint32_t { HOSTCOPY_WORDS8 = 0, HOSTCOPY_WORDS4 = 1, HOSTCOPY_TRIPLES = 2 };
+struct HostCopySeg {
+    const void *src;
+    void *dst;
+    uint64_t n;
+    uint32_t kind;
+    uint32_t src_stride, dst_stride;
+    uint32_t pad;
+};
+struct HostCopyChunk {
+    uint32_t seg;
+    uint32_t count;
+    uint64_t first;
+};
+constexpr uint32_t HOSTCOPY_CHUNK = 16384;
+int launch_host_copy(const HostCopySeg *segs, const HostCopyChunk *chunks, uint32_t n_chunks, int sm_count,
+                     cudaStream_t s);
+
 // Device RNG on arrays (device pointers), for known-answer tests.
 int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
                     const uint32_t *b, uint32_t *h_out, float *u_out, cudaStream_t s);
