@@ -656,24 +656,6 @@ struct pdpd_engine {
     // The worlds' flags and t copied to h_err on the stream (for eval_device_errors once the
     // copy has completed).
     bool host_direct() const { return host_access && cfg_host_direct; }
-    // Run a host copy plan (pdpd_hostio.cu) on the stream: its tables go to the device first.
-    int host_copy(const std::vector<HostCopySeg> &segs, const std::vector<HostCopyChunk> &chunks)
-    {
-        if (chunks.empty()) return PDPD_OK;
-        const size_t sb = (sizeof(HostCopySeg) * segs.size() + 15) & ~size_t(15);
-        const size_t cb = sizeof(HostCopyChunk) * chunks.size();
-        if (d_hostio.alloc(sb + cb) != cudaSuccess) return fail(PDPD_E_NOMEM, "device allocation failed");
-        cudaError_t ce = cudaMemcpyAsync(d_hostio.p, segs.data(), sizeof(HostCopySeg) * segs.size(),
-                                         cudaMemcpyHostToDevice, stream);
-        if (ce == cudaSuccess)
-            ce = cudaMemcpyAsync((char *)d_hostio.p + sb, chunks.data(), cb, cudaMemcpyHostToDevice, stream);
-        if (ce != cudaSuccess) return cuda_fail(ce, "host copy tables");
-        launches += launch_host_copy((const HostCopySeg *)d_hostio.p,
-                                     (const HostCopyChunk *)((const char *)d_hostio.p + sb),
-                                     (uint32_t)chunks.size(), sm_count, stream);
-        ce = cudaGetLastError();
-        return ce == cudaSuccess ? PDPD_OK : cuda_fail(ce, "host copy");
-    }
     int fetch_device_errors()
     {
         size_t nb = sizeof(WorldDev) * worlds.size();
@@ -788,11 +770,91 @@ struct HostCopyPlan {
     }
 };
 
+// Touch, on the host, every page of the host side of a direct copy plan before the kernel runs
+// (host_write: the destinations, else the sources): the device reaches host pages through the
+// host's page tables, and a page the process has never touched is a fault the device waits
+// for -- tens of microseconds a page, serialised (writing 1 GiB of fresh pages from the device
+// took 0.37 s on a GB300 against 5.5 ms for pages already there) -- while the host's threads
+// populate them in parallel.  One aligned word of the plan's own data per page: a destination
+// word is written with its own value by an atomic OR with zero (the page becomes writable, the
+// data stays), a source word is read.
+static void touch_pages(const HostCopyPlan &plan, bool host_write)
+{
+    static const size_t P = []() {
+        const long ps = sysconf(_SC_PAGESIZE);
+        return ps > 0 ? (size_t)ps : (size_t)4096;
+    }();
+    struct Span {
+        const HostCopySeg *sg;
+        uintptr_t base, end;  // host bytes [base, end) the copy covers
+        size_t page0, first;  // its first page, and its first work item in the flat page list
+    };
+    std::vector<Span> spans;
+    size_t total = 0;
+    for (const HostCopySeg &sg : plan.segs) {
+        const uintptr_t base = (uintptr_t)(host_write ? sg.dst : sg.src);
+        const uint32_t stride = host_write ? sg.dst_stride : sg.src_stride;
+        const uintptr_t end = sg.kind == HOSTCOPY_TRIPLES ? base + (sg.n - 1) * stride + 24
+                                                          : base + sg.n * (sg.kind == HOSTCOPY_WORDS4 ? 4 : 8);
+        const size_t p0 = base / P, p1 = (end - 1) / P;
+        spans.push_back({&sg, base, end, p0, total});
+        total += p1 - p0 + 1;
+    }
+    parallel_for(total, 256, [&](size_t i0, size_t i1) {
+        size_t si = (size_t)(std::upper_bound(spans.begin(), spans.end(), i0,
+                                              [](size_t i, const Span &sp) { return i < sp.first; }) -
+                             spans.begin()) - 1;
+        for (size_t i = i0; i < i1; i++) {
+            while (si + 1 < spans.size() && i >= spans[si + 1].first) si++;
+            const Span &sp = spans[si];
+            const uintptr_t ps = std::max<uintptr_t>(sp.base, (sp.page0 + (i - sp.first)) * P), pe = (ps / P + 1) * P;
+            uintptr_t a = ps;  // the first word of the copy at or after the page's start
+            if (sp.sg->kind == HOSTCOPY_TRIPLES) {
+                const uint32_t stride = host_write ? sp.sg->dst_stride : sp.sg->src_stride;
+                const uint64_t k = (ps - sp.base) / stride;
+                const uintptr_t item = sp.base + k * stride;
+                const uintptr_t j = (ps - item + 7) / 8;
+                a = j <= 2 ? item + 8 * j : item + stride;
+                if (j > 2 && k + 1 >= sp.sg->n) continue;
+            }
+            if (a >= pe || a >= sp.end) continue;  // no word of the copy on this page
+            if (sp.sg->kind == HOSTCOPY_WORDS4) {
+                if (host_write) __atomic_fetch_or((uint32_t *)a, 0u, __ATOMIC_RELAXED);
+                else (void)*(volatile const uint32_t *)a;
+            } else {
+                if (host_write) __atomic_fetch_or((uint64_t *)a, (uint64_t)0, __ATOMIC_RELAXED);
+                else (void)*(volatile const uint64_t *)a;
+            }
+        }
+    });
+}
+
 // Host arrays the copy kernel may access: 8-byte aligned vectors at a stride that is a
 // multiple of 8 (4-byte aligned hashes); anything else goes through the staged copies.
 static bool vec_ok(const void *p, size_t stride)
 {
-    return p == nullptr || (((uintptr_t)p & 7u) == 0 && (stride & 7u) == 0);
+    return p == nullptr || (((uintptr_t)p & 7u) == 0 && (stride & 7u) == 0 && stride >= 24 && stride < (1u << 20));
+}
+
+// Run a host copy plan (pdpd_hostio.cu) on the engine's stream: the host pages touched first
+// (touch_pages; host_write: the host side is the destination), the plan's tables uploaded.
+static int run_host_copy(pdpd_engine *e, const HostCopyPlan &plan, bool host_write)
+{
+    if (plan.chunks.empty()) return PDPD_OK;
+    touch_pages(plan, host_write);
+    const size_t sb = (sizeof(HostCopySeg) * plan.segs.size() + 15) & ~size_t(15);
+    const size_t cb = sizeof(HostCopyChunk) * plan.chunks.size();
+    if (e->d_hostio.alloc(sb + cb) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "device allocation failed");
+    cudaError_t ce = cudaMemcpyAsync(e->d_hostio.p, plan.segs.data(), sizeof(HostCopySeg) * plan.segs.size(),
+                                     cudaMemcpyHostToDevice, e->stream);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync((char *)e->d_hostio.p + sb, plan.chunks.data(), cb, cudaMemcpyHostToDevice, e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "host copy tables");
+    e->launches += launch_host_copy((const HostCopySeg *)e->d_hostio.p,
+                                    (const HostCopyChunk *)((const char *)e->d_hostio.p + sb),
+                                    (uint32_t)plan.chunks.size(), e->sm_count, e->stream);
+    ce = cudaGetLastError();
+    return ce == cudaSuccess ? PDPD_OK : e->cuda_fail(ce, "host copy");
 }
 
 // ------------------------------------------------------------------------------------------
@@ -961,6 +1023,44 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     e->n_beads = (uint32_t)nb;
     e->n_cells = (uint32_t)nc;
 
+    // With direct host copies (a whole batch from its descriptors, in arrays the copy kernel
+    // may access) the kernel brings the beads field-major into device staging 0 and the
+    // hashes, launched now so that the transfer runs while the host builds the tables below.
+    bool direct = !any_kept && e->host_direct();
+    for (uint32_t i = 0; direct && i < n_worlds; i++) {
+        const pdpd_world &w = ws[i];
+        const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
+        direct = vec_ok(w.x, sb) && vec_ok(w.v, sb) && vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
+    }
+    if (direct) {
+        if (e->d_staging[0].alloc(sizeof(double) * 9 * nb) != cudaSuccess ||
+            e->d_hash.alloc(sizeof(uint32_t) * std::max<uint64_t>(1, nb)) != cudaSuccess) {
+            cudaGetLastError();
+            e->release();
+            return e->fail(PDPD_E_NOMEM, "device allocation failed");
+        }
+        HostCopyPlan plan;
+        double *ds = e->d_staging[0].as<double>();
+        uint32_t *dh = e->d_hash.as<uint32_t>();
+        size_t bb = 0;  // the world's first global bead (its bead_base)
+        for (uint32_t i = 0; i < n_worlds; i++) {
+            const pdpd_world &w = ws[i];
+            const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
+            plan.vectors(w.x, sb, ds + 3 * bb, 24, w.n_beads);
+            plan.vectors(w.v, sb, ds + 3 * (nb + bb), 24, w.n_beads);
+            plan.vectors(w.f, sb, ds + 3 * (2 * nb + bb), 24, w.n_beads);
+            plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
+            bb += w.n_beads;
+        }
+        int rc = run_host_copy(e, plan, false);
+        if (rc) {
+            std::string m = e->err;
+            e->release();
+            e->err = m;
+            return rc;
+        }
+    }
+
     // --- world table, tiles, pair table
     std::vector<Tile> tiles;
     double max_density = 0;
@@ -1067,8 +1167,10 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     };
     if (n_terms) {
         const size_t row_bytes = (sizeof(uint32_t) * (nb + 1) + 15) & ~size_t(15);
-        if (e->h_meta.alloc(row_bytes + sizeof(BondTerm) * n_terms) != cudaSuccess)
+        if (e->h_meta.alloc(row_bytes + sizeof(BondTerm) * n_terms) != cudaSuccess) {
+            e->release();  // (waits for the direct copy, which reads the caller's arrays)
             return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
+        }
         row = (uint32_t *)e->h_meta.p;
         terms = (BondTerm *)((char *)e->h_meta.p + row_bytes);
         parallel_for(nb + 1, 1 << 18, [&](size_t i0, size_t i1) { memset(row + i0, 0, sizeof(uint32_t) * (i1 - i0)); });
@@ -1212,15 +1314,6 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // Host staging rows of the worlds that come from their descriptors: the whole batch in
     // slot order, or in a re-pack only the new worlds, packed (the kept worlds' rows stay on
     // the device, and the pinned buffer stays the size of what a re-pack brings in).
-    // With direct host copies (a whole batch from its descriptors, arrays the copy kernel may
-    // access) the beads go field-major into device staging 0 by the kernel, and the host stages
-    // nothing.
-    bool direct = !any_kept && e->host_direct();
-    for (uint32_t i = 0; direct && i < n_worlds; i++) {
-        const pdpd_world &w = ws[i];
-        const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
-        direct = vec_ok(w.x, sb) && vec_ok(w.v, sb) && vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
-    }
     std::vector<size_t> hoff(n_worlds);
     size_t h_rows = 0;
     for (uint32_t i = 0; i < n_worlds; i++) {
@@ -1269,25 +1362,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     };
     cudaStream_t s = e->stream;
     if (direct) {
-        HostCopyPlan plan;
-        double *ds = e->d_staging[0].as<double>();
-        uint32_t *dh = e->d_hash.as<uint32_t>();
-        for (uint32_t i = 0; i < n_worlds; i++) {
-            const pdpd_world &w = ws[i];
-            const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
-            const size_t bb = wdev[i].bead_base;
-            plan.vectors(w.x, sb, ds + 3 * bb, 24, w.n_beads);
-            plan.vectors(w.v, sb, ds + 3 * (nb + bb), 24, w.n_beads);
-            plan.vectors(w.f, sb, ds + 3 * (2 * nb + bb), 24, w.n_beads);
-            plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
-        }
-        int rc = e->host_copy(plan.segs, plan.chunks);
-        if (rc) {
-            std::string m = e->err;
-            e->release();
-            e->err = m;
-            return rc;
-        }
+        // (uploaded by the copy kernel launched above)
     } else if (!any_kept) {
         // a whole batch from its descriptors: chunks of 2^20 beads, each uploaded while the
         // next is staged
@@ -1586,7 +1661,7 @@ static int read_direct(pdpd_engine *e, const std::function<void(HostCopyPlan &)>
     if (rc) return rc;
     HostCopyPlan plan;
     fill(plan);
-    rc = e->host_copy(plan.segs, plan.chunks);
+    rc = run_host_copy(e, plan, true);
     ce = cudaStreamSynchronize(e->stream);
     if (rc) return rc;
     return ce == cudaSuccess ? PDPD_OK : e->cuda_fail(ce, "download");

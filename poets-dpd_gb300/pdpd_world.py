@@ -138,7 +138,8 @@ class World:
 
     def copy(self) -> "World":
         """A copy with its own state (x, v, f, t, parameters); the read-only topology arrays
-        and what is derived from them are shared."""
+        and what is derived from them (the hashes, the flat bond lists, the C ABI's topology
+        struct) are shared."""
         w = World(
             box=self.box.copy(), dt=self.dt, lam=self.lam, seed=self.seed, t=self.t,
             conservative=self.conservative.copy(), dissipative=self.dissipative.copy(),
@@ -151,7 +152,10 @@ class World:
             x=self.x.copy(), v=self.v.copy(), f=self.f.copy(),
             cell_conservative=None if self.cell_conservative is None else self.cell_conservative.copy(),
             cell_dissipative=None if self.cell_dissipative is None else self.cell_dissipative.copy())
-        w.__dict__["_cache"] = dict(self.__dict__.get("_cache", {}))
+        # one cache for a World and all its copies: an entry is used only while the topology
+        # arrays it was made from are the ones of the World asking, so a copy whose topology
+        # was replaced recomputes (and the others recompute after it)
+        w.__dict__["_cache"] = self.__dict__.setdefault("_cache", {})
         return w
 
     def flat_bonds(self):

@@ -117,3 +117,22 @@ def test_out_of_box_on_attach_either_path(direct):
     w.x[3, 1] = 4.0
     with pytest.raises(RuntimeError, match="outside the box"):
         _engine("fp32", direct).Attach(w)
+
+
+def test_read_back_into_fresh_arrays():
+    """Arrays the process has never written (np.empty: pages not yet mapped) as read-back
+    destinations: the host touches their pages before the copy kernel writes them."""
+    world = W.make_polymer_box(24, chain_fraction=0.05, seed=46)  # 41,472 beads, ~1 MB per vector array
+    got = {}
+    for direct in (0, 1):
+        eng = _engine("fp32", direct)
+        eng.Attach(world.copy())
+        eng._check(E.lib().pdpd_run(eng._h, 3), "Run")
+        x, v, f = (np.empty((world.n_beads, 3)) for _ in range(3))
+        t = C.c_int64(0)
+        eng._check(E.lib().pdpd_read_state(eng._h, 0, x.ctypes.data, v.ctypes.data, f.ctypes.data, 24,
+                                           C.byref(t)), "read_state")
+        got[direct] = (t.value, x, v, f)
+    assert got[0][0] == got[1][0]
+    for a, b in zip(got[0][1:], got[1][1:]):
+        assert np.array_equal(a, b)
