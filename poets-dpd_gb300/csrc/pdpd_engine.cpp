@@ -302,7 +302,8 @@ struct pdpd_engine {
     HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
     HostPinned h_err;
     DevBuf d_v2err;
-    DevBuf d_hostio;  // segment and chunk tables of the direct host copies
+    DevBuf d_hostio;  // segment and chunk tables of the direct host copies, or the read-back's destinations
+    DevBuf d_inv;     // direct read-back: the sorted slot of each bead id
     cudaEvent_t ev_snap[2] = {nullptr, nullptr};
     cudaEvent_t ev_copied[2] = {nullptr, nullptr};
 
@@ -353,7 +354,7 @@ struct pdpd_engine {
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
                           &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next, &d_hash_old,
-                          &d_hostio};
+                          &d_hostio, &d_inv};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -1648,10 +1649,11 @@ static int read_rows(pdpd_engine *e, size_t r_begin, size_t r_end,
     return rc;
 }
 
-// The read-back by the copy kernel, for a download already on the stream (field-major device
-// staging 0): the worlds' error flags first (the callers' arrays are not written when a world
-// has failed), then `fill` plans the copies into the callers' arrays, and they run.
-static int read_direct(pdpd_engine *e, const std::function<void(HostCopyPlan &)> &fill)
+// The read-back without device staging (k_read_direct), for worlds [w0, w1) of the batch:
+// the worlds' error flags first (the callers' arrays are not written when a world has
+// failed), the callers' pages touched, then the slot of each bead id and one gather kernel
+// writing dest[w] (one entry per attached world).
+static int read_direct(pdpd_engine *e, uint32_t w0, uint32_t w1, const std::vector<ReadDest> &dest)
 {
     int rc = e->fetch_device_errors();
     if (rc) return rc;
@@ -1659,11 +1661,34 @@ static int read_direct(pdpd_engine *e, const std::function<void(HostCopyPlan &)>
     if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
     rc = e->eval_device_errors();
     if (rc) return rc;
-    HostCopyPlan plan;
-    fill(plan);
-    rc = run_host_copy(e, plan, true);
-    ce = cudaStreamSynchronize(e->stream);
-    if (rc) return rc;
+    HostCopyPlan pages;  // (the destinations, for touch_pages only)
+    uint32_t first_tile = 0, n_tiles = 0;
+    for (uint32_t i = 0; i < w1; i++) {
+        const uint32_t nb = e->worlds[i].dev.n_beads, nt = (nb + TILE_BEADS - 1) / TILE_BEADS;
+        if (i < w0) {
+            first_tile += nt;
+            continue;
+        }
+        n_tiles += nt;
+        for (double *o : {dest[i].x, dest[i].v, dest[i].f})
+            if (o) pages.vectors(nullptr, 24, o, dest[i].stride, nb);
+    }
+    touch_pages(pages, true);
+    const size_t db = sizeof(ReadDest) * dest.size();
+    if (e->d_hostio.alloc(db) != cudaSuccess || e->d_inv.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, e->n_beads)) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "device allocation failed");
+    ce = cudaMemcpyAsync(e->d_hostio.p, dest.data(), db, cudaMemcpyHostToDevice, e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "download");
+    const uint32_t s0 = e->worlds[w0].dev.bead_base;
+    const uint32_t s1 = w1 < e->worlds.size() ? e->worlds[w1].dev.bead_base : e->n_beads;
+    KArgs a = e->args;
+    a.tiles = e->args.tiles + first_tile;
+    a.n_tiles = n_tiles;
+    e->launches += launch_slot_of_id(a, s0, s1 - s0, e->d_inv.as<uint32_t>(), e->stream);
+    e->launches += launch_read_direct(a, e->fp64(), e->d_inv.as<uint32_t>(), (const ReadDest *)e->d_hostio.p,
+                                      e->stream);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
     return ce == cudaSuccess ? PDPD_OK : e->cuda_fail(ce, "download");
 }
 
@@ -1692,22 +1717,18 @@ int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double
     if (!e->attached) return e->fail(PDPD_E_STATE, "no world attached");
     if (world >= e->worlds.size()) return e->fail(PDPD_E_INVALID, "world index out of range");
     cudaSetDevice(e->device);
-    int rc = download_world(e, 0, world, e->stream, true);
-    if (rc) return rc;
     const WorldDev &wd = e->worlds[world].dev;
     const size_t sb = stride ? stride : 3 * sizeof(double);
     if (e->host_direct() && vec_ok(x, sb) && vec_ok(v, sb) && vec_ok(f, sb)) {
-        const double *ds = e->d_staging[0].as<double>();
-        const size_t nd = e->n_beads;
-        rc = read_direct(e, [&](HostCopyPlan &p) {
-            double *out[3] = {x, v, f};
-            for (int q = 0; q < 3; q++)
-                if (out[q]) p.vectors(ds + 3 * (q * nd + wd.bead_base), 24, out[q], sb, wd.n_beads);
-        });
+        std::vector<ReadDest> dest(e->worlds.size(), ReadDest{nullptr, nullptr, nullptr, 24});
+        dest[world] = ReadDest{x, v, f, sb};
+        int rc = read_direct(e, world, world + 1, dest);
         if (rc) return rc;
         if (t) *t = e->worlds[world].dev.t;
         return PDPD_OK;
     }
+    int rc = download_world(e, 0, world, e->stream, true);
+    if (rc) return rc;
     rc = read_rows(e, wd.bead_base, (size_t)wd.bead_base + wd.n_beads,
                    [&](const double *h, size_t n, size_t r0, size_t r1) {
                        parallel_for(r1 - r0, 1 << 15, [&](size_t a0, size_t a1) {
@@ -1727,9 +1748,6 @@ int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *o
     if (n_worlds != e->worlds.size())
         return e->fail(PDPD_E_INVALID, "%u views for a batch of %zu worlds", n_worlds, e->worlds.size());
     cudaSetDevice(e->device);
-    int rc = download(e, 0, e->stream, true);
-    if (rc) return rc;
-    // each chunk of the batch's beads, split across host threads whatever the worlds' sizes
     const size_t sb = stride ? stride : 3 * sizeof(double);
     std::vector<uint32_t> base(n_worlds + 1);
     for (uint32_t i = 0; i < n_worlds; i++) base[i] = e->worlds[i].dev.bead_base;
@@ -1737,17 +1755,15 @@ int pdpd_read_states(pdpd_engine *e, uint32_t n_worlds, const pdpd_state_view *o
     bool direct = e->host_direct();
     for (uint32_t i = 0; direct && i < n_worlds; i++)
         direct = vec_ok(out[i].x, sb) && vec_ok(out[i].v, sb) && vec_ok(out[i].f, sb);
+    int rc = PDPD_OK;
     if (direct) {
-        const double *ds = e->d_staging[0].as<double>();
-        const size_t nd = e->n_beads;
-        rc = read_direct(e, [&](HostCopyPlan &p) {
-            for (uint32_t i = 0; i < n_worlds; i++) {
-                double *o[3] = {out[i].x, out[i].v, out[i].f};
-                for (int q = 0; q < 3; q++)
-                    if (o[q]) p.vectors(ds + 3 * (q * nd + base[i]), 24, o[q], sb, base[i + 1] - base[i]);
-            }
-        });
+        std::vector<ReadDest> dest(n_worlds);
+        for (uint32_t i = 0; i < n_worlds; i++) dest[i] = ReadDest{out[i].x, out[i].v, out[i].f, sb};
+        rc = read_direct(e, 0, n_worlds, dest);
     } else {
+        // each chunk of the batch's beads, split across host threads whatever the worlds' sizes
+        rc = download(e, 0, e->stream, true);
+        if (rc) return rc;
         rc = read_rows(e, 0, e->n_beads, [&](const double *h, size_t n, size_t c0, size_t c1) {
             parallel_for(c1 - c0, 1 << 15, [&](size_t a0, size_t a1) {
                 const size_t g0 = c0 + a0, g1 = c0 + a1;

@@ -7,7 +7,7 @@
 // nothing.  The kernel touches exactly the host addresses the staged copies touch.
 #include <algorithm>
 
-#include "pdpd_internal.h"
+#include "pdpd_device.cuh"
 
 namespace pdpd {
 namespace {
@@ -64,7 +64,97 @@ __global__ void __launch_bounds__(HOSTCOPY_THREADS) k_host_copy(const HostCopySe
     }
 }
 
+__global__ void k_slot_of_id(const uint32_t *__restrict__ ids, uint32_t first, uint32_t count, uint32_t *inv)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < count) inv[ids[first + k]] = first + k;
+}
+
+// The read-back without device staging: a block per tile of bead ids gathers the tile's beads
+// from their sorted slots (random 16- or 32-byte reads in device memory), lays x, v and f out
+// in shared memory in the caller's order, and writes each field as one contiguous run of the
+// caller's array (a stride-24 array; otherwise bead by bead).  The link to the host carries
+// each byte once, in full lines, and the gathers overlap it.  x = cell + offset in FP32 and
+// the FP32 -> FP64 conversions are those of the unsort kernels, so the values are the same.
+template <int F64>
+__global__ void __launch_bounds__(TILE_BEADS) k_read_direct(KArgs a, const uint32_t *__restrict__ inv,
+                                                            const ReadDest *__restrict__ dest)
+{
+    __shared__ double sh[3][3 * TILE_BEADS];
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const WorldDev &w = a.worlds[tl.world];
+        const uint32_t cnt = tl.slot_end - tl.slot_begin;
+        const uint32_t t = threadIdx.x;
+        if (t < cnt) {
+            const uint32_t s = inv[tl.slot_begin + t];
+            double x[3], v[3], f[3];
+            if (F64) {
+                const Vec4d p = ((const Vec4d *)a.posA)[s];
+                const Vec4d vv = ((const Vec4d *)a.velA)[s];
+                const Vec4d ff = ((const Vec4d *)a.frc)[s];
+                x[0] = p.x, x[1] = p.y, x[2] = p.z;
+                v[0] = vv.x, v[1] = vv.y, v[2] = vv.z;
+                f[0] = ff.x, f[1] = ff.y, f[2] = ff.z;
+            } else {
+                const float4 p = ((const float4 *)a.posA)[s];
+                const float4 vv = ((const float4 *)a.velA)[s];
+                const float4 ff = ((const float4 *)a.frc)[s];
+                int c[3];
+                decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+                x[0] = (double)c[0] + (double)p.x;
+                x[1] = (double)c[1] + (double)p.y;
+                x[2] = (double)c[2] + (double)p.z;
+                v[0] = vv.x, v[1] = vv.y, v[2] = vv.z;
+                f[0] = ff.x, f[1] = ff.y, f[2] = ff.z;
+            }
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                sh[0][3 * t + d] = x[d];
+                sh[1][3 * t + d] = v[d];
+                sh[2][3 * t + d] = f[d];
+            }
+        }
+        __syncthreads();
+        const ReadDest D = dest[tl.world];
+        const uint64_t k0 = tl.slot_begin - w.bead_base;  // the tile's first bead in its world
+        double *out[3] = {D.x, D.v, D.f};
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (!out[q]) continue;
+            if (D.stride == 24) {
+                double *o = out[q] + 3 * k0;
+                for (uint32_t i = t; i < 3 * cnt; i += TILE_BEADS) o[i] = sh[q][i];
+            } else if (t < cnt) {
+                double *o = (double *)((char *)out[q] + (k0 + t) * D.stride);
+                o[0] = sh[q][3 * t];
+                o[1] = sh[q][3 * t + 1];
+                o[2] = sh[q][3 * t + 2];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+int launch_slot_of_id(const KArgs &a, uint32_t first, uint32_t count, uint32_t *inv, cudaStream_t s)
+{
+    if (count == 0) return 0;
+    k_slot_of_id<<<(count + 255) / 256, 256, 0, s>>>(a.ids, first, count, inv);
+    return 1;
+}
+
+int launch_read_direct(const KArgs &a, int fp64, const uint32_t *inv, const ReadDest *dest, cudaStream_t s)
+{
+    if (a.n_tiles == 0) return 0;
+    const uint32_t grid = std::min<uint32_t>(a.n_tiles, (uint32_t)std::max(1, a.grid_blocks));
+    if (fp64)
+        k_read_direct<1><<<grid, TILE_BEADS, 0, s>>>(a, inv, dest);
+    else
+        k_read_direct<0><<<grid, TILE_BEADS, 0, s>>>(a, inv, dest);
+    return 1;
+}
 
 int launch_host_copy(const HostCopySeg *segs, const HostCopyChunk *chunks, uint32_t n_chunks, int sm_count,
                      cudaStream_t s)

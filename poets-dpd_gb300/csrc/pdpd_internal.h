@@ -189,6 +189,18 @@ struct HostCopyChunk {
 constexpr uint32_t HOSTCOPY_CHUNK = 16384;
 int launch_host_copy(const HostCopySeg *segs, const HostCopyChunk *chunks, uint32_t n_chunks, int sm_count,
                      cudaStream_t s);
+// Direct read-back of the rest state into the callers' host arrays (pdpd_hostio.cu): where
+// world w's x, v, f go (host pointers, null: not read; vectors `stride` bytes apart).
+struct ReadDest {
+    double *x, *v, *f;
+    uint64_t stride;
+};
+// inv[ids[s]] = s for the sorted slots [first, first + count): the slot of each bead id.
+int launch_slot_of_id(const KArgs &a, uint32_t first, uint32_t count, uint32_t *inv, cudaStream_t s);
+// The work tiles of a.tiles[0, a.n_tiles) (each a run of bead ids of one world): each bead's
+// state gathered through inv, x = cell + offset in FP32, and each field of the tile written
+// to dest[world] as one contiguous run (or bead by bead at a stride).
+int launch_read_direct(const KArgs &a, int fp64, const uint32_t *inv, const ReadDest *dest, cudaStream_t s);
 
 // Device RNG on arrays (device pointers), for known-answer tests.
 int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,
