@@ -51,6 +51,7 @@ def build(verbose: bool = False) -> str:
         [nvcc] + common + ["-fmad=false", "-c", os.path.join(CSRC, "pdpd_codec.cu"), "-o",
                            os.path.join(BUILD, "pdpd_codec.o")],
         [nvcc] + common + ["-c", os.path.join(CSRC, "pdpd_hostio.cu"), "-o", os.path.join(BUILD, "pdpd_hostio.o")],
+        [nvcc] + common + ["-c", os.path.join(CSRC, "pdpd_bondcsr.cu"), "-o", os.path.join(BUILD, "pdpd_bondcsr.o")],
         ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
          "-c", os.path.join(CSRC, "pdpd_engine.cpp"), "-o", os.path.join(BUILD, "pdpd_engine.o")],
     ]
@@ -58,7 +59,7 @@ def build(verbose: bool = False) -> str:
         logs = list(ex.map(_run, jobs))
     objs = [os.path.join(BUILD, n) for n in ("pdpd_fp32.o", "pdpd_fp64.o", "pdpd_sort.o",
                                               "pdpd_observe.o", "pdpd_codec.o", "pdpd_hostio.o",
-                                              "pdpd_engine.o")]
+                                              "pdpd_bondcsr.o", "pdpd_engine.o")]
     tmp = LIB + ".tmp"
     _run([nvcc, "-shared"] + ARCH + objs + ["-o", tmp, "-lcudart"])
     os.replace(tmp, LIB)

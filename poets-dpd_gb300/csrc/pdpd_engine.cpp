@@ -301,9 +301,12 @@ struct pdpd_engine {
     HostPinned h_staging[2];
     HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
     HostPinned h_err;
+    HostPinned h_small;  // attach: the number of polymer beads, from the device
     DevBuf d_v2err;
     DevBuf d_hostio;  // segment and chunk tables of the direct host copies, or the read-back's destinations
-    DevBuf d_inv;     // direct read-back: the sorted slot of each bead id
+    DevBuf d_inv;     // direct read-back: the sorted slot of each bead id; attach: scratch
+    DevBuf d_blist;   // attach: the flat bond lists with global ids
+    DevBuf d_scan;    // attach: scan block sums, then the number of polymer beads
     cudaEvent_t ev_snap[2] = {nullptr, nullptr};
     cudaEvent_t ev_copied[2] = {nullptr, nullptr};
 
@@ -354,7 +357,7 @@ struct pdpd_engine {
                           &d_keyrank, &d_tmp, &d_bond_row, &d_bond_terms, &d_bond_params,
                           &d_pair, &d_hash, &d_bonded, &d_fbond, &d_staging[0], &d_staging[1],
                           &d_v2err, &d_cellpair, &d_posf, &d_bterm, &d_zlo, &d_brick_next, &d_hash_old,
-                          &d_hostio, &d_inv};
+                          &d_hostio, &d_inv, &d_blist, &d_scan};
         for (DevBuf *b : bufs) b->release();
         worlds.clear();
         attached = false;
@@ -919,6 +922,8 @@ void pdpd_destroy(pdpd_engine *e)
     e->h_staging[0].release();
     e->h_staging[1].release();
     e->h_err.release();
+    e->h_small.release();
+    e->h_meta.release();
     for (int i = 0; i < 2; i++) {
         if (e->ev_snap[i]) cudaEventDestroy(e->ev_snap[i]);
         if (e->ev_copied[i]) cudaEventDestroy(e->ev_copied[i]);
@@ -1018,9 +1023,9 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         n_terms += 2ull * ws[i].n_bonds + 3ull * ws[i].n_angles;
         n_bparams += ws[i].n_bonds + ws[i].n_angles;
     }
-    if (nb >= (1ull << 31) || nc >= (1ull << 31))
-        return e->fail(PDPD_E_UNSUPPORTED, "batch too large (%llu beads, %llu cells)",
-                       (unsigned long long)nb, (unsigned long long)nc);
+    if (nb >= (1ull << 31) || nc >= (1ull << 31) || n_terms >= (1ull << 32))
+        return e->fail(PDPD_E_UNSUPPORTED, "batch too large (%llu beads, %llu cells, %llu bond terms)",
+                       (unsigned long long)nb, (unsigned long long)nc, (unsigned long long)n_terms);
     e->n_beads = (uint32_t)nb;
     e->n_cells = (uint32_t)nc;
 
@@ -1130,22 +1135,20 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         }
     }
 
-    // --- bond CSR (per bead, by global id): Hookean terms first, then angle terms, each in
-    // the flat list order.
-    // (no bond terms at all, e.g. pure water: the rows are all zero and are set on the device)
-    // Rows and terms are built in pinned memory (uploaded from there, asynchronously), in
-    // passes over all the batch's bond and angle terms split across host threads whatever the
-    // worlds' sizes (one large world as fast as many small ones): counts by atomic increments,
-    // a prefix, terms placed through atomic per-bead cursors, then each bead's few terms put
-    // in flat-list order.
-    // Parameters: every world's Hookean bonds in order, then every world's angle bonds.
+    // --- bond tables.  The host writes the batch's flat bond lists with global ids and the
+    // parameter rows into pinned memory, in one pass over all the batch's bond and angle terms
+    // split across host threads whatever the worlds' sizes (one large world as fast as many
+    // small ones); the per-bead CSR (Hookean terms first, then angle terms, each in flat-list
+    // order) and the list of polymer beads are built from them on the device
+    // (pdpd_bondcsr.cu).  Parameters: every world's Hookean bonds in order, then every world's
+    // angle bonds.
     std::vector<uint32_t> bond_off(n_worlds + 1, 0), angle_off(n_worlds + 1, 0);
     for (uint32_t i = 0; i < n_worlds; i++) {
         bond_off[i + 1] = bond_off[i] + ws[i].n_bonds;
         angle_off[i + 1] = angle_off[i] + ws[i].n_angles;
     }
     const uint32_t n_bond_par = bond_off[n_worlds], n_angle_par = angle_off[n_worlds];
-    // fn(world, k) for the global terms [g0, g1) of a per-world list with offsets off
+    // fn(world, k, g) for the global terms [g0, g1) of a per-world list with offsets off
     auto over_terms = [&](const std::vector<uint32_t> &off, size_t n, auto fn) {
         parallel_for(n, 1 << 14, [&](size_t g0, size_t g1) {
             uint32_t i = (uint32_t)(std::upper_bound(off.begin(), off.end(), (uint32_t)g0) - off.begin()) - 1;
@@ -1155,97 +1158,40 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             }
         });
     };
-    uint32_t *row = nullptr;
-    BondTerm *terms = nullptr;
-    std::unique_ptr<uint32_t[]> fill(n_terms ? new uint32_t[nb] : nullptr);  // per-bead cursors
-    std::vector<double> bp64(f64 ? 4 * (size_t)n_bparams : 0);
-    std::vector<float> bp32(f64 ? 0 : 4 * (size_t)n_bparams);
+    const size_t list_bytes = (sizeof(uint32_t) * (2 * (size_t)n_bond_par + 3 * (size_t)n_angle_par) + 15) & ~size_t(15);
+    const size_t par_bytes = (f64 ? sizeof(double) : sizeof(float)) * 4 * (size_t)n_bparams;
+    if (e->h_meta.alloc(std::max<size_t>(16, list_bytes + par_bytes)) != cudaSuccess) {
+        e->release();  // (waits for the direct copy, which reads the caller's arrays)
+        return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
+    }
+    uint32_t *h_pairs = (uint32_t *)e->h_meta.p, *h_triples = h_pairs + 2 * (size_t)n_bond_par;
+    void *h_par = (char *)e->h_meta.p + list_bytes;
     auto put = [&](uint32_t pidx, const double p[4]) {
         for (int q = 0; q < 4; q++) {
-            if (f64) bp64[4 * (size_t)pidx + q] = p[q];
-            else bp32[4 * (size_t)pidx + q] = (float)p[q];
+            if (f64) ((double *)h_par)[4 * (size_t)pidx + q] = p[q];
+            else ((float *)h_par)[4 * (size_t)pidx + q] = (float)p[q];
         }
     };
-    if (n_terms) {
-        const size_t row_bytes = (sizeof(uint32_t) * (nb + 1) + 15) & ~size_t(15);
-        if (e->h_meta.alloc(row_bytes + sizeof(BondTerm) * n_terms) != cudaSuccess) {
-            e->release();  // (waits for the direct copy, which reads the caller's arrays)
-            return e->fail(PDPD_E_NOMEM, "pinned host allocation failed");
-        }
-        row = (uint32_t *)e->h_meta.p;
-        terms = (BondTerm *)((char *)e->h_meta.p + row_bytes);
-        parallel_for(nb + 1, 1 << 18, [&](size_t i0, size_t i1) { memset(row + i0, 0, sizeof(uint32_t) * (i1 - i0)); });
-        auto bump = [&](uint32_t g) { __atomic_fetch_add(row + g + 1, 1u, __ATOMIC_RELAXED); };
-        over_terms(bond_off, n_bond_par, [&](uint32_t i, uint32_t k, uint32_t) {
-            const uint32_t bb = wdev[i].bead_base;
-            bump(bb + ws[i].bond_beads[2 * k]);
-            bump(bb + ws[i].bond_beads[2 * k + 1]);
-        });
-        over_terms(angle_off, n_angle_par, [&](uint32_t i, uint32_t k, uint32_t) {
-            const uint32_t bb = wdev[i].bead_base;
-            for (int q = 0; q < 3; q++) bump(bb + ws[i].angle_beads[3 * k + q]);
-        });
-        // inclusive prefix of row[1..nb] in parallel chunks: chunk sums, then offsets
-        const size_t n = nb, chunks = std::min<size_t>(64, std::max<size_t>(1, n >> 16));
-        const size_t per = (n + chunks - 1) / chunks;
-        std::vector<uint32_t> part(chunks + 1, 0);
-        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
-            for (size_t c = c0; c < c1; c++) {
-                uint32_t acc = 0;
-                for (size_t i = c * per; i < std::min(n, (c + 1) * per); i++) acc += row[i + 1];
-                part[c + 1] = acc;
-            }
-        });
-        for (size_t c = 0; c < chunks; c++) part[c + 1] += part[c];
-        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
-            for (size_t c = c0; c < c1; c++) {
-                uint32_t acc = part[c];
-                for (size_t i = c * per; i < std::min(n, (c + 1) * per); i++) row[i + 1] = acc += row[i + 1];
-            }
-        });
-        parallel_for(nb, 1 << 18, [&](size_t i0, size_t i1) {
-            memcpy(fill.get() + i0, row + i0, sizeof(uint32_t) * (i1 - i0));
-        });
-        auto slot = [&](uint32_t g) { return __atomic_fetch_add(fill.get() + g, 1u, __ATOMIC_RELAXED); };
-        over_terms(bond_off, n_bond_par, [&](uint32_t i, uint32_t k, uint32_t pidx) {
-            const pdpd_world &w = ws[i];
-            const uint32_t bb = wdev[i].bead_base;
-            const uint32_t h = bb + w.bond_beads[2 * k], t = bb + w.bond_beads[2 * k + 1];
-            terms[slot(h)] = {0u | (0u << 8), t, t, pidx};
-            terms[slot(t)] = {0u | (1u << 8), h, h, pidx};
-            const double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
-            put(pidx, p);
-        });
-        over_terms(angle_off, n_angle_par, [&](uint32_t i, uint32_t k, uint32_t g) {
-            const pdpd_world &w = ws[i];
-            const uint32_t bb = wdev[i].bead_base;
-            const uint32_t pidx = n_bond_par + g;
-            const uint32_t h = bb + w.angle_beads[3 * k], m = bb + w.angle_beads[3 * k + 1],
-                           t = bb + w.angle_beads[3 * k + 2];
-            terms[slot(h)] = {1u | (0u << 8), m, t, pidx};
-            terms[slot(m)] = {1u | (1u << 8), h, t, pidx};
-            terms[slot(t)] = {1u | (2u << 8), h, m, pidx};
-            const double th = w.angle_theta0[k];
-            const double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
-            put(pidx, p);
-        });
-        // each bead's terms in flat-list order (parameter index, then role): the order the
-        // threads placed them in is arbitrary, a bead has only a few
-        parallel_for(nb, 1 << 16, [&](size_t b0, size_t b1) {
-            for (size_t bd = b0; bd < b1; bd++) {
-                BondTerm *t0 = terms + row[bd], *t1 = terms + row[bd + 1];
-                for (BondTerm *x = t0 + 1; x < t1; x++) {
-                    const BondTerm v = *x;
-                    BondTerm *y = x;
-                    for (; y > t0 && (y[-1].param > v.param || (y[-1].param == v.param && y[-1].meta > v.meta)); y--)
-                        *y = y[-1];
-                    *y = v;
-                }
-            }
-        });
+    size_t bead_base_of = 0;
+    std::vector<uint32_t> bb_of(n_worlds);
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        bb_of[i] = (uint32_t)bead_base_of;
+        bead_base_of += ws[i].n_beads;
     }
-    // The per-bead order is this bead's Hookean terms in flat order, then its angle terms in
-    // flat order: each bead belongs to one world, whose bonds are filled before its angles.
+    over_terms(bond_off, n_bond_par, [&](uint32_t i, uint32_t k, uint32_t g) {
+        const pdpd_world &w = ws[i];
+        h_pairs[2 * (size_t)g] = bb_of[i] + w.bond_beads[2 * (size_t)k];
+        h_pairs[2 * (size_t)g + 1] = bb_of[i] + w.bond_beads[2 * (size_t)k + 1];
+        const double p[4] = {w.bond_kappa[k], w.bond_r0[k], 0, 0};
+        put(g, p);
+    });
+    over_terms(angle_off, n_angle_par, [&](uint32_t i, uint32_t k, uint32_t g) {
+        const pdpd_world &w = ws[i];
+        for (int q = 0; q < 3; q++) h_triples[3 * (size_t)g + q] = bb_of[i] + w.angle_beads[3 * (size_t)k + q];
+        const double th = w.angle_theta0[k];
+        const double p[4] = {w.angle_kappa[k], std::cos(th), std::sin(th), 0};
+        put(n_bond_par + g, p);
+    });
 
     // --- allocate
     const size_t P = payload_bytes(f64);
@@ -1277,32 +1223,10 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     A(e->d_pair, (f64 ? sizeof(double) : sizeof(float)) * 2 * n_pair);
     A(e->d_cellpair, std::max<size_t>(16, f64 ? sizeof(double) * cp64.size() : sizeof(float) * cp32.size()));
     A(e->d_hash, sizeof(uint32_t) * nb);
-    // Polymer beads (monomer bit of the hash clear), for the bond kernels: one pass over the
-    // whole batch in chunks of global slots, concatenated in slot order.
-    std::vector<uint32_t> bonded;
-    {
-        const size_t chunks = std::min<size_t>(256, std::max<size_t>(1, nb >> 16));
-        const size_t per = (nb + chunks - 1) / chunks;
-        std::vector<std::vector<uint32_t>> part(chunks);
-        parallel_for(chunks, 1, [&](size_t c0, size_t c1) {
-            for (size_t c = c0; c < c1; c++) {
-                const size_t g0 = c * per, g1 = std::min<size_t>(nb, g0 + per);
-                if (g0 >= g1) continue;
-                uint32_t i = (uint32_t)(std::upper_bound(wdev.begin(), wdev.end(), (uint32_t)g0,
-                                                         [](uint32_t g, const WorldDev &d) { return g < d.bead_base; }) -
-                                        wdev.begin()) - 1;
-                for (size_t g = g0; g < g1;) {
-                    while (g >= (size_t)wdev[i].bead_base + ws[i].n_beads) i++;
-                    const size_t bb = wdev[i].bead_base, k1 = std::min<size_t>(g1 - bb, ws[i].n_beads);
-                    for (size_t k = g - bb; k < k1; k++)
-                        if (!(ws[i].hash[k] & (1u << 27))) part[c].push_back((uint32_t)(bb + k));
-                    g = bb + k1;
-                }
-            }
-        });
-        for (const auto &p : part) bonded.insert(bonded.end(), p.begin(), p.end());
-    }
-    A(e->d_bonded, sizeof(uint32_t) * std::max<size_t>(1, bonded.size()));
+    A(e->d_bonded, sizeof(uint32_t) * std::max<uint64_t>(1, nb));
+    A(e->d_blist, std::max<size_t>(16, list_bytes));
+    A(e->d_inv, sizeof(uint32_t) * std::max<uint64_t>(1, nb));
+    A(e->d_scan, sizeof(uint32_t) * (scan_blocks((uint32_t)nb) + 1));
     A(e->d_fbond, f64 ? 16 : sizeof(float4) * std::max<uint64_t>(1, nb));
     A(e->d_posf, f64 ? sizeof(float4) * std::max<uint64_t>(1, nb) : 16);
     A(e->d_bterm, f64 ? sizeof(double) * 4 * std::max<uint64_t>(1, n_terms) : 16);
@@ -1386,17 +1310,12 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     };
     H2D(e->d_worlds, wdev.data(), sizeof(WorldDev) * n_worlds);
     H2D(e->d_tiles, tiles.data(), sizeof(Tile) * tiles.size());
-    if (n_terms)
-        H2D(e->d_bond_row, row, sizeof(uint32_t) * (nb + 1));
-    else if (ce == cudaSuccess)
-        ce = cudaMemsetAsync(e->d_bond_row.p, 0, sizeof(uint32_t) * (nb + 1), s);
-    H2D(e->d_bond_terms, terms, sizeof(BondTerm) * n_terms);
+    H2D(e->d_blist, h_pairs, sizeof(uint32_t) * (2 * (size_t)n_bond_par + 3 * (size_t)n_angle_par));
+    H2D(e->d_bond_params, h_par, par_bytes);
     if (f64) {
-        H2D(e->d_bond_params, bp64.data(), sizeof(double) * bp64.size());
         H2D(e->d_pair, pair64.data(), sizeof(double) * pair64.size());
         H2D(e->d_cellpair, cp64.data(), sizeof(double) * cp64.size());
     } else {
-        H2D(e->d_bond_params, bp32.data(), sizeof(float) * bp32.size());
         H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
         H2D(e->d_cellpair, cp32.data(), sizeof(float) * cp32.size());
     }
@@ -1424,7 +1343,20 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
                                        cudaMemcpyDeviceToDevice, s);
         }
     }
-    H2D(e->d_bonded, bonded.data(), sizeof(uint32_t) * bonded.size());
+    if (ce == cudaSuccess) {  // (after every write of d_hash)
+        const uint32_t *d_pairs = e->d_blist.as<uint32_t>();
+        e->launches += launch_bond_tables((uint32_t)nb, d_pairs, n_bond_par, d_pairs + 2 * (size_t)n_bond_par,
+                                          n_angle_par, e->d_hash.as<uint32_t>(), e->d_bond_row.as<uint32_t>(),
+                                          e->d_bond_terms.as<BondTerm>(), e->d_bonded.as<uint32_t>(),
+                                          e->d_scan.as<uint32_t>() + scan_blocks((uint32_t)nb),
+                                          e->d_inv.as<uint32_t>(), e->d_slot_of_id.as<uint32_t>(),
+                                          e->d_scan.as<uint32_t>(), s);
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess && e->h_small.alloc(16) != cudaSuccess) ce = cudaErrorMemoryAllocation;
+    if (ce == cudaSuccess)  // the number of polymer beads, read at the end of the attach
+        ce = cudaMemcpyAsync(e->h_small.p, e->d_scan.as<uint32_t>() + scan_blocks((uint32_t)nb), sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, s);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(e->d_cnt.p, 0, sizeof(uint32_t) * nc, s);
     uint32_t total = (uint32_t)nb;  // start[n_cells] = total beads, fixed for the attach
     if (ce == cudaSuccess)
@@ -1464,7 +1396,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     a.pair = e->d_pair.p;
     a.cellpair = e->d_cellpair.p;
     a.bonded_ids = e->d_bonded.as<uint32_t>();
-    a.n_bonded = (uint32_t)bonded.size();
+    a.n_bonded = 0;  // (known once the attach's kernels have run, below)
     a.fbond = e->d_fbond.as<float4>();
     a.posf = f64 ? e->d_posf.as<float4>() : nullptr;
     a.zlo = f64 ? nullptr : e->d_zlo.as<uint16_t>();
@@ -1502,6 +1434,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     }
     e->attached = true;
     int rc = e->check_device_errors();
+    a.n_bonded = *(const uint32_t *)e->h_small.p;
     if (rc) {
         std::string m = e->err;
         e->release();

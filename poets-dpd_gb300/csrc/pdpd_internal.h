@@ -1,5 +1,6 @@
 // Internal interface between the host runtime (pdpd_engine.cpp) and the kernel
-// translation units (pdpd_fp32.cu, pdpd_fp64.cu, pdpd_sort.cu).  Not part of the C ABI.
+// translation units (pdpd_fp32.cu, pdpd_fp64.cu, pdpd_sort.cu, pdpd_bondcsr.cu, pdpd_hostio.cu,
+// pdpd_observe.cu, pdpd_codec.cu).  Not part of the C ABI.
 #pragma once
 
 #include <cstddef>
@@ -201,6 +202,18 @@ int launch_slot_of_id(const KArgs &a, uint32_t first, uint32_t count, uint32_t *
 // state gathered through inv, x = cell + offset in FP32, and each field of the tile written
 // to dest[world] as one contiguous run (or bead by bead at a stride).
 int launch_read_direct(const KArgs &a, int fp64, const uint32_t *inv, const ReadDest *dest, cudaStream_t s);
+
+// Exclusive prefix sum of cnt[0, n) into start[0, n), clearing cnt (pdpd_sort.cu); blocksums
+// holds scan_blocks(n) words.
+void launch_scan(uint32_t *cnt, uint32_t n, uint32_t *blocksums, uint32_t *start, cudaStream_t s);
+// Attach (pdpd_bondcsr.cu): the per-bead bond CSR (row: n_beads + 1 offsets, terms) from the
+// batch's flat lists with global ids -- pairs (head, tail) of the Hookean bonds, parameter k
+// for bond k, and triples (head, middle, tail) of the angle bonds, parameter n_bonds + g for
+// angle g -- and the polymer beads' ids in id order (bonded; their number to *n_bonded).
+// Scratch: scratch and pos n_beads words each, blocksums scan_blocks(n_beads) words.
+int launch_bond_tables(uint32_t n_beads, const uint32_t *pairs, uint32_t n_bonds, const uint32_t *triples,
+                       uint32_t n_angles, const uint32_t *hash, uint32_t *row, BondTerm *terms, uint32_t *bonded,
+                       uint32_t *n_bonded, uint32_t *scratch, uint32_t *pos, uint32_t *blocksums, cudaStream_t s);
 
 // Device RNG on arrays (device pointers), for known-answer tests.
 int launch_rng_eval(size_t n, const uint32_t *t, const uint64_t *seed, const uint32_t *a,

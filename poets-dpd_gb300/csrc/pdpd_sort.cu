@@ -180,6 +180,14 @@ __global__ void k_canon(uint32_t n, const uint4 *__restrict__ tmp, const uint32_
     if (shadow_out) shadow_out[dst] = offset_shadow(p);
 }
 
+void launch_scan(uint32_t *cnt, uint32_t n, uint32_t *blocksums, uint32_t *start, cudaStream_t s)
+{
+    if (n == 0) return;
+    const uint32_t nb = scan_blocks(n);
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(cnt, n, blocksums, nullptr, 0, 0, nullptr);
+    k_scan_final<<<nb, SCAN_THREADS, 0, s>>>(cnt, n, blocksums, start);
+}
+
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s)
 {
     const uint32_t nb = scan_blocks(a.n_cells);
