@@ -565,6 +565,13 @@ def kernel_config(eng):
             if k in ("force_kernel", "brick_x", "brick_y", "brick_z", "autotune")}
 
 
+def host_copies(eng):
+    """How the attach and the read-backs moved the beads: "direct" (a kernel reading and
+    writing the host arrays over the host link) or "staged" (pinned buffers and DMA)."""
+    v = {k: v for k, _, v in eng.GetConfigEntries()}.get("host_direct", "0")
+    return "direct" if v == "1" else "staged"
+
+
 def fixed_kernel(eng, args):
     """--force-kernel K: run FP32 force kernel K (no autotuning), for profiling a variant."""
     if args.force_kernel:
@@ -636,6 +643,7 @@ def measure_grid(args, dev, local, world_size):
     e2e = {"value": total * args.steps / e2e_dt, "unit": "bead-steps/s",
            "h2d_bytes_per_step": upload_bytes(worlds) / args.steps,
            "d2h_bytes_per_step": total * 72 / args.steps,
+           "host_copies": host_copies(eng),
            "note": "AttachBatch (upload of all states) + Run(K) + read-back of x, v, f of every "
                    "state; bytes are per step of K"}
     ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
@@ -679,7 +687,7 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
     e2e_dt = time.perf_counter() - t0
     e2e = {"value": n * args.steps / e2e_dt, "unit": "bead-steps/s",
            "h2d_bytes_per_step": upload_bytes([world]) / args.steps,
-           "d2h_bytes_per_step": n * 72 / args.steps,
+           "d2h_bytes_per_step": n * 72 / args.steps, "host_copies": host_copies(eng),
            "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"}
     ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
                                      lambda: eng.Attach(world.copy()))

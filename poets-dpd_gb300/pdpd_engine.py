@@ -20,6 +20,7 @@ shared library must exist (built by ``build.py``); there is no CPU fallback.
 
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import os
 
@@ -192,7 +193,15 @@ def lib():
 
 
 def _p(a):
-    return a.ctypes.data if a is not None and a.size else None
+    """Address of an array's first element (None for a missing or empty array): through the
+    buffer protocol where the array is writable (a third of the cost of ``a.ctypes``, which
+    counts at one call per array of every world of a batch), else ``a.ctypes``."""
+    if a is None or not a.size:
+        return None
+    try:
+        return C.addressof(C.c_char.from_buffer(a))
+    except (TypeError, ValueError, BufferError):
+        return a.ctypes.data
 
 
 def _dest(world, name, n):
@@ -201,9 +210,10 @@ def _dest(world, name, n):
     the WorldState's beads (its pages are already mapped, unlike a new array's) -- else a new
     array."""
     a = getattr(world, name, None) if world is not None else None
-    if (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.shape == (n, 3)
-            and a.flags.c_contiguous and a.flags.writeable):
-        return a
+    if isinstance(a, np.ndarray) and a.dtype == np.float64 and a.shape == (n, 3):
+        fl = a.flags
+        if fl.c_contiguous and fl.writeable:
+            return a
     return np.empty((n, 3))
 
 
@@ -237,15 +247,23 @@ class _Flat:
         self.struct = s
 
 
+_TOPOLOGY_ARRAYS = ("bead_type", "is_monomer", "polymer_id", "polymer_offset", "poly_type", "poly_start",
+                    "poly_beads")
+
+
 def _topology_struct(world):
     """A PdpdWorld with the hash and bond fields of the World's topology set (and the arrays
-    they point to), cached with the World while those arrays are the same objects."""
-    hash_ = world.hashes()
-    bonds = world.flat_bonds()
+    they point to), cached with the World (and its copies) while its topology arrays are the
+    same objects and its polymer types equal those the struct was made from -- what the
+    World's own hash and bond-list caches depend on."""
     cache = world.__dict__.setdefault("_cache", {})
     hit = cache.get("abi")
-    if hit is not None and hit[0] is hash_ and hit[1] is bonds:
-        return hit[2], hit[3]
+    if hit is not None:
+        d = world.__dict__
+        if all(d.get(k) is a for k, a in zip(_TOPOLOGY_ARRAYS, hit[4])) and hit[5] == world.polymer_types:
+            return hit[2], hit[3]
+    hash_ = world.hashes()
+    bonds = world.flat_bonds()
     h = np.ascontiguousarray(hash_, np.uint32)
     bb, bk, br, ab, ak, at = bonds
     arrs = (h, np.ascontiguousarray(bb, np.uint32), np.ascontiguousarray(bk), np.ascontiguousarray(br),
@@ -256,7 +274,8 @@ def _topology_struct(world):
     s.n_bonds, s.bond_beads, s.bond_kappa, s.bond_r0 = arrs[1].shape[0], _p(arrs[1]), _p(arrs[2]), _p(arrs[3])
     s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (arrs[4].shape[0], _p(arrs[4]), _p(arrs[5]),
                                                                 _p(arrs[6]))
-    cache["abi"] = (hash_, bonds, s, arrs)
+    cache["abi"] = (hash_, bonds, s, arrs, tuple(getattr(world, k) for k in _TOPOLOGY_ARRAYS),
+                    copy.deepcopy(world.polymer_types))
     return s, arrs
 
 
@@ -504,7 +523,9 @@ class GB300DPDEngine:
         out = [(x, v, f, int(ts[i])) for i, (x, v, f) in enumerate(arrs)]
         if into is not None:
             for w, (x, v, f, t) in zip(into, out):
-                w.x, w.v, w.f, w.t = x, v, f, t
+                if w.x is not x or w.v is not v or w.f is not f:  # (else written in place)
+                    w.x, w.v, w.f = x, v, f
+                w.t = t
         return out
 
     def read_state(self, world_index=0, into=None):
