@@ -512,15 +512,51 @@ def grid_workload_name(n_states):
             f"5% H-T5 chains, a_WT ~ U[25,100], gamma ~ U[3,6], fp32 batched")
 
 
-def upload_bytes(worlds):
+def upload_bytes(worlds, fp64=False):
     """Host-to-device bytes of an Attach: x, v, f (doubles) and the hash of every bead, the
-    bond CSR rows and terms."""
+    flat bond lists (bead ids) and a parameter row per bond and angle (the per-bead bond
+    tables are built on the device)."""
     total = 0
     for w in worlds:
         n = w.n_beads
         bb, _, _, ab, _, _ = w.flat_bonds()
-        total += n * (9 * 8 + 4) + (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
+        total += (n * (9 * 8 + 4) + (2 * bb.shape[0] + 3 * ab.shape[0]) * 4
+                  + (bb.shape[0] + ab.shape[0]) * (32 if fp64 else 16))
     return total
+
+
+def host_link_gbs(device, nbytes=1 << 30):
+    """Pinned-memory DMA bandwidth of the host link each way (GB/s, best of 3 under CUDA
+    events): the floor under the e2e run's uploads and read-backs."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    out = {}
+    for name, (dst, src) in (("h2d", (d, h)), ("d2h", (h, d))):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = nbytes / best / 1e6
+    del h, d
+    return out
+
+
+def e2e_floor(e2e, steps, ms_per_step, link):
+    """The e2e rate if the uploads and read-backs ran at the link's DMA bandwidth and nothing
+    else cost time beside the K steps: adds link, copy_floor_ms, floor and frac_of_floor."""
+    copy_ms = (e2e["h2d_bytes_per_step"] * steps / link["h2d"] + e2e["d2h_bytes_per_step"] * steps / link["d2h"]) / 1e6
+    bead_steps = e2e["value"] * e2e["wall_s"]
+    floor = bead_steps / ((steps * ms_per_step + copy_ms) / 1e3)
+    e2e.update({"link_gbs": link, "copy_floor_ms": copy_ms, "floor": floor, "frac_of_floor": e2e["value"] / floor})
+    return e2e
 
 
 ISSUE_SLOTS_PER_S = 152 * 4 * 2.07e9  # warp-instruction issue slots per second of a GB300
@@ -640,7 +676,7 @@ def measure_grid(args, dev, local, world_size):
     eng.AttachBatch(hw)
     eng.Run(args.steps)  # Run() reads x, v, f of every state back into the host worlds
     e2e_dt = time.perf_counter() - t0
-    e2e = {"value": total * args.steps / e2e_dt, "unit": "bead-steps/s",
+    e2e = {"value": total * args.steps / e2e_dt, "unit": "bead-steps/s", "wall_s": e2e_dt,
            "h2d_bytes_per_step": upload_bytes(worlds) / args.steps,
            "d2h_bytes_per_step": total * 72 / args.steps,
            "host_copies": host_copies(eng),
@@ -650,6 +686,7 @@ def measure_grid(args, dev, local, world_size):
                                      lambda: eng.AttachBatch([w.copy() for w in worlds]))
     if tuned is None:  # the size-aware default the engine chose for this batch
         tuned = kernel_config(eng)
+    e2e_floor(e2e, args.steps, ms / args.steps, host_link_gbs(dev))
     roof, ph = force_roofline(eng.profile_run(args.steps), total, "fp32", "fp32_grid")
     eng.close()
     plain = plain_fp64_metrics(worlds, device=local) if not args.no_plain and world_size == 1 else None
@@ -685,14 +722,15 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
     eng.Attach(w_e2e)
     eng.Run(args.steps)  # Run() reads x, v, f back into the host world
     e2e_dt = time.perf_counter() - t0
-    e2e = {"value": n * args.steps / e2e_dt, "unit": "bead-steps/s",
-           "h2d_bytes_per_step": upload_bytes([world]) / args.steps,
+    e2e = {"value": n * args.steps / e2e_dt, "unit": "bead-steps/s", "wall_s": e2e_dt,
+           "h2d_bytes_per_step": upload_bytes([world], precision == "fp64") / args.steps,
            "d2h_bytes_per_step": n * 72 / args.steps, "host_copies": host_copies(eng),
            "note": "Attach (upload) + Run(K) + read-back of x, v, f; bytes are per step of K"}
     ms, launches, clocks = timed_run(eng, args.steps, args.warmup, dev, local, world_size,
                                      lambda: eng.Attach(world.copy()))
     if tuned is None:  # the size-aware default the engine chose for this world
         tuned = kernel_config(eng)
+    e2e_floor(e2e, args.steps, ms / args.steps, host_link_gbs(dev))
     roof, ph = force_roofline(eng.profile_run(args.steps), n, precision)
     snap = None
     if snapshot and world_size == 1:

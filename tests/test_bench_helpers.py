@@ -27,9 +27,21 @@ def test_upload_bytes_counts_state_hashes_and_bonds():
     w = W.make_polymer_box(8, chain_fraction=0.1, seed=3)
     bb, _, _, ab, _, _ = w.flat_bonds()
     n = w.n_beads
-    expect = n * (9 * 8 + 4) + (n + 1) * 4 + (2 * bb.shape[0] + 3 * ab.shape[0]) * 16
+    lists = (2 * bb.shape[0] + 3 * ab.shape[0]) * 4
+    expect = n * (9 * 8 + 4) + lists + (bb.shape[0] + ab.shape[0]) * 16
     assert bench.upload_bytes([w]) == expect
     assert bench.upload_bytes([w, w]) == 2 * expect
+    assert bench.upload_bytes([w], fp64=True) == expect + (bb.shape[0] + ab.shape[0]) * 16
+
+
+def test_e2e_floor_arithmetic():
+    # 1e9 bead-steps in 2 s; K = 10 steps of 100 ms (1 s); 200 GB up at 200 GB/s (1 s) and
+    # 100 GB down at 100 GB/s (1 s): a floor of 3 s
+    e2e = {"value": 5e8, "wall_s": 2.0, "h2d_bytes_per_step": 20e9, "d2h_bytes_per_step": 10e9}
+    out = bench.e2e_floor(e2e, 10, 100.0, {"h2d": 200.0, "d2h": 100.0})
+    assert out["copy_floor_ms"] == pytest.approx(2000.0)
+    assert out["floor"] == pytest.approx(1e9 / 3.0)
+    assert out["frac_of_floor"] == pytest.approx(5e8 / (1e9 / 3.0))
 
 
 def test_force_roofline_arithmetic():
