@@ -108,7 +108,12 @@ int pdpd_can_support(const pdpd_world *w, char *reason, size_t reason_len);
 double pdpd_max_bond_length(void);
 
 /* DPDEngine::Attach (dpd_engine.hpp:177): copy the world to the device and build its cell
- * list.  w == NULL detaches.  The host arrays are not retained. */
+ * list.  w == NULL detaches.  The host arrays are not retained.  With config host_direct (the
+ * default) on a device that reaches pageable host memory through the host's page tables, a
+ * GPU kernel reads x, v, f and hash from the caller's arrays directly (vectors 8-byte aligned
+ * at a stride that is a multiple of 8, hashes 4-byte aligned; else, or on other devices,
+ * through pinned staging): they must be ordinary host memory, readable until the call
+ * returns. */
 int pdpd_attach(pdpd_engine *e, const pdpd_world *w);
 
 /* Batched attach: n independent worlds share one device arena and are stepped together;
@@ -129,14 +134,17 @@ int pdpd_sync(pdpd_engine *e);
 void *pdpd_stream(pdpd_engine *e);
 
 /* Copy world `world`'s state x(t), v(t), f(t) and t to host arrays (bead-id order, vector
- * layout as in pdpd_world; any pointer may be NULL). */
+ * layout as in pdpd_world; any pointer may be NULL).  With host_direct (see pdpd_attach) a GPU
+ * kernel writes the arrays directly; nothing outside the vectors is written either way, and
+ * nothing at all when a world has failed. */
 int pdpd_read_state(pdpd_engine *e, uint32_t world, double *x, double *v, double *f,
                     size_t bead_stride_bytes, int64_t *t);
 
 /* Every world of an attached batch at once (after Run(nSteps) of a batch, DPDEngine::Run's
- * write-back of dpd_engine.hpp:179-184 for each state): one device unsort, one copy and a
- * parallel host scatter instead of one round trip per world.  out[i] receives world i's
- * state as pdpd_read_state would (any of its pointers may be NULL). */
+ * write-back of dpd_engine.hpp:179-184 for each state): one gather kernel writing every
+ * world's arrays (host_direct), or one device unsort, one copy and a parallel host scatter,
+ * instead of one round trip per world.  out[i] receives world i's state as pdpd_read_state
+ * would (any of its pointers may be NULL). */
 typedef struct pdpd_state_view {
     double *x, *v, *f;
     int64_t *t;
