@@ -549,6 +549,22 @@ def host_link_gbs(device, nbytes=1 << 30):
     return out
 
 
+def e2e_phases(eng, worlds, steps):
+    """Where an e2e run's wall time goes, from a second run of the same calls split at their
+    boundaries (wall clock, ms): AttachBatch of the host worlds (the Python binding's
+    flattening included), the K steps (run_async + sync), and the read-back of every state
+    into its host arrays."""
+    t0 = time.perf_counter()
+    eng.AttachBatch(worlds)
+    t1 = time.perf_counter()
+    eng.run_async(steps)
+    eng.sync()
+    t2 = time.perf_counter()
+    eng.read_states(into=worlds)
+    t3 = time.perf_counter()
+    return {"attach": 1e3 * (t1 - t0), "steps": 1e3 * (t2 - t1), "read_back": 1e3 * (t3 - t2)}
+
+
 def e2e_floor(e2e, steps, ms_per_step, link):
     """The e2e rate if the uploads and read-backs ran at the link's DMA bandwidth and nothing
     else cost time beside the K steps: adds link, copy_floor_ms, floor and frac_of_floor."""
@@ -686,6 +702,7 @@ def measure_grid(args, dev, local, world_size):
                                      lambda: eng.AttachBatch([w.copy() for w in worlds]))
     if tuned is None:  # the size-aware default the engine chose for this batch
         tuned = kernel_config(eng)
+    e2e["phases_ms"] = e2e_phases(eng, [w.copy() for w in worlds], args.steps)
     e2e_floor(e2e, args.steps, ms / args.steps, host_link_gbs(dev))
     roof, ph = force_roofline(eng.profile_run(args.steps), total, "fp32", "fp32_grid")
     eng.close()
@@ -730,6 +747,7 @@ def measure_box(args, name, side, precision, dev, local, world_size, autotune, s
                                      lambda: eng.Attach(world.copy()))
     if tuned is None:  # the size-aware default the engine chose for this world
         tuned = kernel_config(eng)
+    e2e["phases_ms"] = e2e_phases(eng, [world.copy()], args.steps)
     e2e_floor(e2e, args.steps, ms / args.steps, host_link_gbs(dev))
     roof, ph = force_roofline(eng.profile_run(args.steps), n, precision)
     snap = None
