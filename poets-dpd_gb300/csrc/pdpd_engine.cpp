@@ -302,6 +302,8 @@ struct pdpd_engine {
     HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
     HostPinned h_err;
     HostPinned h_small;  // attach: the number of polymer beads, from the device
+    HostPinned h_plan;   // the tables of a direct host copy, uploaded from here (each call
+                         // that copies directly waits for the copy before it returns)
     DevBuf d_v2err;
     DevBuf d_hostio;  // segment and chunk tables of the direct host copies, or the read-back's destinations
     DevBuf d_inv;     // direct read-back: the sorted slot of each bead id; attach: scratch
@@ -849,10 +851,12 @@ static int run_host_copy(pdpd_engine *e, const HostCopyPlan &plan, bool host_wri
     const size_t sb = (sizeof(HostCopySeg) * plan.segs.size() + 15) & ~size_t(15);
     const size_t cb = sizeof(HostCopyChunk) * plan.chunks.size();
     if (e->d_hostio.alloc(sb + cb) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "device allocation failed");
-    cudaError_t ce = cudaMemcpyAsync(e->d_hostio.p, plan.segs.data(), sizeof(HostCopySeg) * plan.segs.size(),
-                                     cudaMemcpyHostToDevice, e->stream);
-    if (ce == cudaSuccess)
-        ce = cudaMemcpyAsync((char *)e->d_hostio.p + sb, plan.chunks.data(), cb, cudaMemcpyHostToDevice, e->stream);
+    // (through pinned memory: a copy from pageable memory would wait for the stream's earlier
+    // work -- in a re-pack the previous epoch's steps -- and hold the host up with it)
+    if (e->h_plan.alloc(sb + cb) != cudaSuccess) return e->fail(PDPD_E_NOMEM, "pinned allocation failed");
+    memcpy(e->h_plan.p, plan.segs.data(), sizeof(HostCopySeg) * plan.segs.size());
+    memcpy((char *)e->h_plan.p + sb, plan.chunks.data(), cb);
+    cudaError_t ce = cudaMemcpyAsync(e->d_hostio.p, e->h_plan.p, sb + cb, cudaMemcpyHostToDevice, e->stream);
     if (ce != cudaSuccess) return e->cuda_fail(ce, "host copy tables");
     e->launches += launch_host_copy((const HostCopySeg *)e->d_hostio.p,
                                     (const HostCopyChunk *)((const char *)e->d_hostio.p + sb),
@@ -923,6 +927,7 @@ void pdpd_destroy(pdpd_engine *e)
     e->h_staging[1].release();
     e->h_err.release();
     e->h_small.release();
+    e->h_plan.release();
     e->h_meta.release();
     for (int i = 0; i < 2; i++) {
         if (e->ev_snap[i]) cudaEventDestroy(e->ev_snap[i]);
@@ -1032,12 +1037,16 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // With direct host copies (a whole batch from its descriptors, in arrays the copy kernel
     // may access) the kernel brings the beads field-major into device staging 0 and the
     // hashes, launched now so that the transfer runs while the host builds the tables below.
-    bool direct = !any_kept && e->host_direct();
+    // In a re-pack the kept worlds' rows come from the old arena (below) and the kernel brings
+    // only the new worlds', into rows of 9 doubles (x, v, f) like theirs.
+    bool direct = e->host_direct();
     for (uint32_t i = 0; direct && i < n_worlds; i++) {
         const pdpd_world &w = ws[i];
+        if (any_kept && keep_old[i] >= 0) continue;
         const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
         direct = vec_ok(w.x, sb) && vec_ok(w.v, sb) && vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
     }
+    const bool field_major = direct && !any_kept;  // the layout of device staging 0 for the bin
     if (direct) {
         if (e->d_staging[0].alloc(sizeof(double) * 9 * nb) != cudaSuccess ||
             e->d_hash.alloc(sizeof(uint32_t) * std::max<uint64_t>(1, nb)) != cudaSuccess) {
@@ -1052,10 +1061,16 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         for (uint32_t i = 0; i < n_worlds; i++) {
             const pdpd_world &w = ws[i];
             const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
-            plan.vectors(w.x, sb, ds + 3 * bb, 24, w.n_beads);
-            plan.vectors(w.v, sb, ds + 3 * (nb + bb), 24, w.n_beads);
-            plan.vectors(w.f, sb, ds + 3 * (2 * nb + bb), 24, w.n_beads);
-            plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
+            if (field_major) {
+                plan.vectors(w.x, sb, ds + 3 * bb, 24, w.n_beads);
+                plan.vectors(w.v, sb, ds + 3 * (nb + bb), 24, w.n_beads);
+                plan.vectors(w.f, sb, ds + 3 * (2 * nb + bb), 24, w.n_beads);
+                plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
+            } else if (keep_old[i] < 0) {
+                for (int q = 0; q < 3; q++)
+                    plan.vectors(q == 0 ? w.x : (q == 1 ? w.v : w.f), sb, ds + 9 * bb + 3 * q, 72, w.n_beads);
+                plan.add(HOSTCOPY_WORDS4, w.hash, dh + bb, w.n_beads);
+            }
             bb += w.n_beads;
         }
         int rc = run_host_copy(e, plan, false);
@@ -1319,7 +1334,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
         H2D(e->d_pair, pair32.data(), sizeof(float) * pair32.size());
         H2D(e->d_cellpair, cp32.data(), sizeof(float) * cp32.size());
     }
-    if (any_kept) {  // only the rows of the worlds that come from their descriptors
+    if (any_kept && !direct) {  // only the rows of the worlds that come from their descriptors
         for (uint32_t i = 0; i < n_worlds; i++)
             if (keep_old[i] < 0 && ws[i].n_beads && ce == cudaSuccess)
                 ce = cudaMemcpyAsync(e->d_staging[0].as<double>() + 9 * (size_t)wdev[i].bead_base,
@@ -1337,6 +1352,7 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             if (ws[i].n_beads == 0) continue;
             uint32_t *dst = e->d_hash.as<uint32_t>() + wdev[i].bead_base;
             const size_t n = sizeof(uint32_t) * ws[i].n_beads;
+            if (keep_old[i] < 0 && direct) continue;  // (the copy kernel's)
             ce = keep_old[i] < 0
                      ? cudaMemcpyAsync(dst, hh + hoff[i], n, cudaMemcpyHostToDevice, s)
                      : cudaMemcpyAsync(dst, e->d_hash_old.as<uint32_t>() + old_base[keep_old[i]], n,
@@ -1421,8 +1437,8 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     // --- bin + sort into the rest state
     const uint32_t *hash_in = e->d_hash.as<uint32_t>();
     {
-        KArgs ab = a;  // the direct copies left the staging field-major
-        ab.staging_fields = direct ? 1u : 0u;
+        KArgs ab = a;  // the direct copies of a whole batch left the staging field-major
+        ab.staging_fields = field_major ? 1u : 0u;
         ab.staging_n = (uint32_t)nb;
         e->launches += f64 ? launch_bin64(ab, hash_in, s) : launch_bin32(ab, hash_in, s);
     }
