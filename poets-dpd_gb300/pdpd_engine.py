@@ -275,8 +275,60 @@ def _topology_struct(world):
     s.n_angles, s.angle_beads, s.angle_kappa, s.angle_theta0 = (arrs[4].shape[0], _p(arrs[4]), _p(arrs[5]),
                                                                 _p(arrs[6]))
     cache["abi"] = (hash_, bonds, s, arrs, tuple(getattr(world, k) for k in _TOPOLOGY_ARRAYS),
-                    copy.deepcopy(world.polymer_types))
+                    copy.deepcopy(world.polymer_types), bytes(s))
     return s, arrs
+
+
+_WORLD_DTYPE = np.dtype(PdpdWorld)
+_VIEW_DTYPE = np.dtype(PdpdStateView)
+
+
+def _flat_batch(worlds):
+    """The PdpdWorld array of a batch attach, byte for byte the structs ``_Flat`` makes, built
+    column by column: each World's topology part as the bytes cached with it, its state and
+    parameters gathered into lists and written per field (the per-World cost of building
+    ctypes structs one by one counts once per state of a large batch).  Returns the array
+    and the arrays it points to, to keep alive for the call."""
+    n = len(worlds)
+    topo, keep = [], []
+    box = np.empty((n, 3), np.int32)
+    dt, lam, seed, t = [], [], [], []
+    ntypes, nbeads = [], []
+    ptr = {k: [] for k in ("conservative", "dissipative", "stationary", "x", "v", "f",
+                           "cell_conservative", "cell_dissipative")}
+    for i, w in enumerate(worlds):
+        _topology_struct(w)
+        topo.append(w.__dict__["_cache"]["abi"][6])
+        cons = np.ascontiguousarray(w.conservative, np.float64)
+        diss = np.ascontiguousarray(w.dissipative, np.float64)
+        stat = w.stationary
+        stat = (stat.view(np.uint8) if isinstance(stat, np.ndarray) and stat.dtype == np.bool_
+                and stat.flags.c_contiguous else np.ascontiguousarray(stat, np.uint8))
+        x = np.ascontiguousarray(w.x, np.float64)
+        v = np.ascontiguousarray(w.v, np.float64)
+        f = np.ascontiguousarray(w.f, np.float64)
+        cc, cd = getattr(w, "cell_conservative", None), getattr(w, "cell_dissipative", None)
+        cc = None if cc is None else np.ascontiguousarray(cc, np.float64)
+        cd = None if cd is None else np.ascontiguousarray(cd, np.float64)
+        keep.append((cons, diss, stat, x, v, f, cc, cd))
+        box[i] = w.box
+        dt.append(float(w.dt))
+        lam.append(float(w.lam))
+        seed.append(int(w.seed) & 0xFFFFFFFFFFFFFFFF)
+        t.append(int(w.t))
+        ntypes.append(cons.shape[0])
+        nbeads.append(x.shape[0])
+        for k, a in zip(ptr, (cons, diss, stat, x, v, f, cc, cd)):
+            ptr[k].append(_p(a) or 0)
+    out = np.frombuffer(b"".join(topo), _WORLD_DTYPE).copy() if n else np.zeros(0, _WORLD_DTYPE)
+    out["box"] = box
+    out["dt"], out["lam"] = dt, lam
+    out["seed"] = np.array(seed, np.uint64)
+    out["t"] = t
+    out["n_bead_types"], out["n_beads"] = ntypes, nbeads
+    for k, v in ptr.items():
+        out[k] = np.array(v, np.uint64)
+    return out, keep
 
 
 def can_support(world) -> str:
@@ -361,9 +413,10 @@ class GB300DPDEngine:
         self._worlds = [world]
 
     def AttachBatch(self, worlds):
-        flats = [_Flat(w) for w in worlds]
-        arr = (PdpdWorld * len(flats))(*[f.struct for f in flats])
-        self._check(lib().pdpd_attach_batch(self._h, arr, len(flats)), "AttachBatch")
+        arr, keep = _flat_batch(worlds)
+        self._check(lib().pdpd_attach_batch(self._h, arr.ctypes.data_as(C.POINTER(PdpdWorld)), len(arr)),
+                    "AttachBatch")
+        del keep
         self._worlds = list(worlds)
 
     def Run(self, *args):
@@ -513,13 +566,15 @@ class GB300DPDEngine:
         list of (x, v, f, t), and writes them into the given Worlds when ``into`` is given."""
         n = len(self._worlds)
         dst = into if into is not None else [None] * n
-        arrs = [tuple(_dest(d, k, w.n_beads) for k in ("x", "v", "f")) for w, d in zip(self._worlds, dst)]
-        ts = (C.c_int64 * max(1, n))()
-        views = (PdpdStateView * max(1, n))()
-        for i, (x, v, f) in enumerate(arrs):
-            views[i].x, views[i].v, views[i].f = _p(x), _p(v), _p(f)
-            views[i].t = C.addressof(ts) + 8 * i
-        self._check(lib().pdpd_read_states(self._h, n, views, 24), "read_states")
+        arrs = [(_dest(d, "x", w.n_beads), _dest(d, "v", w.n_beads), _dest(d, "f", w.n_beads))
+                for w, d in zip(self._worlds, dst)]
+        ts = np.zeros(max(1, n), np.int64)
+        views = np.zeros(max(1, n), _VIEW_DTYPE)  # (filled per field: one World costs little)
+        for q, k in enumerate(("x", "v", "f")):
+            views[k][:n] = [_p(a[q]) or 0 for a in arrs]
+        views["t"] = ts.ctypes.data + 8 * np.arange(max(1, n), dtype=np.uint64)
+        self._check(lib().pdpd_read_states(self._h, n, views.ctypes.data_as(C.POINTER(PdpdStateView)), 24),
+                    "read_states")
         out = [(x, v, f, int(ts[i])) for i, (x, v, f) in enumerate(arrs)]
         if into is not None:
             for w, (x, v, f, t) in zip(into, out):
