@@ -299,7 +299,7 @@ struct pdpd_engine {
     DevBuf d_bond_row, d_bond_terms, d_bond_params, d_pair, d_hash, d_bonded, d_fbond, d_cellpair, d_posf, d_bterm, d_zlo, d_brick_next, d_hash_old;
     DevBuf d_staging[2];
     HostPinned h_staging[2];
-    HostPinned h_meta;  // attach: the bond CSR rows and terms, built here and uploaded from here
+    HostPinned h_meta;  // attach: the flat bond lists and parameter rows, written here and uploaded from here
     HostPinned h_err;
     HostPinned h_small;  // attach: the number of polymer beads, from the device
     HostPinned h_plan;   // the tables of a direct host copy, uploaded from here (each call
