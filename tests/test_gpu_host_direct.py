@@ -36,7 +36,9 @@ def _batch():
 def test_device_reports_pageable_host_access():
     """Which path the default takes on this device (informational: the staged path is correct
     everywhere, the direct one only where the device reaches pageable host memory)."""
-    cfg = {n: v for n, _, v in E.GB300DPDEngine("fp32").GetConfigEntries()}
+    eng = E.GB300DPDEngine("fp32")
+    eng.SetConfigEntry("host_direct", 1)  # (the default, whatever the test run forces)
+    cfg = {n: v for n, _, v in eng.GetConfigEntries()}
     if "staged" in cfg["host_direct"]:
         pytest.skip("host_direct: " + cfg["host_direct"])
     assert cfg["host_direct"] == "1"
