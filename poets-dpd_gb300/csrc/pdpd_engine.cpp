@@ -755,7 +755,10 @@ static const double *vec_at(const double *base, size_t stride_bytes, uint32_t i)
     return (const double *)((const char *)base + s * (size_t)i);
 }
 
-// A plan of direct host copies: segments cut into chunks of at most HOSTCOPY_CHUNK units.
+// A plan of direct host copies (uploads: the host is the source): segments cut into chunks of
+// at most HOSTCOPY_CHUNK units.  A run of words is cut at the 128-byte lines of its source,
+// so that every warp of the copy kernel reads whole lines (a short first chunk up to the
+// first line boundary): lines read in parts by two blocks cross the link more slowly.
 struct HostCopyPlan {
     std::vector<HostCopySeg> segs;
     std::vector<HostCopyChunk> chunks;
@@ -764,7 +767,16 @@ struct HostCopyPlan {
         if (n == 0) return;
         const uint32_t si = (uint32_t)segs.size();
         segs.push_back({src, dst, n, kind, src_stride, dst_stride, 0});
-        for (uint64_t k = 0; k < n; k += HOSTCOPY_CHUNK)
+        uint64_t k = 0;
+        if (kind != HOSTCOPY_TRIPLES) {
+            const uint64_t wb = kind == HOSTCOPY_WORDS8 ? 8 : 4;
+            const uint64_t lead = ((128 - ((uintptr_t)src & 127)) & 127) / wb;  // words before a line boundary
+            if (lead > 0 && lead < n) {
+                chunks.push_back({si, (uint32_t)lead, 0});
+                k = lead;
+            }
+        }
+        for (; k < n; k += HOSTCOPY_CHUNK)
             chunks.push_back({si, (uint32_t)std::min<uint64_t>(HOSTCOPY_CHUNK, n - k), k});
     }
     // n beads' vectors (3 doubles each): a packed array (stride 24) as one run of words, a

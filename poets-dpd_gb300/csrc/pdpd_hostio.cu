@@ -72,21 +72,27 @@ __global__ void k_slot_of_id(const uint32_t *__restrict__ ids, uint32_t first, u
 
 // The read-back without device staging: a block per tile of bead ids gathers the tile's beads
 // from their sorted slots (random 16- or 32-byte reads in device memory), lays x, v and f out
-// in shared memory in the caller's order, and writes each field as one contiguous run of the
-// caller's array (a stride-24 array; otherwise bead by bead).  The link to the host carries
-// each byte once, in full lines, and the gathers overlap it.  x = cell + offset in FP32 and
-// the FP32 -> FP64 conversions are those of the unsort kernels, so the values are the same.
+// in shared memory in the caller's order, and writes each field of a stride-24 array in whole
+// 128-byte lines of host memory (otherwise bead by bead).  Lines a tile's run shares with the
+// next tile's are written whole by the tile whose run holds the line's first byte, which
+// gathers the few beads of the next tile the line reaches: a line written in parts by two
+// blocks crossed the host link a fifth slower (152 against 193 GB/s for 3 KB runs 8 bytes off
+// the line boundary, on a GB300).  The link carries each byte once and the gathers overlap
+// it.  x = cell + offset in FP32 and the FP32 -> FP64 conversions are those of the unsort
+// kernels, so the values are the same.
+constexpr int LINE_BEADS = 6;  // beads past a tile that a 128-byte line can reach (120 / 24 + 1)
+
 template <int F64>
 __global__ void __launch_bounds__(TILE_BEADS) k_read_direct(KArgs a, const uint32_t *__restrict__ inv,
                                                             const ReadDest *__restrict__ dest)
 {
-    __shared__ double sh[3][3 * TILE_BEADS];
+    __shared__ double sh[3][3 * (TILE_BEADS + LINE_BEADS)];
     for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const Tile tl = a.tiles[tile];
         const WorldDev &w = a.worlds[tl.world];
         const uint32_t cnt = tl.slot_end - tl.slot_begin;
-        const uint32_t t = threadIdx.x;
-        if (t < cnt) {
+        const uint32_t extra = min((uint32_t)LINE_BEADS, w.bead_base + w.n_beads - tl.slot_end);
+        for (uint32_t t = threadIdx.x; t < cnt + extra; t += TILE_BEADS) {
             const uint32_t s = inv[tl.slot_begin + t];
             double x[3], v[3], f[3];
             if (F64) {
@@ -123,13 +129,26 @@ __global__ void __launch_bounds__(TILE_BEADS) k_read_direct(KArgs a, const uint3
         for (int q = 0; q < 3; q++) {
             if (!out[q]) continue;
             if (D.stride == 24) {
-                double *o = out[q] + 3 * k0;
-                for (uint32_t i = t; i < 3 * cnt; i += TILE_BEADS) o[i] = sh[q][i];
-            } else if (t < cnt) {
-                double *o = (double *)((char *)out[q] + (k0 + t) * D.stride);
-                o[0] = sh[q][3 * t];
-                o[1] = sh[q][3 * t + 1];
-                o[2] = sh[q][3 * t + 2];
+                // the doubles [i0, i1) of the array this tile writes: from the first line boundary
+                // in its run (the array's start for its first tile) to the end of the line that
+                // holds its run's last byte, within the array
+                const uintptr_t A = (uintptr_t)out[q];
+                const uintptr_t run0 = A + 24 * k0, run1 = A + 24 * (k0 + cnt);
+                const uintptr_t end = A + 24 * (uintptr_t)w.n_beads;
+                const uintptr_t w0 = k0 == 0 ? A : (run0 + 127) & ~(uintptr_t)127;
+                const uintptr_t w1 = min((run1 + 127) & ~(uintptr_t)127, end);
+                if (w1 > w0) {
+                    const uint32_t i0 = (uint32_t)((w0 - A) / 8 - 3 * k0), n = (uint32_t)((w1 - w0) / 8);
+                    double *o = (double *)w0;
+                    for (uint32_t i = threadIdx.x; i < n; i += TILE_BEADS) o[i] = sh[q][i0 + i];
+                }
+            } else {
+                for (uint32_t t = threadIdx.x; t < cnt; t += TILE_BEADS) {
+                    double *o = (double *)((char *)out[q] + (k0 + t) * D.stride);
+                    o[0] = sh[q][3 * t];
+                    o[1] = sh[q][3 * t + 1];
+                    o[2] = sh[q][3 * t + 2];
+                }
             }
         }
         __syncthreads();
