@@ -1017,49 +1017,27 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
     }
     e->reset();
     char reason[256];
-    uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
-    {  // the worlds' checks (each scans its beads), in parallel; the first failure is reported
-        std::vector<int> wrc(n_worlds, PDPD_OK);
-        std::vector<std::string> why(n_worlds);
-        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
-            for (size_t i = i0; i < i1; i++) {
-                char r[256];
-                const bool kept = keep_old && keep_old[i] >= 0;
-                wrc[i] = check_world(&ws[i], r, sizeof r, !kept);
-                if (wrc[i]) why[i] = r;
-            }
-        });
-        for (uint32_t i = 0; i < n_worlds; i++)
-            if (wrc[i]) return e->fail(wrc[i], "world %u: %s", i, why[i].c_str());
-    }
-    (void)reason;
-    for (uint32_t i = 0; i < n_worlds; i++) {
-        nb += ws[i].n_beads;
-        nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
-        n_pair += (uint64_t)ws[i].n_bead_types * ws[i].n_bead_types;
-        n_terms += 2ull * ws[i].n_bonds + 3ull * ws[i].n_angles;
-        n_bparams += ws[i].n_bonds + ws[i].n_angles;
-    }
-    if (nb >= (1ull << 31) || nc >= (1ull << 31) || n_terms >= (1ull << 32))
-        return e->fail(PDPD_E_UNSUPPORTED, "batch too large (%llu beads, %llu cells, %llu bond terms)",
-                       (unsigned long long)nb, (unsigned long long)nc, (unsigned long long)n_terms);
-    e->n_beads = (uint32_t)nb;
-    e->n_cells = (uint32_t)nc;
-
     // With direct host copies (a whole batch from its descriptors, in arrays the copy kernel
     // may access) the kernel brings the beads field-major into device staging 0 and the
     // hashes, launched now so that the transfer runs while the host builds the tables below.
     // In a re-pack the kept worlds' rows come from the old arena (below) and the kernel brings
     // only the new worlds', into rows of 9 doubles (x, v, f) like theirs.
-    bool direct = e->host_direct();
+    // (Launched before the worlds' checks, which scan every bead: it needs only the arrays'
+    // presence and alignment and the bead counts, checked here; a batch that then fails a
+    // check waits for the copy, which only reads, before the error returns.)
+    uint64_t nb_direct = 0;
+    for (uint32_t i = 0; i < n_worlds; i++) nb_direct += ws[i].n_beads;
+    bool direct = e->host_direct() && nb_direct < (1ull << 31);
     for (uint32_t i = 0; direct && i < n_worlds; i++) {
         const pdpd_world &w = ws[i];
         if (any_kept && keep_old[i] >= 0) continue;
         const size_t sb = w.bead_stride_bytes ? w.bead_stride_bytes : 3 * sizeof(double);
-        direct = vec_ok(w.x, sb) && vec_ok(w.v, sb) && vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
+        direct = (w.n_beads == 0 || (w.x && w.v && w.f && w.hash)) && vec_ok(w.x, sb) && vec_ok(w.v, sb) &&
+                 vec_ok(w.f, sb) && ((uintptr_t)w.hash & 3u) == 0;
     }
     const bool field_major = direct && !any_kept;  // the layout of device staging 0 for the bin
     if (direct) {
+        const uint64_t nb = nb_direct;
         if (e->d_staging[0].alloc(sizeof(double) * 9 * nb) != cudaSuccess ||
             e->d_hash.alloc(sizeof(uint32_t) * std::max<uint64_t>(1, nb)) != cudaSuccess) {
             cudaGetLastError();
@@ -1093,6 +1071,40 @@ static int attach_impl(pdpd_engine *e, const pdpd_world *ws, uint32_t n_worlds, 
             return rc;
         }
     }
+
+    uint64_t nb = 0, nc = 0, n_pair = 0, n_terms = 0, n_bparams = 0;
+    {  // the worlds' checks (each scans its beads), in parallel; the first failure is reported
+        std::vector<int> wrc(n_worlds, PDPD_OK);
+        std::vector<std::string> why(n_worlds);
+        parallel_for(n_worlds, 1, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; i++) {
+                char r[256];
+                const bool kept = keep_old && keep_old[i] >= 0;
+                wrc[i] = check_world(&ws[i], r, sizeof r, !kept);
+                if (wrc[i]) why[i] = r;
+            }
+        });
+        for (uint32_t i = 0; i < n_worlds; i++)
+            if (wrc[i]) {
+                cudaStreamSynchronize(e->stream);  // (the direct copy reads the caller's arrays)
+                return e->fail(wrc[i], "world %u: %s", i, why[i].c_str());
+            }
+    }
+    (void)reason;
+    for (uint32_t i = 0; i < n_worlds; i++) {
+        nb += ws[i].n_beads;
+        nc += (uint64_t)ws[i].box[0] * ws[i].box[1] * ws[i].box[2];
+        n_pair += (uint64_t)ws[i].n_bead_types * ws[i].n_bead_types;
+        n_terms += 2ull * ws[i].n_bonds + 3ull * ws[i].n_angles;
+        n_bparams += ws[i].n_bonds + ws[i].n_angles;
+    }
+    if (nb >= (1ull << 31) || nc >= (1ull << 31) || n_terms >= (1ull << 32)) {
+        cudaStreamSynchronize(e->stream);
+        return e->fail(PDPD_E_UNSUPPORTED, "batch too large (%llu beads, %llu cells, %llu bond terms)",
+                       (unsigned long long)nb, (unsigned long long)nc, (unsigned long long)n_terms);
+    }
+    e->n_beads = (uint32_t)nb;
+    e->n_cells = (uint32_t)nc;
 
     // --- world table, tiles, pair table
     std::vector<Tile> tiles;
