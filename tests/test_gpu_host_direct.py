@@ -138,3 +138,49 @@ def test_read_back_into_fresh_arrays():
     assert got[0][0] == got[1][0]
     for a, b in zip(got[0][1:], got[1][1:]):
         assert np.array_equal(a, b)
+
+
+def _ragged_world(n, seed, offset_arrays=False):
+    """A water-like world of exactly n beads (n from 1 up), optionally with x, v, f held 8 bytes
+    into a larger buffer (8-byte but not 16-byte aligned arrays)."""
+    rng = np.random.default_rng(seed)
+    L = np.array([6, 5, 7], np.int32)
+    x = rng.random((n, 3)) * L[None, :]
+    v = rng.standard_normal((n, 3))
+    w = W._assemble_monomer_world(L, x, v, np.array([[25.0]]), np.array([[4.5]]), 0.02, seed, 0, 1)
+    if offset_arrays:
+        for k in ("x", "v", "f"):
+            buf = np.empty(3 * n + 1)
+            a = buf[1:].reshape(n, 3)
+            a[:] = getattr(w, k)
+            setattr(w, k, a)
+    return w
+
+
+RAGGED = [1, 5, 7, 24, 127, 128, 129, 133, 134, 255, 262, 1000]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_ragged_worlds_and_misaligned_arrays_direct_equals_staged(precision):
+    """Worlds of 1 to 1000 beads (tile tails and the lines a tile shares with the next), some
+    with arrays 8 bytes off a 16-byte boundary: the read-back kernel writes whole 128-byte
+    lines, so these are its edge cases.  Every world read back at once and one at a time."""
+    def make():
+        return [_ragged_world(n, 100 + i, offset_arrays=bool(i % 2)) for i, n in enumerate(RAGGED)]
+    out = {}
+    for direct in (0, 1):
+        ws = make()
+        eng = _engine(precision, direct)
+        eng.AttachBatch(ws)
+        eng.Run(3)  # every world read back into its own arrays
+        singles = [eng.read_state(i) for i in (0, 5, 7, len(RAGGED) - 1)]
+        out[direct] = (ws, singles)
+    (ws0, s0), (ws1, s1) = out[0], out[1]
+    for a, b in zip(ws0, ws1):
+        assert a.t == b.t
+        assert np.array_equal(a.x, b.x) and np.array_equal(a.v, b.v) and np.array_equal(a.f, b.f)
+    for (i, (a, b)) in zip((0, 5, 7, len(RAGGED) - 1), zip(s0, s1)):
+        assert a[3] == b[3] == ws1[i].t
+        for q in range(3):
+            assert np.array_equal(a[q], b[q])
+            assert np.array_equal(b[q], (ws1[i].x, ws1[i].v, ws1[i].f)[q])
