@@ -1,10 +1,11 @@
-// The attach's upload and the read-backs as one kernel that reads and writes the caller's host
-// arrays directly, on devices that access pageable host memory coherently through the host's
-// page tables (Grace-Blackwell: the GPU reaches the Grace CPU's memory over NVLink-C2C with
-// address translation services).  The staged alternative copies every byte on the host twice
-// (the caller's arrays to pinned staging, or back) around the DMA, so host memory bandwidth,
-// not the link, bounds it; here the link carries each byte once and the host's cores do
-// nothing.  The kernel touches exactly the host addresses the staged copies touch.
+// The attach's upload (k_host_copy) and the read-backs (k_slot_of_id + k_read_direct) as
+// kernels that read and write the caller's host arrays directly, on devices that access
+// pageable host memory coherently through the host's page tables (Grace-Blackwell: the GPU
+// reaches the Grace CPU's memory over NVLink-C2C with address translation services).  The
+// staged alternative copies every byte on the host twice (the caller's arrays to pinned
+// staging, or back) around the DMA, so host memory bandwidth, not the link, bounds it; here
+// the link carries each byte once and the host's cores do nothing.  The kernels touch exactly
+// the host bytes the staged copies touch, and run at the link's DMA rate.
 #include <algorithm>
 
 #include "pdpd_device.cuh"
