@@ -584,7 +584,7 @@ def force_roofline(phases, beads, precision, traffic_key=None):
     force_ms = phases["force_ms"] / max(1, phases["force_launches"])
     peak, peak_kind = measured_peaks()
     achieved = ALGO_BYTES[precision] * beads / (force_ms / 1e3) / 1e9
-    traffic = instr = None
+    traffic = instr = pipes = None
     tpath = os.path.join(ROOT, "profiles", "force_kernel_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
@@ -594,6 +594,7 @@ def force_roofline(phases, beads, precision, traffic_key=None):
             traffic = tj[f"{key}_bytes_per_bead_step"] * beads
         if f"{key}_warp_instructions_per_bead_step" in tj:
             instr = tj[f"{key}_warp_instructions_per_bead_step"]
+        pipes = tj.get(f"{key}_pipes")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "kernel": "force", "kernel_ms": force_ms,
             "algo_bytes_per_bead_step": ALGO_BYTES[precision], "peak_source": peak_kind,
@@ -608,6 +609,9 @@ def force_roofline(phases, beads, precision, traffic_key=None):
         cap = ISSUE_SLOTS_PER_S
         roof["issue"] = {"warp_instructions_per_bead_step": instr, "slots_per_s": cap,
                          "frac": instr * beads / (force_ms / 1e3) / cap}
+    if pipes is not None:
+        # FP32 (FMA) and integer (ALU) pipe utilisation of the kernel, from its ncu capture
+        roof["pipes"] = dict(pipes, source="ncu --set full of one launch (profiles/)")
     ph = {"force": force_ms, "sort": phases["sort_ms"] / max(1, phases["sort_launches"])}
     return roof, ph
 
