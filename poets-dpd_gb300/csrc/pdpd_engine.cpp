@@ -1533,12 +1533,14 @@ void *pdpd_stream(pdpd_engine *e)
 static int download(pdpd_engine *e, int buf, cudaStream_t s, bool fields = false)
 {
     KArgs a = e->args;
-    if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess)
+    if (e->d_staging[buf].alloc(sizeof(double) * 9 * (size_t)e->n_beads) != cudaSuccess ||
+        e->d_inv.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, e->n_beads)) != cudaSuccess)
         return e->fail(PDPD_E_NOMEM, "staging allocation failed");
     a.staging = e->d_staging[buf].as<double>();
     a.staging_fields = fields ? 1u : 0u;
     a.staging_n = e->n_beads;
-    e->launches += e->fp64() ? launch_unsort64(a, s, 0, e->n_beads) : launch_unsort32(a, s);
+    e->launches += launch_slot_of_id(a, 0, e->n_beads, e->d_inv.as<uint32_t>(), s);
+    e->launches += launch_unsort(a, e->fp64(), e->d_inv.as<uint32_t>(), s);
     return PDPD_OK;
 }
 
@@ -1559,7 +1561,10 @@ static int download_world(pdpd_engine *e, int buf, uint32_t world, cudaStream_t 
     a.grid_blocks = (int)std::min<uint32_t>((uint32_t)std::max(1, e->args.grid_blocks), a.n_tiles);
     a.staging = e->d_staging[buf].as<double>();
     const WorldDev &wd = e->worlds[world].dev;
-    e->launches += e->fp64() ? launch_unsort64(a, s, wd.bead_base, wd.n_beads) : launch_unsort32(a, s);
+    if (e->d_inv.alloc(sizeof(uint32_t) * std::max<uint32_t>(1, e->n_beads)) != cudaSuccess)
+        return e->fail(PDPD_E_NOMEM, "staging allocation failed");
+    e->launches += launch_slot_of_id(a, wd.bead_base, wd.n_beads, e->d_inv.as<uint32_t>(), s);
+    e->launches += launch_unsort(a, e->fp64(), e->d_inv.as<uint32_t>(), s);
     return PDPD_OK;
 }
 

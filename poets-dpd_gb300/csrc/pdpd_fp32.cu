@@ -804,34 +804,6 @@ __global__ void k_finish32(KArgs a)
         for (uint32_t w = threadIdx.x; w < a.n_worlds; w += blockDim.x) a.worlds[w].t += 1;
 }
 
-// Rest state -> id-ordered FP64 staging (x, v, f): x = cell + offset exactly.
-__global__ void __launch_bounds__(TILE_BEADS) k_unsort32(KArgs a)
-{
-    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
-        const Tile tl = a.tiles[tile];
-        const uint32_t s = tl.slot_begin + threadIdx.x;
-        if (s >= tl.slot_end) continue;
-        const WorldDev &w = a.worlds[tl.world];
-        const float4 p = ((const float4 *)a.posA)[s];
-        const float4 v = ((const float4 *)a.velA)[s];
-        const float4 f = ((const float4 *)a.frc)[s];
-        int c[3];
-        decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
-        // rows of 9 doubles, or field-major blocks (x, v, f) of staging_n beads each
-        const size_t id = a.ids[s];
-        const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
-        double *st = a.staging + stride * id;
-        st[0] = (double)c[0] + (double)p.x;
-        st[1] = (double)c[1] + (double)p.y;
-        st[2] = (double)c[2] + (double)p.z;
-        st[field + 0] = v.x;
-        st[field + 1] = v.y;
-        st[field + 2] = v.z;
-        st[2 * field + 0] = f.x;
-        st[2 * field + 1] = f.y;
-        st[2 * field + 2] = f.z;
-    }
-}
 
 #include "pdpd_fp32_brick.cuh"
 
@@ -945,12 +917,6 @@ int launch_pair_log32(const KArgs &a, const uint32_t *sel, uint32_t n_sel, const
 int launch_finish32(const KArgs &a, cudaStream_t s)
 {
     k_finish32<<<(a.n_beads + 255) / 256 + 1, 256, 0, s>>>(a);
-    return 1;
-}
-
-int launch_unsort32(const KArgs &a, cudaStream_t s)
-{
-    k_unsort32<<<a.grid_blocks, TILE_BEADS, 0, s>>>(a);
     return 1;
 }
 

@@ -681,29 +681,6 @@ __global__ void k_finish64(KArgs a)
         for (uint32_t w = threadIdx.x; w < a.n_worlds; w += blockDim.x) a.worlds[w].t += 1;
 }
 
-__global__ void k_unsort64(KArgs a, uint32_t first, uint32_t count)
-{
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    const uint32_t s = first + k;
-    const Vec4d p = ((const Vec4d *)a.posA)[s];
-    const Vec4d v = ((const Vec4d *)a.velA)[s];
-    const Vec4d f = ((const Vec4d *)a.frc)[s];
-    const size_t id = a.ids[s];
-    // rows of 9 doubles, or field-major blocks (x, v, f) of staging_n beads each
-    const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
-    double *st = a.staging + stride * id;
-    st[0] = p.x;
-    st[1] = p.y;
-    st[2] = p.z;
-    st[field + 0] = v.x;
-    st[field + 1] = v.y;
-    st[field + 2] = v.z;
-    st[2 * field + 0] = f.x;
-    st[2 * field + 1] = f.y;
-    st[2 * field + 2] = f.z;
-}
-
 }  // namespace
 
 int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s)
@@ -744,13 +721,6 @@ int launch_force64(const KArgs &a, int final_step, cudaStream_t s)
 int launch_finish64(const KArgs &a, cudaStream_t s)
 {
     k_finish64<<<(a.n_beads + 255) / 256 + 1, 256, 0, s>>>(a);
-    return 1;
-}
-
-int launch_unsort64(const KArgs &a, cudaStream_t s, uint32_t first, uint32_t count)
-{
-    if (count == 0) return 0;
-    k_unsort64<<<(count + 255) / 256, 256, 0, s>>>(a, first, count);
     return 1;
 }
 

@@ -156,7 +156,56 @@ __global__ void __launch_bounds__(TILE_BEADS) k_read_direct(KArgs a, const uint3
     }
 }
 
+// The rest state to id-ordered device staging (rows of 9 doubles, or field-major blocks of
+// staging_n beads each), as a gather: a thread per bead id of a tile reads the bead from its
+// sorted slot through inv and writes its row or vectors where consecutive ids are adjacent, so
+// the stores of a warp are contiguous (a scatter from the sorted order writes 24- or 72-byte
+// pieces all over the staging, each a partial write of its sectors).
+template <int F64>
+__global__ void __launch_bounds__(TILE_BEADS) k_unsort_gather(KArgs a, const uint32_t *__restrict__ inv)
+{
+    const size_t stride = a.staging_fields ? 3 : 9, field = a.staging_fields ? 3 * (size_t)a.staging_n : 3;
+    for (uint32_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const Tile tl = a.tiles[tile];
+        const uint32_t id = tl.slot_begin + threadIdx.x;
+        if (id >= tl.slot_end) continue;
+        const uint32_t s = inv[id];
+        double *st = a.staging + stride * id;
+        if (F64) {
+            const Vec4d p = ((const Vec4d *)a.posA)[s];
+            const Vec4d v = ((const Vec4d *)a.velA)[s];
+            const Vec4d f = ((const Vec4d *)a.frc)[s];
+            st[0] = p.x, st[1] = p.y, st[2] = p.z;
+            st[field + 0] = v.x, st[field + 1] = v.y, st[field + 2] = v.z;
+            st[2 * field + 0] = f.x, st[2 * field + 1] = f.y, st[2 * field + 2] = f.z;
+        } else {
+            const WorldDev &w = a.worlds[tl.world];
+            const float4 p = ((const float4 *)a.posA)[s];
+            const float4 v = ((const float4 *)a.velA)[s];
+            const float4 f = ((const float4 *)a.frc)[s];
+            int c[3];
+            decode_cell(a.cellg[s] - w.cell_base, w.L, c[0], c[1], c[2]);
+            st[0] = (double)c[0] + (double)p.x;  // x = cell + offset exactly
+            st[1] = (double)c[1] + (double)p.y;
+            st[2] = (double)c[2] + (double)p.z;
+            st[field + 0] = v.x, st[field + 1] = v.y, st[field + 2] = v.z;
+            st[2 * field + 0] = f.x, st[2 * field + 1] = f.y, st[2 * field + 2] = f.z;
+        }
+    }
+}
+
 }  // namespace
+
+int launch_unsort(const KArgs &a, int fp64, const uint32_t *inv, cudaStream_t s)
+{
+    if (a.n_tiles == 0) return 0;
+    const uint32_t grid = std::min<uint32_t>(a.n_tiles, (uint32_t)std::max(1, a.grid_blocks));
+    if (fp64)
+        k_unsort_gather<1><<<grid, TILE_BEADS, 0, s>>>(a, inv);
+    else
+        k_unsort_gather<0><<<grid, TILE_BEADS, 0, s>>>(a, inv);
+    return 1;
+}
 
 int launch_slot_of_id(const KArgs &a, uint32_t first, uint32_t count, uint32_t *inv, cudaStream_t s)
 {

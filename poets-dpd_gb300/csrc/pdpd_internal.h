@@ -138,18 +138,16 @@ struct KArgs {
 //   force:  A -> B: forces, update_mom and (unless final) the next update_pos with counts;
 //           final: v(t+1) -> B.vel, f(t+1) -> frc
 //   finish: B.vel -> A.vel and t += 1                           (after a final force pass)
-//   unsort: A rest state -> id-ordered staging                  (download)
+//   unsort: A rest state -> id-ordered staging (pdpd_hostio.cu)   (download)
 //   sort:   B -> A counting sort (pdpd_sort.cu)
 int launch_bin32(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
 int launch_begin32(const KArgs &a, cudaStream_t s);
 int launch_force32(const KArgs &a, int final_step, cudaStream_t s);  // includes the bond kernel
 int launch_finish32(const KArgs &a, cudaStream_t s);
-int launch_unsort32(const KArgs &a, cudaStream_t s);
 int launch_bin64(const KArgs &a, const uint32_t *hash_in, cudaStream_t s);
 int launch_begin64(const KArgs &a, cudaStream_t s);
 int launch_force64(const KArgs &a, int final_step, cudaStream_t s);
 int launch_finish64(const KArgs &a, cudaStream_t s);
-int launch_unsort64(const KArgs &a, cudaStream_t s, uint32_t first, uint32_t count);  // sorted slots [first, first + count)
 int launch_sort(const KArgs &a, int fp64, int tick, int with_force, cudaStream_t s);
 
 // One record of the pair log (pdpd_log_pair_terms; the C ABI's pdpd_pair_terms has this
@@ -190,6 +188,10 @@ struct HostCopyChunk {
 constexpr uint32_t HOSTCOPY_CHUNK = 16384;
 int launch_host_copy(const HostCopySeg *segs, const HostCopyChunk *chunks, uint32_t n_chunks, int sm_count,
                      cudaStream_t s);
+// The rest state of the tiles a.tiles[0, a.n_tiles) to id-ordered device staging (a.staging:
+// rows of 9 doubles, or field-major with a.staging_fields), gathered through inv (the slot of
+// each bead id of those tiles, launch_slot_of_id).
+int launch_unsort(const KArgs &a, int fp64, const uint32_t *inv, cudaStream_t s);
 // Direct read-back of the rest state into the callers' host arrays (pdpd_hostio.cu): where
 // world w's x, v, f go (host pointers, null: not read; vectors `stride` bytes apart).
 struct ReadDest {
