@@ -629,9 +629,12 @@ def host_copies(eng):
 
 
 def fixed_kernel(eng, args):
-    """--force-kernel K: run FP32 force kernel K (no autotuning), for profiling a variant."""
+    """--force-kernel K: run FP32 force kernel K (no autotuning), for profiling a variant;
+    --host-direct 0: the host copies through pinned staging and DMA, to measure that path."""
     if args.force_kernel:
         eng.SetConfigEntry("force_kernel", args.force_kernel)
+    if args.host_direct is not None:
+        eng.SetConfigEntry("host_direct", args.host_direct)
 
 
 def tune(eng, attach, steps=64):
@@ -874,6 +877,9 @@ def main():
                     help="1: autotune the FP32 force kernel first (default); 0: default kernel")
     ap.add_argument("--force-kernel", type=int, default=0,
                     help="FP32 force kernel variant to run instead of autotuning (1, 6, 8, 9)")
+    ap.add_argument("--host-direct", type=int, default=None, choices=[0, 1],
+                    help="the engines' host_direct config (default: the engine's own, direct "
+                         "where the device reaches host memory)")
     ap.add_argument("--serving-window", type=float, default=20.0,
                     help="seconds of Poisson arrivals of the serving stream (0 skips it)")
     ap.add_argument("--serving-light-rate", type=float, default=20.0,
