@@ -12,7 +12,7 @@ independent runs, not assumed:
 Each replica or state gives one difference GPU - oracle of its time-averaged observables; they
 are independent, so the standard error of the mean difference is their spread / sqrt(count).
 A difference passes when it is within 5 standard errors, and temperature and pressure also
-within 0.5% and 1% of the oracle's (the benchmark spec's bounds)."""
+within 0.5% and 1% of the oracle's (the engine's stated bounds for those two)."""
 
 import numpy as np
 import pytest
