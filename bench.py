@@ -808,7 +808,7 @@ def run_engine_arm(args):
     serving = serving_light = None
     if args.serving_window > 0 and world_size == 1:
         serving = serving_metrics(window_s=args.serving_window, device=local)
-    if args.serving_light_rate > 0 and args.serving_window > 0 and world_size == 1:
+    if args.serving_light_rate > 0 and args.serving_light_window > 0 and args.serving_window > 0 and world_size == 1:
         # the same job mix offered below the server's capacity: latency without a standing queue
         serving_light = serving_metrics(rate=args.serving_light_rate, window_s=args.serving_light_window,
                                         seed=6, device=local, seq_fp32=0, seq_fp64=0)
